@@ -1,0 +1,310 @@
+"""Seeded synthetic RT problems and hp meshes.
+
+Each problem is the five callables the reference's ``rt.Problem`` takes
+(rt/class_Problem.py:12-23): kappa(x, y) (total extinction), sigma(x, y)
+(scattering), Phi(th, phi), f(x, y, th), and ``bcs_dirac = [bcs, dirac]``.
+Coefficient callables accept numpy arrays (broadcasting) and scalars.
+
+The mesh recipes only call ``Mesh(...)``, ``ref_mesh``, ``ref_col`` and
+``ref_cell``, so the same recipe applied to the reference's ``dg.mesh.Mesh``
+produces the same mesh.
+
+The Henyey-Greenstein phase function is the one the reference's experiment
+drivers supply (experiments/two-strong-scatterers/problem.py:36-43):
+Phi(th, phi) = (1 - g^2) / N_g / (1 + g^2 - 2 g cos(th - phi))^(3/2), with N_g
+its integral over [0, 2 pi] computed by adaptive quadrature to 1e-9.
+"""
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from .mesh import Mesh
+
+PI = math.pi
+
+
+@dataclass
+class RTProblemSpec:
+    name: str
+    kappa: Callable
+    sigma: Callable
+    Phi: Callable
+    f: Callable
+    bcs_dirac: list
+    u_exact: Optional[Callable] = None
+    meta: dict = field(default_factory=dict)
+
+
+def _quad(fn, a, b):
+    from scipy.integrate import quad
+    val, _ = quad(fn, a, b, epsabs=1.e-9, epsrel=1.e-9, limit=100, maxp1=100)
+    return val
+
+
+def hg_phase(g):
+    """Reference-normalised HG kernel with exponent 3/2 (see module docstring)."""
+    g = float(g)
+    norm = _quad(lambda d: (1. - g ** 2) / (1 + g ** 2 - 2. * g * np.cos(d)) ** (3. / 2.),
+                 0., 2. * PI)
+
+    def Phi(th, phi):
+        return ((1. - g ** 2) / norm) / (1 + g ** 2 - 2. * g * np.cos(th - phi)) ** (3. / 2.)
+
+    Phi.g = g
+    Phi.norm = norm
+    return Phi
+
+
+# ----------------------------------------------------------------- problems
+def manufactured_problem(Lx=1., Ly=1., sigma_t=1.1, sigma_s=0.5, g=0.8, width=0.05):
+    """u = exp(-((x-Lx/2)^2 + (y-Ly/2)^2)/width) (1 + cos(th)/2), constant
+    coefficients; f = s.grad u + sigma_t u - sigma_s int Phi u dth', inflow data u.
+
+    int_0^{2pi} Phi(th, th') (1 + cos th'/2) dth' = 1 + (c1/2) cos th with
+    c1 = int Phi(0, d) cos d dd, because Phi integrates to one and depends on
+    th - th' only."""
+    Phi = hg_phase(g)
+    c1 = _quad(lambda d: Phi(0., d) * np.cos(d), 0., 2. * PI)
+    xc, yc = Lx / 2., Ly / 2.
+
+    def X(x, y):
+        return np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / width)
+
+    def u(x, y, th):
+        return X(x, y) * (1. + 0.5 * np.cos(th))
+
+    def kappa(x, y):
+        return sigma_t + 0. * (x + y)
+
+    def sigma(x, y):
+        return sigma_s + 0. * (x + y)
+
+    def f(x, y, th):
+        Xv = X(x, y)
+        dX = -2. * Xv / width
+        Th = 1. + 0.5 * np.cos(th)
+        prop = (np.cos(th) * (x - xc) + np.sin(th) * (y - yc)) * dX * Th
+        return prop + sigma_t * Xv * Th - sigma_s * Xv * (1. + 0.5 * c1 * np.cos(th))
+
+    def bcs(x, y, th):
+        return u(x, y, th)
+
+    return RTProblemSpec("manufactured", kappa, sigma, Phi, f, [bcs, [None, None, None]],
+                         u_exact=u, meta={"g": g, "c1": c1})
+
+
+def smooth_variable_problem(Lx=1., Ly=1., g=0.6):
+    """Variable kappa/sigma, smooth forcing and inflow data (no exact solution);
+    exercises every operator term with non-constant coefficients."""
+    Phi = hg_phase(g)
+
+    def kappa(x, y):
+        return 1.5 + 0.5 * np.sin(PI * x / Lx) * np.cos(PI * y / Ly)
+
+    def sigma(x, y):
+        return 0.6 * kappa(x, y)
+
+    def f(x, y, th):
+        return (1. + x * y) * (1. + 0.3 * np.sin(th) + 0.2 * np.cos(2. * th))
+
+    def bcs(x, y, th):
+        return np.exp(-x) * (1. + 0.5 * np.cos(th - 0.3)) + 0.1 * y
+
+    return RTProblemSpec("smooth_variable", kappa, sigma, Phi, f, [bcs, [None, None, None]],
+                         meta={"g": g})
+
+
+def gaussian_bump_problem(Lx=3., Ly=2., amp=0.9, width=0.15, xc=1.5, yc=1.0, g=0.9):
+    """Single adaptive problem: sigma_s = amp exp(-r^2 / (2 width^2)) centred at
+    (xc, yc), sigma_t = sigma_s + 0.01, isotropic inflow 1 on x = 0 for
+    th in (-pi/4, pi/4), zero elsewhere, no interior source."""
+    Phi = hg_phase(g)
+
+    def sigma(x, y):
+        return amp * np.exp(-((x - xc) ** 2 + (y - yc) ** 2) / (2. * width ** 2))
+
+    def kappa(x, y):
+        return sigma(x, y) + 0.01
+
+    def f(x, y, th):
+        return 0. * (x + y + th)
+
+    def bcs(x, y, th):
+        x = np.asarray(x, dtype=float)
+        th = np.asarray(th, dtype=float)
+        beam = (th < PI / 4.) | (th > 7. * PI / 4.)
+        return np.where((x == 0.) & beam, 1., 0.)
+
+    return RTProblemSpec("gaussian_bump", kappa, sigma, Phi, f, [bcs, [None, None, None]],
+                         meta={"g": g})
+
+
+def two_disc_problem(Lx=2., Ly=2., g=0.95):
+    """Two strong scatterers: discs of radius 0.2 at (0.6, 0.6) and (1.4, 1.4)
+    with sigma_s = 50, sigma_t = 50.1 inside; background sigma_t = 0.1,
+    sigma_s = 0.01; beam inflow on y = 0 for |x - 1| < 0.25, |th - pi/2| < pi/8."""
+    Phi = hg_phase(g)
+    discs = ((0.6, 0.6), (1.4, 1.4))
+    rad = 0.2
+
+    def inside(x, y):
+        x = np.asarray(x, dtype=float)
+        y = np.asarray(y, dtype=float)
+        m = np.zeros(np.broadcast(x, y).shape, dtype=bool)
+        for (cx, cy) in discs:
+            m |= ((x - cx) ** 2 + (y - cy) ** 2) <= rad ** 2
+        return m
+
+    def kappa(x, y):
+        return np.where(inside(x, y), 50.1, 0.1)
+
+    def sigma(x, y):
+        return np.where(inside(x, y), 50., 0.01)
+
+    def f(x, y, th):
+        return 0. * (x + y + th)
+
+    def bcs(x, y, th):
+        x = np.asarray(x, dtype=float)
+        y = np.asarray(y, dtype=float)
+        th = np.asarray(th, dtype=float)
+        on = (y == 0.) & (np.abs(x - 1.) < 0.25) & (np.abs(th - PI / 2.) < PI / 8.)
+        return np.where(on, 1., 0.)
+
+    return RTProblemSpec("two_disc", kappa, sigma, Phi, f, [bcs, [None, None, None]],
+                         meta={"g": g, "discs": discs, "radius": rad})
+
+
+def gaussian_source_problem(sigma_t, ratio, g, Lx=1., Ly=1., xs=0.5, ys=0.5, ws=0.1):
+    """Batched instance: constant sigma_t, sigma_s = ratio * sigma_t, Gaussian
+    isotropic source at (xs, ys), vacuum inflow."""
+    Phi = hg_phase(g)
+
+    def kappa(x, y):
+        return sigma_t + 0. * (x + y)
+
+    def sigma(x, y):
+        return ratio * sigma_t + 0. * (x + y)
+
+    def f(x, y, th):
+        return np.exp(-((x - xs) ** 2 + (y - ys) ** 2) / ws ** 2) + 0. * th
+
+    def bcs(x, y, th):
+        return 0. * (x + y + th)
+
+    return RTProblemSpec("gaussian_source", kappa, sigma, Phi, f, [bcs, [None, None, None]],
+                         meta={"g": g, "sigma_t": sigma_t, "ratio": ratio})
+
+
+# -------------------------------------------------------------- mesh recipes
+def uniform_mesh(Ls, n, nref_ang, nref_spt, mesh_cls=Mesh, pbcs=(False, False)):
+    """``Mesh(Ls, pbcs, [n, n, n])`` refined uniformly ``nref_ang`` times in angle
+    then ``nref_spt`` times in space (experiments/manufactured-solution/mesh.py:18-28)."""
+    mesh = mesh_cls(list(Ls), list(pbcs), [n, n, n], True)
+    for _ in range(nref_ang):
+        mesh.ref_mesh(kind="ang", form="h")
+    for _ in range(nref_spt):
+        mesh.ref_mesh(kind="spt", form="h")
+    return mesh
+
+
+def config1_mesh(mesh_cls=Mesh):
+    """[0,1]^2, 4x4 columns x 4 angular cells, 4 nodes per dimension (4096 DOF)."""
+    return uniform_mesh([1., 1.], 4, 2, 2, mesh_cls)
+
+
+def hanging_hp_mesh(mesh_cls=Mesh):
+    """The scripted refinement sequence of the reference's mesh test
+    (tests/test_dg/test_mesh/test_Mesh.py:40-66): non-conforming spatial and
+    angular neighbours with mixed degrees."""
+    mesh = mesh_cls([1., 2.], [False, False], [2, 3, 4], True)
+    for ck, kind, form in zip([0, 0, 0, 1, 10, 48], ["ang", "ang", "spt", "spt", "spt", "spt"],
+                              ["h", "h", "h", "h", "hp", "hp"]):
+        mesh.ref_col(col_key=ck, kind=kind, form=form)
+    for kk, form in zip([3, 7, 15], ["h", "hp", "hp"]):
+        mesh.ref_cell(col_key=204, cell_key=kk, form=form)
+    return mesh
+
+
+def quadrant_free_mesh(mesh_cls=Mesh):
+    """Two angular cells per column ([0, pi], [pi, 2 pi]): cells outside any
+    single quadrant, so no face is treated as outflow for them."""
+    mesh = mesh_cls([1., 1.], [False, False], [3, 3, 2], True)
+    mesh.ref_mesh(kind="ang", form="h")
+    mesh.ref_mesh(kind="spt", form="h")
+    mesh.ref_mesh(kind="spt", form="h")
+    mesh.ref_col(col_key=sorted(mesh.cols.keys())[5], kind="spt", form="p")
+    return mesh
+
+
+def periodic_mesh(mesh_cls=Mesh):
+    """Periodic in x, vacuum-bounded in y."""
+    mesh = mesh_cls([1., 1.], [True, False], [3, 3, 3], True)
+    mesh.ref_mesh(kind="ang", form="h")
+    mesh.ref_mesh(kind="ang", form="h")
+    mesh.ref_mesh(kind="spt", form="h")
+    return mesh
+
+
+def random_hp_mesh(Ls, n0, nth0, rounds, seed, frac_spt=0.3, frac_ang=0.2,
+                   p_prob=0.4, n_max=7, nref_ang=2, nref_spt=2, mesh_cls=Mesh,
+                   ndof_cap=None):
+    """Seeded random hp refinement: start from a uniform mesh, then for each
+    round pick leaf columns to refine in space (h or p) and leaf cells to refine
+    in angle (h or p), with ``numpy.random.default_rng(seed)``.  Refinement
+    goes through the mesh's own ``ref_col``/``ref_cell`` (2:1 balance kept).
+    Degrees are capped at ``n_max`` nodes; ``ndof_cap`` stops early."""
+    rng = np.random.default_rng(seed)
+    mesh = mesh_cls(list(Ls), [False, False], [n0, n0, nth0], True)
+    for _ in range(nref_ang):
+        mesh.ref_mesh(kind="ang", form="h")
+    for _ in range(nref_spt):
+        mesh.ref_mesh(kind="spt", form="h")
+    for _ in range(rounds):
+        keys = sorted(mesh.cols.keys())
+        pick = rng.random(len(keys)) < frac_spt
+        forms = rng.random(len(keys)) < p_prob
+        for ck, pk, pf in zip(keys, pick, forms):
+            if not pk or ck not in mesh.cols:
+                continue
+            col = mesh.cols[ck]
+            if pf and col.ndofs[0] < n_max:
+                mesh.ref_col(ck, kind="spt", form="p")
+            elif not pf:
+                mesh.ref_col(ck, kind="spt", form="h")
+        keys = sorted(mesh.cols.keys())
+        for ck in keys:
+            if ck not in mesh.cols:
+                continue
+            ckeys = sorted(mesh.cols[ck].cells.keys())
+            pick = rng.random(len(ckeys)) < frac_ang
+            forms = rng.random(len(ckeys)) < p_prob
+            for kk, pk, pf in zip(ckeys, pick, forms):
+                if not pk or ck not in mesh.cols or kk not in mesh.cols[ck].cells:
+                    continue
+                cell = mesh.cols[ck].cells[kk]
+                if pf and cell.ndofs[0] < n_max:
+                    mesh.ref_cell(ck, kk, form="p")
+                elif not pf and cell.lv < 6:
+                    mesh.ref_cell(ck, kk, form="h")
+        if ndof_cap is not None and mesh.get_ndof() >= ndof_cap:
+            break
+    return mesh
+
+
+def small_random_mesh(mesh_cls=Mesh, seed=3):
+    """A few thousand DOF of random hp refinement on [0,3]x[0,2]."""
+    return random_hp_mesh([3., 2.], 2, 3, rounds=3, seed=seed, frac_spt=0.35,
+                          frac_ang=0.3, n_max=5, nref_ang=2, nref_spt=1,
+                          mesh_cls=mesh_cls)
+
+
+def config2_mesh(mesh_cls=Mesh, seed=0):
+    """Single adaptive problem mesh: [0,3]x[0,2], six rounds of seeded random
+    hp refinement, nodes per dimension in [3, 7] (degree 2..6), about 2e5 DOF."""
+    return random_hp_mesh([3., 2.], 3, 3, rounds=6, seed=seed, frac_spt=0.22,
+                          frac_ang=0.12, p_prob=0.45, n_max=7, nref_ang=2,
+                          nref_spt=2, mesh_cls=mesh_cls)
