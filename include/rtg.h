@@ -1,0 +1,191 @@
+/*
+ * rtg.h -- C ABI of the GB300 radiative-transfer DG solve (librtg.so).
+ *
+ * The library applies the reference's steady monochromatic RT system
+ *     A = (BC - IC) + (M - S)
+ * matrix-free on one GPU and solves the interior/inflow split system of
+ * rt/solve.py:81-132 with device-resident Krylov methods.  All entry points
+ * take plain pointers and sizes; no exceptions cross the ABI.  Every function
+ * returns RTG_OK (0) or a positive error code; rtg_last_error() gives the
+ * message of the calling thread's last failure.  Vectors passed as "device"
+ * live in GPU memory in the reference's global DOF order (sorted column keys,
+ * sorted cell keys, beta = nth*ny*i + nth*j + a: dg/matrix/get_idxs.py:11-80).
+ *
+ * Reference interfaces replaced (src/ of jasonltorchinsky/radiative-transfer-amr):
+ *   rtg_create            -- the per-call mesh walks of every rt builder
+ *                            (rt/mass_matrix.py:23-106 and siblings); the mesh
+ *                            arrives flattened (dg/mesh/class_Mesh.py:12-61)
+ *   rtg_apply             -- rt.Problem.mass_matrix / scattering_matrix /
+ *                            preconditioner_matrix / interior_convection_matrix /
+ *                            boundary_convection_matrix followed by Mat.mult
+ *                            (rt/mass_matrix.py:23, rt/scattering_matrix.py:22,
+ *                            rt/preconditioner_matrix.py:22,
+ *                            rt/interior_convection_matrix.py:25,
+ *                            rt/boundary_convection_matrix.py:27)
+ *   rtg_interior_mask     -- dg.matrix.get_intr_mask (dg/matrix/get_masks.py:22-129)
+ *   rtg_split_vector /    -- dg.matrix.split_vector / merge_vectors
+ *   rtg_merge_vectors        (dg/matrix/split_vector.py:15-48, merge_vectors.py:14-56)
+ *   rtg_weight_forcing    -- the quadrature weighting of rt.Problem.forcing_vector
+ *                            (rt/forcing_vector.py:103-155)
+ *   rtg_solve             -- rt.Problem.solve (rt/solve.py:21-149)
+ *   rtg_quad_nodes        -- dg.quadrature.quad_xyth (dg/quadrature/quad_xyth.py:22-86)
+ */
+#ifndef RTG_H
+#define RTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTG_ABI_VERSION 1
+
+/* status codes */
+#define RTG_OK            0
+#define RTG_ERR_ARG       1  /* bad argument (null pointer, size, flag) */
+#define RTG_ERR_MESH      2  /* mesh description inconsistent */
+#define RTG_ERR_CUDA      3  /* CUDA runtime error */
+#define RTG_ERR_TIMEOUT   4  /* a bounded device wait gave up */
+#define RTG_ERR_NONFINITE 5  /* NaN/Inf in an input or iterate */
+#define RTG_ERR_SIZE      6  /* request exceeds a stated maximum */
+
+/* rtg_apply component flags.  A plain combination adds the selected
+ * reference matrices; RTG_SYSTEM selects A = (BC - IC) + (M - S) with the
+ * (M - S) block and its |entry| <= 1e-14 drop rule taken from
+ * rt/preconditioner_matrix.py:363-514. */
+#define RTG_MASS      1u   /* + M   (rt/mass_matrix.py:108-180)                     */
+#define RTG_SCAT      2u   /* + S   (reference sign: entries <= 0,
+                                      rt/scattering_matrix.py:106-247)              */
+#define RTG_IC        4u   /* + IC  (rt/interior_convection_matrix.py:110-250)      */
+#define RTG_BC        8u   /* + BC  (rt/boundary_convection_matrix.py:160-540)      */
+#define RTG_SYSTEM   16u   /* BC - IC + (M - S)                                      */
+#define RTG_MASK_ROWS 32u  /* zero the rows of inflow-boundary DOFs in the output   */
+
+/* precisions of rtg_apply / solver inner iterations */
+#define RTG_FP64 0
+#define RTG_FP32 1
+
+typedef struct rtg_handle rtg_handle;
+
+/* Flattened hp mesh.  Columns in sorted-key order; elements (leaf cells) in
+ * global order: for each column, its cells in sorted-key order. */
+typedef struct rtg_mesh_desc {
+    int32_t ncols;
+    int32_t nelem;
+    const double*  col_pos;        /* [ncols*4] x0, y0, x1, y1                      */
+    const int32_t* col_ndofs;      /* [ncols*2] nx, ny (nodes per direction)        */
+    const int32_t* col_lv;         /* [ncols]   spatial refinement level            */
+    const int32_t* col_nbr;        /* [ncols*8] neighbour column index per face F
+                                      (0 right, 1 top, 2 left, 3 bottom) and slot
+                                      (2 per face), -1 for none                      */
+    const int32_t* col_elem_start; /* [ncols+1] first element of each column        */
+    const double*  cell_pos;       /* [nelem*2] th0, th1                            */
+    const int32_t* cell_ndof;      /* [nelem]   nth                                 */
+    const int32_t* cell_lv;        /* [nelem]   angular refinement level            */
+    const int32_t* cell_idx;       /* [nelem]   angular index at that level         */
+    const int32_t* cell_quadrant;  /* [nelem]   0..3, or -1 for none                */
+} rtg_mesh_desc;
+
+/* Coefficients sampled at the nodes.  kappa/sigma: per column, nx*ny values at
+ * (x_i, y_j), index i*ny + j, columns concatenated in order.  Phi: per
+ * distinct column angular mesh ("signature"), the dense block
+ * Phi(th_r, th'_a) over all angular nodes of the column in column order
+ * (cells sorted, nodes ascending), row-major; col_sig maps columns to blocks. */
+typedef struct rtg_coeffs {
+    const double*  kappa;
+    const double*  sigma;
+    int32_t        nsig;
+    const int64_t* sig_off;        /* [nsig+1] offsets into phi (in doubles)        */
+    const double*  phi;
+    const int32_t* col_sig;        /* [ncols]                                        */
+} rtg_coeffs;
+
+typedef struct rtg_info {
+    int64_t ndof;          /* N                                  */
+    int64_t ndof_interior; /* unknowns of the split system       */
+    int32_t ncols;
+    int32_t nelem;
+    int32_t ncoupling;     /* face couplings to neighbour cells  */
+    int32_t nsig;          /* distinct column angular meshes     */
+    int32_t max_col_ndof;
+    int32_t max_nth_col;
+    int64_t table_bytes;   /* device bytes of operator tables    */
+    int64_t bytes_per_apply_fp64; /* algorithmic bytes of one FP64 apply */
+    int64_t bytes_per_apply_fp32;
+    int64_t flops_per_apply;
+} rtg_info;
+
+typedef struct rtg_solve_opts {
+    int32_t method;        /* 0: GMRES(restart) in FP64 (the plain method)
+                              1: FP32 inner GMRES + FP64 iterative refinement   */
+    int32_t restart;       /* Krylov subspace size (reference: 50)              */
+    int32_t max_it;        /* total inner iterations cap (reference: 5000)      */
+    double  rtol;          /* relative residual target on ||r||/||b||           */
+    double  atol;          /* absolute residual target                           */
+    int32_t precond;       /* 0 none, 1 element block-Jacobi (sweep later)      */
+    int32_t nonzero_guess; /* 1: start from x (reference: x0 = f_I)             */
+    double  inner_rtol;    /* method 1: inner FP32 reduction per outer step     */
+    int32_t max_outer;     /* method 1: cap on refinement steps                 */
+    int32_t verbose;
+} rtg_solve_opts;
+
+typedef struct rtg_solve_info {
+    int32_t converged;     /* 1 converged, 0 hit max_it, <0 breakdown         */
+    int32_t iterations;    /* inner Krylov iterations                          */
+    int32_t outer;         /* refinement steps (method 1)                      */
+    int32_t fp64_applies;
+    int32_t fp32_applies;
+    double  res0;          /* ||b - A x0||                                     */
+    double  res_f;         /* final true residual ||b - A x|| (FP64)           */
+    double  rhs_norm;      /* ||b||                                            */
+    double  seconds;       /* wall time inside rtg_solve                       */
+    int32_t hist_len;      /* residual history entries written                 */
+} rtg_solve_info;
+
+/* library / quadrature ------------------------------------------------------ */
+int         rtg_abi_version(void);
+const char* rtg_last_error(void);
+/* kind 0: Legendre-Gauss-Lobatto (x, y), 1: Legendre-Gauss (th); ascending on
+ * [-1, 1]; n in [1, 16]. */
+int rtg_quad_nodes(int kind, int n, double* nodes, double* weights);
+
+/* handle ---------------------------------------------------------------- */
+int  rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device,
+                rtg_handle** out);
+void rtg_destroy(rtg_handle* h);
+int  rtg_get_info(const rtg_handle* h, rtg_info* info);
+
+/* operator -------------------------------------------------------------- */
+/* y = Op(flags) x on `stream` (cudaStream_t, NULL = legacy default).
+ * x, y: device arrays of N doubles (RTG_FP64) or floats (RTG_FP32); x and y
+ * must not alias. */
+int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y,
+              void* stream);
+/* mask[N] (device, uint8): 1 for unknowns, 0 for inflow-boundary DOFs. */
+int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream);
+/* out = x with the entries of one part zeroed: part 0 keeps the unknowns,
+ * part 1 keeps the inflow-boundary DOFs (device, doubles, in place allowed). */
+int rtg_mask_vector(rtg_handle* h, int part, const double* x, double* out, void* stream);
+/* Compact a full vector to its interior part (length ndof_interior) and back:
+ * merge writes x_int at the unknowns and g at the inflow-boundary DOFs. */
+int rtg_split_vector(rtg_handle* h, const double* x, double* x_int, void* stream);
+int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, double* x,
+                      void* stream);
+/* out_beta = (dx dy dth / 8) wx_i wy_j wth_a * fvals_beta (device doubles). */
+int rtg_weight_forcing(rtg_handle* h, const double* fvals, double* out, void* stream);
+
+/* solve ------------------------------------------------------------------ */
+/* Solve A_II u_I = f_I - A_IB g_B (f, g full-length device vectors), writing
+ * the merged solution u (device, N doubles).  With opts->nonzero_guess the
+ * interior of u on entry is the initial guess.  hist (host, may be NULL)
+ * receives up to hist_cap residual norms. */
+int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u,
+              const rtg_solve_opts* opts, rtg_solve_info* info,
+              double* hist, int hist_cap, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTG_H */

@@ -673,3 +673,50 @@ def l2_weights(mesh, L=None):
     with kappa = 1 (rt/mass_matrix.py:145-169)."""
     L = L or Layout(mesh)
     return mass_matrix(mesh, lambda x, y: 1.0 + 0. * (x + y), L).diagonal()
+
+
+def column_block_preconditioner(MS, mask, L):
+    """Per-column inverse of the (M - S) block restricted to the unknowns: the
+    preconditioner rt/preconditioner_matrix.py:506-507 returns
+    (return_preconditioner=True), used here in place of PETSc bjacobi."""
+    I = np.nonzero(mask)[0]
+    pos = np.full(len(mask), -1, dtype=np.int64)
+    pos[I] = np.arange(len(I))
+    MS = MS.tocsr()
+    blocks = []
+    bounds = []
+    col_start = [L.off[(ck, sorted(L.mesh.cols[ck].cells.keys())[0])] for ck in L.col_keys] + [L.N]
+    for c in range(len(L.col_keys)):
+        g = np.arange(col_start[c], col_start[c + 1])
+        g = g[mask[g]]
+        if len(g) == 0:
+            continue
+        B = MS[g][:, g].tocsc()
+        blocks.append(spla.splu(B))
+        bounds.append(pos[g])
+
+    def apply(r):
+        z = np.empty_like(r)
+        for lu, idx in zip(blocks, bounds):
+            z[idx] = lu.solve(r[idx])
+        return z
+
+    return spla.LinearOperator((len(I), len(I)), matvec=apply, dtype=np.float64)
+
+
+def solve_gmres(A, MS, f, g, mask, L, rtol=1e-10, restart=50, maxiter=5000, x0=None):
+    """GMRES(restart) on the split system with the per-column (M - S)^-1
+    preconditioner; returns (u merged, iterations)."""
+    A_II, _, rhs, I, B = split_system(A, f, g, mask)
+    P = column_block_preconditioner(MS, mask, L)
+    count = [0]
+
+    def cb(_):
+        count[0] += 1
+
+    x, info = spla.gmres(A_II.tocsr(), rhs, x0=x0, rtol=rtol, atol=0., restart=restart,
+                         maxiter=maxiter, M=P, callback=cb, callback_type="pr_norm")
+    u = np.zeros(len(mask))
+    u[I] = x
+    u[B] = g[B]
+    return u, count[0]

@@ -1,0 +1,261 @@
+// extern "C" entry points of librtg (declared in include/rtg.h).
+#include <cstring>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "rtg_internal.h"
+
+namespace rtg {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string& msg) { g_err = msg; }
+
+namespace {
+
+template <typename T>
+T* upload(rtg_handle* h, const std::vector<T>& v) {
+    void* p = nullptr;
+    const size_t bytes = sizeof(T) * std::max<size_t>(v.size(), 1);
+    RTG_CUDA(cudaMalloc(&p, bytes));
+    h->allocs.push_back(p);
+    h->table_bytes += (int64_t)bytes;
+    if (!v.empty()) RTG_CUDA(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return (T*)p;
+}
+
+std::vector<float> to_f32(const std::vector<double>& v) {
+    std::vector<float> o(v.size());
+    for (size_t i = 0; i < v.size(); ++i) o[i] = (float)v[i];
+    return o;
+}
+
+__global__ void gather_kernel(const double* __restrict__ x, const int64_t* __restrict__ idx,
+                              double* __restrict__ out, int64_t n) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = x[idx[k]];
+}
+
+__global__ void scatter_kernel(const double* __restrict__ xi, const int64_t* __restrict__ idx,
+                               double* __restrict__ out, int64_t n) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        out[idx[k]] = xi[k];
+}
+
+int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 8); }
+
+// Run fn, turning exceptions into a status code and the thread's error string.
+int guard(const char* what, const std::function<void()>& fn) {
+    try {
+        fn();
+        return RTG_OK;
+    } catch (const RtgError& e) {
+        set_error(std::string(what) + ": " + e.msg);
+        return e.code;
+    } catch (const std::exception& e) {
+        set_error(std::string(what) + ": " + e.what());
+        return RTG_ERR_ARG;
+    }
+}
+}  // namespace
+}  // namespace rtg
+
+using namespace rtg;
+
+extern "C" {
+
+int rtg_abi_version(void) { return RTG_ABI_VERSION; }
+
+const char* rtg_last_error(void) { return g_err.c_str(); }
+
+int rtg_quad_nodes(int kind, int n, double* nodes, double* weights) {
+    return guard("rtg_quad_nodes", [&] {
+        if (n < 1 || n > kMaxNodes) throw RtgError{RTG_ERR_SIZE, "n outside [1, 16]"};
+        if (!nodes || !weights) throw RtgError{RTG_ERR_ARG, "null output"};
+        if (kind == 0)
+            quad_lgl(n, nodes, weights);
+        else if (kind == 1)
+            quad_lg(n, nodes, weights);
+        else
+            throw RtgError{RTG_ERR_ARG, "kind must be 0 (LGL) or 1 (LG)"};
+    });
+}
+
+int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, rtg_handle** out) {
+    if (!out) {
+        set_error("rtg_create: null output handle");
+        return RTG_ERR_ARG;
+    }
+    *out = nullptr;
+    rtg_handle* h = new rtg_handle();
+    const int rc = guard("rtg_create", [&] {
+        h->device = device;
+        RTG_CUDA(cudaSetDevice(device));
+        build_tables(mesh, coeffs, h->host);
+        HostTables& t = h->host;
+        ColDev* cols = upload(h, t.cols);
+        ElemDev* elems = upload(h, t.elems);
+        CplDev* cpls = upload(h, t.cpls);
+        int64_t* woff = upload(h, t.W_off);
+        OpView<double>& a = h->v64;
+        a.cols = cols;
+        a.elems = elems;
+        a.cpls = cpls;
+        a.W_off = woff;
+        a.kw = upload(h, t.kw);
+        a.sw = upload(h, t.sw);
+        a.ang = upload(h, t.ang);
+        a.W = upload(h, t.W);
+        a.G = upload(h, t.G);
+        a.lglw = upload(h, t.lglw);
+        a.mort = upload(h, t.mort);
+        a.ncols = (int32_t)t.cols.size();
+        a.nelem = (int32_t)t.elems.size();
+        OpView<float>& b = h->v32;
+        b.cols = cols;
+        b.elems = elems;
+        b.cpls = cpls;
+        b.W_off = woff;
+        b.kw = upload(h, to_f32(t.kw));
+        b.sw = upload(h, to_f32(t.sw));
+        b.ang = upload(h, to_f32(t.ang));
+        b.W = upload(h, to_f32(t.W));
+        b.G = upload(h, to_f32(t.G));
+        b.lglw = upload(h, to_f32(t.lglw));
+        b.mort = upload(h, to_f32(t.mort));
+        b.ncols = a.ncols;
+        b.nelem = a.nelem;
+        // index of every unknown in the full vector
+        std::vector<int64_t> idx;
+        idx.reserve((size_t)t.ndof_interior);
+        for (const ElemDev& E : t.elems) {
+            const ColDev& C = t.cols[E.col];
+            const int bm = E.flags >> 4;
+            for (int i = 0; i < C.nx; ++i)
+                for (int j = 0; j < C.ny; ++j) {
+                    const bool bd = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) ||
+                                    ((bm & 4) && i == 0) || ((bm & 8) && j == 0);
+                    if (bd) continue;
+                    for (int r = 0; r < E.nth; ++r) idx.push_back(E.dof_off + ((int64_t)i * C.ny + j) * E.nth + r);
+                }
+        }
+        h->d_interior_index = upload(h, idx);
+    });
+    if (rc != RTG_OK) {
+        rtg_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return RTG_OK;
+}
+
+void rtg_destroy(rtg_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    free_workspace(h);
+    for (void* p : h->allocs) cudaFree(p);
+    delete h;
+}
+
+int rtg_get_info(const rtg_handle* h, rtg_info* info) {
+    return guard("rtg_get_info", [&] {
+        if (!h || !info) throw RtgError{RTG_ERR_ARG, "null argument"};
+        const HostTables& t = h->host;
+        rtg_info o{};
+        o.ndof = t.ndof;
+        o.ndof_interior = t.ndof_interior;
+        o.ncols = (int32_t)t.cols.size();
+        o.nelem = (int32_t)t.elems.size();
+        o.ncoupling = (int32_t)t.cpls.size();
+        o.nsig = (int32_t)t.sig_nth.size();
+        o.max_col_ndof = t.max_col_ndof;
+        o.max_nth_col = t.max_nth_col;
+        o.table_bytes = h->table_bytes;
+        // algorithmic bytes: read x, write y, read kappa and sigma at the spatial nodes
+        int64_t nodes = 0, flops = 0;
+        for (const ColDev& C : t.cols) {
+            nodes += (int64_t)C.nx * C.ny;
+            flops += (int64_t)C.ndof * 2 * (C.nx + C.ny + C.nth_col + 1);
+        }
+        o.bytes_per_apply_fp64 = t.ndof * 16 + nodes * 16;
+        o.bytes_per_apply_fp32 = t.ndof * 8 + nodes * 8;
+        o.flops_per_apply = flops;
+        *info = o;
+    });
+}
+
+int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y, void* stream) {
+    return guard("rtg_apply", [&] {
+        if (!h || !x || !y) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (x == y) throw RtgError{RTG_ERR_ARG, "x and y alias"};
+        if (!(flags & (RTG_MASS | RTG_SCAT | RTG_IC | RTG_BC | RTG_SYSTEM)))
+            throw RtgError{RTG_ERR_ARG, "no operator component selected"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64)
+            launch_apply<double>(h, h->v64, flags, (const double*)x, (double*)y, s);
+        else if (prec == RTG_FP32)
+            launch_apply<float>(h, h->v32, flags, (const float*)x, (float*)y, s);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
+int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream) {
+    return guard("rtg_interior_mask", [&] {
+        if (!h || !mask) throw RtgError{RTG_ERR_ARG, "null argument"};
+        launch_interior_mask(h, mask, (cudaStream_t)stream);
+    });
+}
+
+int rtg_mask_vector(rtg_handle* h, int part, const double* x, double* out, void* stream) {
+    return guard("rtg_mask_vector", [&] {
+        if (!h || !x || !out) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (part != 0 && part != 1) throw RtgError{RTG_ERR_ARG, "part must be 0 or 1"};
+        launch_mask_vector(h, part, x, out, (cudaStream_t)stream);
+    });
+}
+
+int rtg_split_vector(rtg_handle* h, const double* x, double* x_int, void* stream) {
+    return guard("rtg_split_vector", [&] {
+        if (!h || !x || !x_int) throw RtgError{RTG_ERR_ARG, "null argument"};
+        const int64_t n = h->host.ndof_interior;
+        gather_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(x, h->d_interior_index, x_int, n);
+        RTG_CUDA(cudaGetLastError());
+    });
+}
+
+int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, double* x, void* stream) {
+    return guard("rtg_merge_vectors", [&] {
+        if (!h || !x_int || !g || !x) throw RtgError{RTG_ERR_ARG, "null argument"};
+        cudaStream_t s = (cudaStream_t)stream;
+        launch_mask_vector(h, 1, g, x, s);
+        const int64_t n = h->host.ndof_interior;
+        scatter_kernel<<<grid_for(n), 256, 0, s>>>(x_int, h->d_interior_index, x, n);
+        RTG_CUDA(cudaGetLastError());
+    });
+}
+
+int rtg_weight_forcing(rtg_handle* h, const double* fvals, double* out, void* stream) {
+    return guard("rtg_weight_forcing", [&] {
+        if (!h || !fvals || !out) throw RtgError{RTG_ERR_ARG, "null argument"};
+        launch_weight_forcing(h, fvals, out, (cudaStream_t)stream);
+    });
+}
+
+int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* opts,
+              rtg_solve_info* info, double* hist, int hist_cap, void* stream) {
+    int inner = RTG_OK;
+    const int rc = guard("rtg_solve", [&] {
+        if (!h || !f || !g || !u || !opts) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (opts->restart < 1 || opts->restart > 60) throw RtgError{RTG_ERR_ARG, "restart outside [1, 60]"};
+        if (opts->method != 0 && opts->method != 1) throw RtgError{RTG_ERR_ARG, "unknown method"};
+        if (!(opts->rtol >= 0.) || !(opts->atol >= 0.)) throw RtgError{RTG_ERR_ARG, "bad tolerance"};
+        inner = solve(h, f, g, u, opts, info, hist, hist_cap, (cudaStream_t)stream);
+    });
+    return rc != RTG_OK ? rc : inner;
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// Internal definitions of librtg: operator tables on the host and device.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "rtg.h"
+
+namespace rtg {
+
+constexpr int kMaxNodes = 16;          // nodes per direction supported
+constexpr double kSmall = 1.e-14;      // 10*EPS drop rule of the (M - S) blocks
+constexpr double kBcTol = 1.e-15;      // drop rule of the face terms
+
+void set_error(const std::string& msg);
+
+struct RtgError {
+    int code;
+    std::string msg;
+};
+
+#define RTG_CUDA(call)                                                        \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess)                                                \
+            throw ::rtg::RtgError{RTG_ERR_CUDA, std::string(#call) + ": " +   \
+                                                    cudaGetErrorString(e_)};  \
+    } while (0)
+
+// Per column.
+struct ColDev {
+    double dx, dy;
+    int64_t dof_off;      // first DOF
+    int32_t nx, ny;
+    int32_t node_off;     // into kw/sw/cw tables (nx*ny entries)
+    int32_t elem_begin, elem_end;
+    int32_t sig;          // angular mesh id
+    int32_t nth_col;      // angular nodes in the column
+    int32_t ndof;         // nx*ny*nth_col
+    int32_t pad;
+};
+
+// Per element (column, leaf cell).
+struct ElemDev {
+    int64_t dof_off;
+    double dth;
+    int32_t col;
+    int32_t nth;
+    int32_t ang;          // offset of this cell's angular table (7*nth doubles)
+    int32_t row;          // first angular row of the cell in the column mesh
+    int32_t flags;        // bits 0-3 face F outflow, bits 4-7 face F inflow boundary
+    int32_t cpl_begin, cpl_end;
+    int32_t pad;
+};
+
+// Face coupling of an element to one neighbour element.
+struct CplDev {
+    double dcoeff;        // (dy dth/4) on x-faces, (dx dth/4) on y-faces
+    int32_t face;
+    int32_t nbr;          // neighbour element
+    int32_t es;           // spatial mortar offset ([m1][m0] row-major)
+    int32_t et;           // angular mortar offset ([nth1][nth0] row-major)
+};
+
+// Device-side view passed to kernels by value.
+template <typename T>
+struct OpView {
+    const ColDev* cols;
+    const ElemDev* elems;
+    const CplDev* cpls;
+    const T* kw;          // wx wy kappa per node
+    const T* sw;          // wx wy sigma per node
+    const T* ang;         // per-cell angular tables: wth, wth sin, wth cos, ThF[4]
+    const T* W;           // angular scattering matrices per signature
+    const int64_t* W_off; // per signature
+    const T* G;           // G[n][p][i] = l'_p(x_i) w_i for n nodes, offset n*n*... see gofs
+    const T* lglw;        // [kMaxNodes+1][kMaxNodes] LGL weights
+    const T* mort;        // spatial + angular mortar matrices
+    int32_t ncols;
+    int32_t nelem;
+};
+
+struct HostTables {
+    std::vector<ColDev> cols;
+    std::vector<ElemDev> elems;
+    std::vector<CplDev> cpls;
+    std::vector<double> kw, sw, ang, W, G, lglw, mort;
+    std::vector<int64_t> W_off;
+    std::vector<int32_t> sig_nth;
+    int64_t ndof = 0, ndof_interior = 0;
+    int32_t max_col_ndof = 0, max_nth_col = 0;
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct Workspace;  // Krylov workspace (rtg_krylov.cu)
+
+}  // namespace rtg
+
+struct rtg_handle {
+    int device = 0;
+    rtg::HostTables host;
+    // device copies (FP64 and FP32 variants of the value tables)
+    rtg::OpView<double> v64{};
+    rtg::OpView<float> v32{};
+    std::vector<void*> allocs;
+    int64_t table_bytes = 0;
+    int64_t* d_interior_index = nullptr;   // [ndof_interior] full index of each unknown
+    rtg::Workspace* ws = nullptr;
+};
+
+namespace rtg {
+
+// Host builders (rtg_build.cpp)
+void quad_lgl(int n, double* x, double* w);
+void quad_lg(int n, double* x, double* w);
+void build_tables(const rtg_mesh_desc* m, const rtg_coeffs* c, HostTables& t);
+
+// Kernel launchers (rtg_apply.cu)
+template <typename T>
+void launch_apply(const rtg_handle* h, const OpView<T>& v, uint32_t flags, const T* x, T* y,
+                  cudaStream_t s);
+void launch_interior_mask(const rtg_handle* h, uint8_t* mask, cudaStream_t s);
+void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* out,
+                        cudaStream_t s);
+void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s);
+
+// Solver (rtg_krylov.cu)
+int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,
+          rtg_solve_info* info, double* hist, int hist_cap, cudaStream_t s);
+void free_workspace(rtg_handle* h);
+
+}  // namespace rtg

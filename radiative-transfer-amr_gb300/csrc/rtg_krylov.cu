@@ -1,0 +1,410 @@
+// Device-resident Krylov solvers for the split RT system A_II u_I = b
+// (rt/solve.py:81-132).  Vectors stay full length (N) with the inflow-boundary
+// entries held at zero, so every product is one masked operator apply.
+//
+//  * method 0 (plain): GMRES(m) in FP64, CGS2 Arnoldi, Givens on the host.
+//  * method 1 (mixed): FP64 iterative refinement around FP32 GMRES(m): the
+//    true residual r = b - A x is formed with the FP64 operator, the
+//    correction A d = r is solved with FP32 applies and FP32 basis vectors
+//    whose inner products accumulate in FP64; Hessenberg, Givens and the
+//    convergence test are FP64.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "rtg_internal.h"
+
+namespace rtg {
+
+namespace {
+
+constexpr int kRedBlocks = 296;   // 2 x 148-ish; partial sums per reduction
+constexpr int kRedThreads = 256;
+constexpr int kDotGroup = 8;      // vectors per pass in multi_dot
+
+template <typename T>
+__global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, const T* __restrict__ w,
+                                 int64_t n, double* __restrict__ partial) {
+    __shared__ double red[kDotGroup][kRedThreads / 32];
+    for (int g0 = 0; g0 < k; g0 += kDotGroup) {
+        const int gk = min(kDotGroup, k - g0);
+        double acc[kDotGroup];
+#pragma unroll
+        for (int q = 0; q < kDotGroup; ++q) acc[q] = 0.;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+             i += (int64_t)gridDim.x * blockDim.x) {
+            const double wi = (double)w[i];
+#pragma unroll
+            for (int q = 0; q < kDotGroup; ++q)
+                if (q < gk) acc[q] += (double)V[(int64_t)(g0 + q) * ldv + i] * wi;
+        }
+#pragma unroll
+        for (int q = 0; q < kDotGroup; ++q) {
+            double s = acc[q];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
+        }
+        __syncthreads();
+        if (threadIdx.x < gk) {
+            double s = 0.;
+            for (int wq = 0; wq < kRedThreads / 32; ++wq) s += red[threadIdx.x][wq];
+            partial[(int64_t)blockIdx.x * k + g0 + threadIdx.x] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// out[q] = sum_b partial[b][q]; with add, also out_sum[q] = out[q] + add[q]
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nb, int k,
+                                       double* __restrict__ out, const double* __restrict__ add,
+                                       double* __restrict__ out_sum) {
+    const int q = blockIdx.x;
+    double s = 0.;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(int64_t)b * k + q];
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.;
+        for (int wq = 0; wq < (int)(blockDim.x + 31) / 32; ++wq) t += red[wq];
+        out[q] = t;
+        if (add) out_sum[q] = t + add[q];
+    }
+}
+
+// w -= sum_q h[q] V_q
+template <typename T>
+__global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
+                                  const double* __restrict__ h, int64_t n) {
+    __shared__ double hs[64];
+    if (threadIdx.x < k) hs[threadIdx.x] = h[threadIdx.x];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double s = (double)w[i];
+        for (int q = 0; q < k; ++q) s -= hs[q] * (double)V[(int64_t)q * ldv + i];
+        w[i] = (T)s;
+    }
+}
+
+// out = w / sqrt(nrm2sq[0]); hcol[k] = sqrt(nrm2sq[0])
+template <typename T>
+__global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, const double* nrm2sq,
+                                 double* hcol, int k, int64_t n) {
+    const double nr = sqrt(nrm2sq[0]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) hcol[k] = nr;
+    const double inv = nr > 0. ? 1. / nr : 0.;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (T)((double)w[i] * inv);
+}
+
+// y = a*x + b*y over full vectors of possibly different types
+template <typename TX, typename TY>
+__global__ void axpby_kernel(double a, const TX* __restrict__ x, double b, TY* __restrict__ y, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (TY)(a * (double)x[i] + (b == 0. ? 0. : b * (double)y[i]));
+}
+
+// x += sum_q c[q] V_q (c on device)
+template <typename TV, typename TX>
+__global__ void combine_kernel(TX* __restrict__ x, const TV* __restrict__ V, int64_t ldv, int k,
+                               const double* __restrict__ c, double scale, int64_t n) {
+    __shared__ double cs[64];
+    if (threadIdx.x < k) cs[threadIdx.x] = c[threadIdx.x];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.;
+        for (int q = 0; q < k; ++q) s += cs[q] * (double)V[(int64_t)q * ldv + i];
+        x[i] = (TX)((double)x[i] + scale * s);
+    }
+}
+
+inline int grid_for(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    return (int)std::min<int64_t>(g, 152 * 8);
+}
+
+}  // namespace
+
+struct Workspace {
+    int m = 0;
+    int64_t N = 0;
+    double* V64 = nullptr;   // (m+1) x N
+    float* V32 = nullptr;    // (m+1) x N
+    double *b = nullptr, *r = nullptr, *x = nullptr, *t = nullptr, *gb = nullptr;
+    double* w64 = nullptr;
+    float *w32 = nullptr, *d32 = nullptr;
+    double* partial = nullptr;  // kRedBlocks x (m+1)
+    double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
+    double* hhost = nullptr;    // pinned
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+template <typename T>
+T* dalloc(Workspace* ws, int64_t n) {
+    void* p = nullptr;
+    RTG_CUDA(cudaMalloc(&p, sizeof(T) * (size_t)std::max<int64_t>(n, 1)));
+    ws->allocs.push_back(p);
+    return (T*)p;
+}
+
+Workspace* get_ws(rtg_handle* h, int m) {
+    Workspace* ws = h->ws;
+    const int64_t N = h->host.ndof;
+    if (ws && ws->m >= m && ws->N == N) return ws;
+    free_workspace(h);
+    ws = new Workspace();
+    h->ws = ws;
+    ws->m = m;
+    ws->N = N;
+    ws->V64 = dalloc<double>(ws, (int64_t)(m + 1) * N);
+    ws->V32 = dalloc<float>(ws, (int64_t)(m + 1) * N);
+    ws->b = dalloc<double>(ws, N);
+    ws->r = dalloc<double>(ws, N);
+    ws->x = dalloc<double>(ws, N);
+    ws->t = dalloc<double>(ws, N);
+    ws->gb = dalloc<double>(ws, N);
+    ws->w64 = dalloc<double>(ws, N);
+    ws->w32 = dalloc<float>(ws, N);
+    ws->d32 = dalloc<float>(ws, N);
+    ws->partial = dalloc<double>(ws, (int64_t)kRedBlocks * (m + 2));
+    ws->hdev = dalloc<double>(ws, 4 * (m + 2));
+    RTG_CUDA(cudaMallocHost(&ws->hhost, sizeof(double) * 4 * (m + 2)));
+    return ws;
+}
+
+template <typename T>
+void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, double* out,
+          const double* add, double* out_sum, cudaStream_t s) {
+    multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial);
+    reduce_partials_kernel<<<k, 256, 0, s>>>(ws->partial, kRedBlocks, k, out, add, out_sum);
+}
+
+template <typename T>
+const OpView<T>& view(const rtg_handle* h);
+template <>
+const OpView<double>& view<double>(const rtg_handle* h) { return h->v64; }
+template <>
+const OpView<float>& view<float>(const rtg_handle* h) { return h->v32; }
+
+double norm2(rtg_handle* h, Workspace* ws, const double* v, cudaStream_t s) {
+    dots<double>(ws, v, 0, 1, v, ws->N, ws->hdev, nullptr, nullptr, s);
+    RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    RTG_CUDA(cudaStreamSynchronize(s));
+    return std::sqrt(ws->hhost[0]);
+}
+
+// r = b - A_II x (FP64), returns ||r||
+double residual64(rtg_handle* h, Workspace* ws, const double* b, const double* x, double* r,
+                  cudaStream_t s) {
+    launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, x, r, s);
+    axpby_kernel<double, double><<<grid_for(ws->N), 256, 0, s>>>(1., b, -1., r, ws->N);
+    return norm2(h, ws, r, s);
+}
+
+struct GmresResult {
+    int iters = 0;
+    bool converged = false;
+    double res = 0.;
+};
+
+// GMRES(m) for A_II d = r0 in precision T starting from d = 0.  rhs is given
+// in T (scaled); stops when the estimated residual <= tol_abs or after
+// max_it iterations.  Returns the solution in xT (T).  hist gets estimates.
+template <typename T>
+GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T* V, int m,
+                  double tol_abs, int max_it, std::vector<double>* hist, int* applies,
+                  cudaStream_t s) {
+    const int64_t N = ws->N;
+    GmresResult res;
+    const OpView<T>& v = view<T>(h);
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+    axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., rhs, 0., xT, N);
+    // r = rhs - A x = rhs (x = 0)
+    int total = 0;
+    bool first = true;
+    while (total < max_it) {
+        // r = rhs - A x  into V_0 (unnormalised), beta = ||r||
+        if (first) {
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, 0., wbuf, N);
+        } else {
+            launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, xT, wbuf, s);
+            ++*applies;
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, -1., wbuf, N);
+        }
+        first = false;
+        dots<T>(ws, wbuf, 0, 1, wbuf, N, ws->hdev + 3 * (m + 2), nullptr, nullptr, s);
+        normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ws->hdev + 3 * (m + 2),
+                                                         ws->hdev + 2 * (m + 2), 0, N);
+        RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev + 2 * (m + 2), sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+        RTG_CUDA(cudaStreamSynchronize(s));
+        const double beta = ws->hhost[0];
+        res.res = beta;
+        if (!std::isfinite(beta)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+        if (beta <= tol_abs) {
+            res.converged = true;
+            break;
+        }
+        std::fill(g.begin(), g.end(), 0.);
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && total < max_it; ++j) {
+            T* vj = V + (int64_t)j * N;
+            T* vn = V + (int64_t)(j + 1) * N;
+            launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
+            ++*applies;
+            double* h1 = ws->hdev;
+            double* h2 = ws->hdev + (m + 2);
+            double* ho = ws->hdev + 2 * (m + 2);
+            double* nr = ws->hdev + 3 * (m + 2);
+            // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
+            dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s);
+            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N);
+            dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
+            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N);
+            dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
+            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N);
+            RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
+                                     cudaMemcpyDeviceToHost, s));
+            RTG_CUDA(cudaStreamSynchronize(s));
+            ++total;
+            double* hc = &H[(size_t)j * (m + 1)];
+            for (int q = 0; q <= j; ++q) hc[q] = ws->hhost[2 * (m + 2) + q];
+            hc[j + 1] = ws->hhost[2 * (m + 2) + j + 1];
+            // Givens
+            for (int q = 0; q < j; ++q) {
+                const double a = hc[q], b = hc[q + 1];
+                hc[q] = cs[q] * a + sn[q] * b;
+                hc[q + 1] = -sn[q] * a + cs[q] * b;
+            }
+            const double a = hc[j], b = hc[j + 1];
+            const double rr = std::hypot(a, b);
+            cs[j] = rr > 0. ? a / rr : 1.;
+            sn[j] = rr > 0. ? b / rr : 0.;
+            hc[j] = rr;
+            hc[j + 1] = 0.;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            const double est = std::fabs(g[j + 1]);
+            if (!std::isfinite(est)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+            if (hist) hist->push_back(est);
+            res.res = est;
+            if (est <= tol_abs || rr == 0.) {
+                ++j;
+                res.converged = est <= tol_abs;
+                break;
+            }
+        }
+        // y = H^{-1} g (upper triangular j x j)
+        for (int q = j - 1; q >= 0; --q) {
+            double sacc = g[q];
+            for (int c = q + 1; c < j; ++c) sacc -= H[(size_t)c * (m + 1) + q] * y[c];
+            y[q] = sacc / H[(size_t)q * (m + 1) + q];
+        }
+        RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
+        combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N);
+        res.iters = total;
+        if (res.converged) break;
+    }
+    res.iters = total;
+    return res;
+}
+
+}  // namespace
+
+void free_workspace(rtg_handle* h) {
+    if (!h->ws) return;
+    for (void* p : h->ws->allocs) cudaFree(p);
+    if (h->ws->hhost) cudaFreeHost(h->ws->hhost);
+    delete h->ws;
+    h->ws = nullptr;
+}
+
+int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,
+          rtg_solve_info* info, double* hist, int hist_cap, cudaStream_t s) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int m = std::max(1, std::min(o->restart, 60));
+    Workspace* ws = get_ws(h, m);
+    const int64_t N = ws->N;
+    rtg_solve_info inf{};
+    std::vector<double> hv;
+
+    // b = mask_I (f - A mask_B g)     (rt/solve.py:98-101)
+    launch_mask_vector(h, 1, g, ws->gb, s);
+    launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, ws->gb, ws->t, s);
+    inf.fp64_applies++;
+    launch_mask_vector(h, 0, f, ws->b, s);
+    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(-1., ws->t, 1., ws->b, N);
+    // x0 = u_I (nonzero guess) or 0; the reference starts from f_I (rt/solve.py:104)
+    if (o->nonzero_guess)
+        launch_mask_vector(h, 0, u, ws->x, s);
+    else
+        axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(0., ws->b, 0., ws->x, N);
+
+    inf.rhs_norm = norm2(h, ws, ws->b, s);
+    const double tol = std::max(o->rtol * inf.rhs_norm, o->atol);
+    double res = residual64(h, ws, ws->b, ws->x, ws->r, s);
+    inf.fp64_applies++;
+    inf.res0 = res;
+    hv.push_back(res);
+    int applies32 = 0, applies64 = 0;
+
+    if (o->method == 0) {
+        // GMRES on the correction: A d = r, x += d, repeated until converged.
+        int used = 0;
+        while (res > tol && used < o->max_it) {
+            GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
+                                           o->max_it - used, &hv, &applies64, s);
+            used += std::max(gr.iters, 1);
+            axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N);
+            res = residual64(h, ws, ws->b, ws->x, ws->r, s);
+            inf.fp64_applies++;
+            hv.push_back(res);
+            if (gr.iters == 0) break;
+        }
+        inf.iterations = used;
+    } else {
+        int used = 0, outer = 0;
+        const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
+        const double inner_rtol = o->inner_rtol > 0. ? o->inner_rtol : 1e-6;
+        while (res > tol && used < o->max_it && outer < max_outer) {
+            // r32 = r / ||r||
+            axpby_kernel<double, float><<<grid_for(N), 256, 0, s>>>(1. / res, ws->r, 0., ws->w32, N);
+            GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, (float*)ws->t, ws->V32, m,
+                                          std::max(inner_rtol, tol / res), o->max_it - used,
+                                          nullptr, &applies32, s);
+            used += std::max(gr.iters, 1);
+            axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N);
+            res = residual64(h, ws, ws->b, ws->x, ws->r, s);
+            inf.fp64_applies++;
+            hv.push_back(res);
+            ++outer;
+        }
+        inf.iterations = used;
+        inf.outer = outer;
+    }
+    inf.fp64_applies += applies64;
+    inf.fp32_applies += applies32;
+    inf.res_f = res;
+    inf.converged = res <= tol ? 1 : 0;
+    // u = x on the unknowns, g on the inflow-boundary DOFs (rt/solve.py:163)
+    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->x, 1., ws->gb, N);
+    RTG_CUDA(cudaMemcpyAsync(u, ws->gb, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    RTG_CUDA(cudaStreamSynchronize(s));
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    inf.hist_len = (int)std::min<size_t>(hv.size(), hist ? (size_t)hist_cap : 0);
+    if (hist)
+        for (int q = 0; q < inf.hist_len; ++q) hist[q] = hv[q];
+    if (info) *info = inf;
+    return RTG_OK;
+}
+
+}  // namespace rtg

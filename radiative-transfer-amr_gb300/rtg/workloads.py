@@ -305,6 +305,6 @@ def small_random_mesh(mesh_cls=Mesh, seed=3):
 def config2_mesh(mesh_cls=Mesh, seed=0):
     """Single adaptive problem mesh: [0,3]x[0,2], six rounds of seeded random
     hp refinement, nodes per dimension in [3, 7] (degree 2..6), about 2e5 DOF."""
-    return random_hp_mesh([3., 2.], 3, 3, rounds=6, seed=seed, frac_spt=0.22,
-                          frac_ang=0.12, p_prob=0.45, n_max=7, nref_ang=2,
+    return random_hp_mesh([3., 2.], 3, 3, rounds=6, seed=seed, frac_spt=0.3,
+                          frac_ang=0.12, p_prob=0.5, n_max=7, nref_ang=2,
                           nref_spt=2, mesh_cls=mesh_cls)
