@@ -172,13 +172,13 @@ def run_ours(args):
     w = (ones / kap).cpu().numpy()
 
     # judge solution: tight plain FP64 solve
-    u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=50000)
+    u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=20000, precond=1)
     u_ref_h = u_ref.cpu().numpy()
 
     def calibrate(method):
         for k in range(6, 15):
             rtol = 10.0 ** (-k)
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=50000)
+            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
             err = rel_l2(u.cpu().numpy(), u_ref_h, w)
             if err <= ERR_TARGET:
                 return rtol, err, info
@@ -192,7 +192,7 @@ def run_ours(args):
 
     def timed(method, rtol, steps, warm):
         for _ in range(warm):
-            ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=50000)
+            ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
         times, errs, infos = [], [], []
         for _ in range(steps):
             flush.fill_(1.0)
@@ -200,7 +200,7 @@ def run_ours(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=50000)
+            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
             e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
@@ -226,7 +226,7 @@ def run_ours(args):
     fw = torch.empty_like(fd)
     gd = torch.empty_like(fd)
     ud = torch.zeros_like(fd)
-    opts = _lib.SolveOpts(method=1, restart=50, max_it=50000, rtol=rtol_mx, atol=0., precond=0,
+    opts = _lib.SolveOpts(method=1, restart=50, max_it=50000, rtol=rtol_mx, atol=0., precond=1,
                           nonzero_guess=0, inner_rtol=1e-6, max_outer=20, verbose=0)
     sinfo = _lib.SolveInfo()
     sp = C.c_void_p(stream.cuda_stream)

@@ -124,7 +124,7 @@ typedef struct rtg_solve_opts {
     int32_t max_it;        /* total inner iterations cap (reference: 5000)      */
     double  rtol;          /* relative residual target on ||r||/||b||           */
     double  atol;          /* absolute residual target                           */
-    int32_t precond;       /* 0 none, 1 element block-Jacobi (sweep later)      */
+    int32_t precond;       /* 0 none, 1 upwind transport sweep (right precond.) */
     int32_t nonzero_guess; /* 1: start from x (reference: x0 = f_I)             */
     double  inner_rtol;    /* method 1: inner FP32 reduction per outer step     */
     int32_t max_outer;     /* method 1: cap on refinement steps                 */
@@ -142,6 +142,7 @@ typedef struct rtg_solve_info {
     double  rhs_norm;      /* ||b||                                            */
     double  seconds;       /* wall time inside rtg_solve                       */
     int32_t hist_len;      /* residual history entries written                 */
+    int32_t sweeps;        /* preconditioner (sweep) applications              */
 } rtg_solve_info;
 
 /* library / quadrature ------------------------------------------------------ */

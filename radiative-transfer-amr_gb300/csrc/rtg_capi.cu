@@ -156,6 +156,7 @@ void rtg_destroy(rtg_handle* h) {
     if (!h) return;
     cudaSetDevice(h->device);
     free_workspace(h);
+    free_sweep(h);
     for (void* p : h->allocs) cudaFree(p);
     delete h;
 }

@@ -100,6 +100,7 @@ struct DevBuf {
 };
 
 struct Workspace;  // Krylov workspace (rtg_krylov.cu)
+struct Sweep;      // sweep preconditioner (rtg_sweep.cu)
 
 }  // namespace rtg
 
@@ -113,6 +114,7 @@ struct rtg_handle {
     int64_t table_bytes = 0;
     int64_t* d_interior_index = nullptr;   // [ndof_interior] full index of each unknown
     rtg::Workspace* ws = nullptr;
+    rtg::Sweep* sweep = nullptr;
 };
 
 namespace rtg {
@@ -130,6 +132,14 @@ void launch_interior_mask(const rtg_handle* h, uint8_t* mask, cudaStream_t s);
 void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* out,
                         cudaStream_t s);
 void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s);
+
+// Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
+template <typename T>
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
+Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
+int sweep_levels_count(rtg_handle* h, cudaStream_t s);
+int sweep_lagged_count(rtg_handle* h, cudaStream_t s);
+void free_sweep(rtg_handle* h);
 
 // Solver (rtg_krylov.cu)
 int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,

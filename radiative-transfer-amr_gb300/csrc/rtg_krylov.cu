@@ -137,8 +137,8 @@ struct Workspace {
     double* V64 = nullptr;   // (m+1) x N
     float* V32 = nullptr;    // (m+1) x N
     double *b = nullptr, *r = nullptr, *x = nullptr, *t = nullptr, *gb = nullptr;
-    double* w64 = nullptr;
-    float *w32 = nullptr, *d32 = nullptr;
+    double *w64 = nullptr, *z64 = nullptr, *t64 = nullptr;
+    float *w32 = nullptr, *d32 = nullptr, *z32 = nullptr, *t32 = nullptr, *s32 = nullptr;
     double* partial = nullptr;  // kRedBlocks x (m+1)
     double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
@@ -174,6 +174,11 @@ Workspace* get_ws(rtg_handle* h, int m) {
     ws->w64 = dalloc<double>(ws, N);
     ws->w32 = dalloc<float>(ws, N);
     ws->d32 = dalloc<float>(ws, N);
+    ws->z64 = dalloc<double>(ws, N);
+    ws->t64 = dalloc<double>(ws, N);
+    ws->z32 = dalloc<float>(ws, N);
+    ws->t32 = dalloc<float>(ws, N);
+    ws->s32 = dalloc<float>(ws, N);
     ws->partial = dalloc<double>(ws, (int64_t)kRedBlocks * (m + 2));
     ws->hdev = dalloc<double>(ws, 4 * (m + 2));
     RTG_CUDA(cudaMallocHost(&ws->hhost, sizeof(double) * 4 * (m + 2)));
@@ -221,7 +226,7 @@ struct GmresResult {
 template <typename T>
 GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T* V, int m,
                   double tol_abs, int max_it, std::vector<double>* hist, int* applies,
-                  cudaStream_t s) {
+                  bool pc, T* zbuf, T* tbuf, int* sweeps, cudaStream_t s) {
     const int64_t N = ws->N;
     GmresResult res;
     const OpView<T>& v = view<T>(h);
@@ -259,7 +264,13 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         for (; j < m && total < max_it; ++j) {
             T* vj = V + (int64_t)j * N;
             T* vn = V + (int64_t)(j + 1) * N;
-            launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
+            if (pc) {
+                apply_sweep<T>(h, vj, zbuf, s);   // right preconditioning: w = A P^{-1} v_j
+                ++*sweeps;
+                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zbuf, wbuf, s);
+            } else {
+                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
+            }
             ++*applies;
             double* h1 = ws->hdev;
             double* h2 = ws->hdev + (m + 2);
@@ -310,7 +321,16 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             y[q] = sacc / H[(size_t)q * (m + 1) + q];
         }
         RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
-        combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N);
+        if (pc) {
+            // x += P^{-1} (V y)
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., tbuf, 0., tbuf, N);
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(tbuf, V, N, j, ws->hdev, 1., N);
+            apply_sweep<T>(h, tbuf, zbuf, s);
+            ++*sweeps;
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., zbuf, 1., xT, N);
+        } else {
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N);
+        }
         res.iters = total;
         if (res.converged) break;
     }
@@ -355,14 +375,17 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.fp64_applies++;
     inf.res0 = res;
     hv.push_back(res);
-    int applies32 = 0, applies64 = 0;
+    int applies32 = 0, applies64 = 0, sweeps = 0;
+    const bool pc = o->precond == 1;
+    if (pc) get_sweep(h, s);
 
     if (o->method == 0) {
         // GMRES on the correction: A d = r, x += d, repeated until converged.
         int used = 0;
         while (res > tol && used < o->max_it) {
             GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
-                                           o->max_it - used, &hv, &applies64, s);
+                                           o->max_it - used, &hv, &applies64, pc, ws->z64, ws->t64,
+                                           &sweeps, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N);
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
@@ -378,9 +401,11 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
         while (res > tol && used < o->max_it && outer < max_outer) {
             // r32 = r / ||r||
             axpby_kernel<double, float><<<grid_for(N), 256, 0, s>>>(1. / res, ws->r, 0., ws->w32, N);
-            GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, (float*)ws->t, ws->V32, m,
-                                          std::max(inner_rtol, tol / res), o->max_it - used,
-                                          nullptr, &applies32, s);
+            // one FP32 solve per refinement step, capped at 20 restart cycles
+            const int inner_cap = std::min(o->max_it - used, 20 * m);
+            GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, ws->s32, ws->V32, m,
+                                          std::max(inner_rtol, tol / res), inner_cap,
+                                          nullptr, &applies32, pc, ws->z32, ws->t32, &sweeps, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N);
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
@@ -393,6 +418,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     }
     inf.fp64_applies += applies64;
     inf.fp32_applies += applies32;
+    inf.sweeps = sweeps;
     inf.res_f = res;
     inf.converged = res <= tol ? 1 : 0;
     // u = x on the unknowns, g on the inflow-boundary DOFs (rt/solve.py:163)

@@ -1,0 +1,410 @@
+// Upwind block transport sweep used as the preconditioner of the RT solve.
+//
+// P is the block-lower-triangular part of the transport-plus-self-scattering
+// operator in an upwind element order:
+//   * element-diagonal block, per angular node r of the element: the
+//     (nx ny) x (nx ny) matrix of extinction minus the r == a self-scattering
+//     term, minus interior streaming, plus the outflow face terms (the same
+//     entries rtg_apply uses with RTG_SYSTEM);
+//   * off-diagonal blocks: the inflow face couplings to neighbour elements
+//     that come earlier in the order.
+// Elements are ordered by Kahn levels of the "depends on the upwind
+// neighbour" graph over all angular cells at once; where the graph has a
+// cycle (cells that lie in no single quadrant couple on every face) the
+// couplings that close it are dropped from P.  Each level is one launch with
+// one CTA per element; the levels of a sweep are captured in a CUDA graph.
+// Applying P^{-1} is exact for the transport part of an acyclic mesh; the
+// cross-cell scattering is left to the Krylov iteration.
+#include <algorithm>
+#include <cmath>
+#include <queue>
+#include <vector>
+
+#include "rtg_internal.h"
+
+namespace rtg {
+
+namespace {
+
+constexpr int kSweepThreads = 128;
+constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
+
+__device__ __forceinline__ int gofs_s(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
+
+// One CTA per (element, angular node): assemble the element block for that
+// node in shared memory as [A | I] and invert it by Gauss-Jordan elimination
+// with partial pivoting.  Rows of inflow-boundary nodes become identity rows.
+__global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __restrict__ blk_elem,
+                                           const int32_t* __restrict__ blk_r,
+                                           const int64_t* __restrict__ blk_off, double* __restrict__ inv64,
+                                           float* __restrict__ inv32, int* __restrict__ status) {
+    extern __shared__ double smem[];
+    const int b = blockIdx.x;
+    const int e = blk_elem[b];
+    const int r = blk_r[b];
+    const ElemDev E = v.elems[e];
+    const ColDev C = v.cols[E.col];
+    const int nx = C.nx, ny = C.ny, nn = nx * ny, nth = E.nth;
+    const int ld = 2 * nn;
+    double* M = smem;                      // nn x 2nn
+    __shared__ int piv;
+    __shared__ double pval;
+    const double* A = v.ang + E.ang;
+    const double* W = v.W + v.W_off[C.sig];
+    const double* Gx = v.G + gofs_s(nx);
+    const double* Gy = v.G + gofs_s(ny);
+    const double* wxs = v.lglw + nx * kMaxNodes;
+    const double* wys = v.lglw + ny * kMaxNodes;
+    const double dxdy8 = C.dx * C.dy / 8.;
+    const double wsr = A[nth + r], wcr = A[2 * nth + r], wr = A[r];
+    const double self = W[(int64_t)(E.row + r) * C.nth_col + E.row + r];
+    const int bm = E.flags >> 4;
+    for (int k = threadIdx.x; k < nn * ld; k += blockDim.x) {
+        const int row = k / ld, col = k % ld;
+        const int p = row / ny, q = row % ny;
+        const bool bd = ((bm & 1) && p == nx - 1) || ((bm & 2) && q == ny - 1) || ((bm & 4) && p == 0) ||
+                        ((bm & 8) && q == 0);
+        double val = 0.;
+        if (col >= nn) {
+            val = (col - nn == row) ? 1. : 0.;
+        } else if (bd) {
+            val = (col == row) ? 1. : 0.;
+        } else {
+            const int i = col / ny, j = col % ny;
+            const int node = C.node_off + col;
+            if (col == row) {
+                val += dxdy8 * E.dth * wr * v.kw[node] - dxdy8 * v.sw[node] * self;
+                for (int F = 0; F < 4; ++F) {
+                    if (!(E.flags & (1 << F))) continue;
+                    const bool on = (F == 0 && p == nx - 1) || (F == 1 && q == ny - 1) || (F == 2 && p == 0) ||
+                                    (F == 3 && q == 0);
+                    if (!on) continue;
+                    const double dc = (F % 2 == 0) ? C.dy * E.dth / 4. : C.dx * E.dth / 4.;
+                    const double w = (F % 2 == 0) ? wys[q] : wxs[p];
+                    val += dc * w * wr * A[(3 + F) * nth + r];
+                }
+            }
+            if (p == i) val -= (C.dx * E.dth / 4.) * wxs[p] * wsr * Gy[q * ny + j];
+            if (q == j) val -= (C.dy * E.dth / 4.) * wys[q] * wcr * Gx[p * nx + i];
+        }
+        M[k] = val;
+    }
+    __syncthreads();
+    for (int k = 0; k < nn; ++k) {
+        if (threadIdx.x == 0) {
+            int best = k;
+            double bv = fabs(M[k * ld + k]);
+            for (int i = k + 1; i < nn; ++i) {
+                const double a = fabs(M[i * ld + k]);
+                if (a > bv) {
+                    bv = a;
+                    best = i;
+                }
+            }
+            piv = best;
+            pval = M[best * ld + k];
+            if (!(bv > 0.)) atomicExch(status, 1);
+        }
+        __syncthreads();
+        if (piv != k)
+            for (int c = threadIdx.x; c < ld; c += blockDim.x) {
+                const double t = M[k * ld + c];
+                M[k * ld + c] = M[piv * ld + c];
+                M[piv * ld + c] = t;
+            }
+        __syncthreads();
+        const double inv = pval != 0. ? 1. / pval : 0.;
+        for (int c = threadIdx.x; c < ld; c += blockDim.x) M[k * ld + c] *= inv;
+        __syncthreads();
+        for (int t = threadIdx.x; t < nn * ld; t += blockDim.x) {
+            const int i = t / ld, c = t % ld;
+            if (i == k || c == k) continue;
+            M[t] -= M[i * ld + k] * M[k * ld + c];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nn; i += blockDim.x)
+            if (i != k) M[i * ld + k] = 0.;
+        __syncthreads();
+    }
+    double* o64 = inv64 + blk_off[b];
+    float* o32 = inv32 + blk_off[b];
+    for (int t = threadIdx.x; t < nn * nn; t += blockDim.x) {
+        const double val = M[(t / nn) * ld + nn + (t % nn)];
+        o64[t] = val;
+        o32[t] = (float)val;
+    }
+}
+
+// One level of the sweep: z_e = B_e^{-1} (rin_e - sum_upwind C_ee' z_e').
+template <typename T>
+__global__ void __launch_bounds__(kSweepThreads)
+sweep_level_kernel(OpView<T> v, const int32_t* __restrict__ level_elems, const uint8_t* __restrict__ active,
+                   const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
+                   const T* __restrict__ rin, T* __restrict__ z) {
+    extern __shared__ unsigned char sraw[];
+    T* rhs = reinterpret_cast<T*>(sraw);
+    const int e = level_elems[blockIdx.x];
+    const ElemDev E = v.elems[e];
+    const ColDev C = v.cols[E.col];
+    const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
+    const int bm = E.flags >> 4;
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+        const bool bd = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) || ((bm & 4) && i == 0) ||
+                        ((bm & 8) && j == 0);
+        T acc = bd ? T(0) : rin[E.dof_off + l];
+        if (!bd) {
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                if (!active[k]) continue;
+                const CplDev cp = v.cpls[k];
+                const int F = cp.face;
+                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                (F == 3 && j == 0);
+                if (!on) continue;
+                const ElemDev E1 = v.elems[cp.nbr];
+                const ColDev C1 = v.cols[E1.col];
+                const int nth1 = E1.nth;
+                const int q = (F % 2 == 0) ? j : i;
+                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                const T* Es = v.mort + cp.es;
+                const T* Et = v.mort + cp.et;
+                int64_t base, stride;
+                int m1;
+                if (F % 2 == 0) {
+                    base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
+                    stride = nth1;
+                    m1 = C1.ny;
+                } else {
+                    base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
+                    stride = (int64_t)C1.ny * nth1;
+                    m1 = C1.nx;
+                }
+                const T dc = T(cp.dcoeff);
+                for (int jj = 0; jj < m1; ++jj) {
+                    const T es = dc * Es[jj * n0 + q];
+                    const T* zl = z + base + jj * stride;
+                    for (int a = 0; a < nth1; ++a) acc -= es * Et[a * nth + r] * zl[a];
+                }
+            }
+        }
+        rhs[l] = acc;
+    }
+    __syncthreads();
+    const T* B = inv + inv_elem_off[e];
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int r = l % nth, ij = l / nth;
+        const T* row = B + ((int64_t)r * nn + ij) * nn;
+        T acc = T(0);
+        for (int k = 0; k < nn; ++k) acc += row[k] * rhs[k * nth + r];
+        z[E.dof_off + l] = acc;
+    }
+}
+
+}  // namespace
+
+struct Sweep {
+    int nlev = 0;
+    std::vector<int32_t> lev_start;      // host CSR over levels
+    int32_t* d_lev_elems = nullptr;
+    uint8_t* d_active = nullptr;
+    double* d_inv64 = nullptr;
+    float* d_inv32 = nullptr;
+    int64_t* d_inv_off = nullptr;
+    int64_t inv_entries = 0;
+    int max_nloc = 0;
+    int n_lagged = 0;
+    std::vector<void*> allocs;
+    // captured graphs per precision
+    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+    double *r64 = nullptr, *z64 = nullptr;
+    float *r32 = nullptr, *z32 = nullptr;
+};
+
+namespace {
+
+template <typename T>
+T* sw_alloc(Sweep* s, size_t n) {
+    void* p = nullptr;
+    RTG_CUDA(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)));
+    s->allocs.push_back(p);
+    return (T*)p;
+}
+
+}  // namespace
+
+void free_sweep(rtg_handle* h) {
+    Sweep* s = h->sweep;
+    if (!s) return;
+    if (s->g64) cudaGraphExecDestroy(s->g64);
+    if (s->g32) cudaGraphExecDestroy(s->g32);
+    for (void* p : s->allocs) cudaFree(p);
+    delete s;
+    h->sweep = nullptr;
+}
+
+Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
+    if (h->sweep) return h->sweep;
+    const HostTables& t = h->host;
+    const int ne = (int)t.elems.size();
+    for (const ColDev& C : t.cols)
+        if (C.nx * C.ny > kMaxBlock)
+            throw RtgError{RTG_ERR_SIZE, "sweep preconditioner supports nx*ny <= 100"};
+    Sweep* s = new Sweep();
+    h->sweep = s;
+    // ---- upwind order: Kahn levels with cycle breaking
+    std::vector<std::vector<int32_t>> succ(ne);
+    std::vector<int32_t> indeg(ne, 0);
+    for (int e = 0; e < ne; ++e)
+        for (int k = t.elems[e].cpl_begin; k < t.elems[e].cpl_end; ++k) {
+            const int p = t.cpls[k].nbr;
+            if (p == e) continue;
+            succ[p].push_back(e);
+            indeg[e]++;
+        }
+    // Kahn's algorithm, ready elements taken lowest level first; a cycle is
+    // broken by forcing the lowest-index unprocessed element.
+    std::vector<int32_t> level(ne, -1);
+    std::vector<char> done(ne, 0);
+    std::vector<int32_t> order;
+    order.reserve(ne);
+    std::priority_queue<std::pair<int, int>, std::vector<std::pair<int, int>>, std::greater<>> ready;
+    std::vector<int32_t> lvl_pred(ne, 0);  // 1 + max level of processed predecessors
+    for (int e = 0; e < ne; ++e)
+        if (indeg[e] == 0) ready.push({0, e});
+    int processed = 0;
+    int next_forced = 0;
+    while (processed < ne) {
+        if (ready.empty()) {
+            // cycle: force the lowest-index unprocessed element
+            while (next_forced < ne && done[next_forced]) ++next_forced;
+            const int e = next_forced;
+            s->n_lagged += indeg[e];
+            indeg[e] = 0;
+            ready.push({lvl_pred[e], e});
+        }
+        const auto top = ready.top();
+        ready.pop();
+        const int e = top.second;
+        if (done[e]) continue;
+        done[e] = 1;
+        level[e] = lvl_pred[e];
+        order.push_back(e);
+        ++processed;
+        for (int q : succ[e]) {
+            if (done[q]) continue;
+            lvl_pred[q] = std::max(lvl_pred[q], level[e] + 1);
+            if (--indeg[q] == 0) ready.push({lvl_pred[q], q});
+        }
+    }
+    int nlev = 0;
+    for (int e = 0; e < ne; ++e) nlev = std::max(nlev, level[e] + 1);
+    s->nlev = nlev;
+    s->lev_start.assign(nlev + 1, 0);
+    for (int e = 0; e < ne; ++e) s->lev_start[level[e] + 1]++;
+    for (int L = 0; L < nlev; ++L) s->lev_start[L + 1] += s->lev_start[L];
+    std::vector<int32_t> lev_elems(ne), fill(s->lev_start.begin(), s->lev_start.end() - 1);
+    for (int e = 0; e < ne; ++e) lev_elems[fill[level[e]]++] = e;
+    // a coupling is active when its upwind element sits on an earlier level
+    std::vector<uint8_t> active(t.cpls.size(), 0);
+    for (int e = 0; e < ne; ++e)
+        for (int k = t.elems[e].cpl_begin; k < t.elems[e].cpl_end; ++k)
+            active[k] = level[t.cpls[k].nbr] < level[e] ? 1 : 0;
+    // ---- element block inverses
+    std::vector<int32_t> blk_elem, blk_r;
+    std::vector<int64_t> blk_off, inv_off(ne);
+    int64_t off = 0;
+    int max_nn = 1;
+    for (int e = 0; e < ne; ++e) {
+        const ElemDev& E = t.elems[e];
+        const ColDev& C = t.cols[E.col];
+        const int nn = C.nx * C.ny;
+        max_nn = std::max(max_nn, nn);
+        s->max_nloc = std::max(s->max_nloc, nn * E.nth);
+        inv_off[e] = off;
+        for (int r = 0; r < E.nth; ++r) {
+            blk_elem.push_back(e);
+            blk_r.push_back(r);
+            blk_off.push_back(off);
+            off += (int64_t)nn * nn;
+        }
+    }
+    s->inv_entries = off;
+    s->d_lev_elems = sw_alloc<int32_t>(s, ne);
+    s->d_active = sw_alloc<uint8_t>(s, active.size());
+    s->d_inv_off = sw_alloc<int64_t>(s, ne);
+    s->d_inv64 = sw_alloc<double>(s, off);
+    s->d_inv32 = sw_alloc<float>(s, off);
+    int32_t* d_be = sw_alloc<int32_t>(s, blk_elem.size());
+    int32_t* d_br = sw_alloc<int32_t>(s, blk_r.size());
+    int64_t* d_bo = sw_alloc<int64_t>(s, blk_off.size());
+    int* d_status = sw_alloc<int>(s, 1);
+    RTG_CUDA(cudaMemcpy(s->d_lev_elems, lev_elems.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
+    if (!active.empty())
+        RTG_CUDA(cudaMemcpy(s->d_active, active.data(), active.size(), cudaMemcpyHostToDevice));
+    RTG_CUDA(cudaMemcpy(s->d_inv_off, inv_off.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
+    RTG_CUDA(cudaMemcpy(d_be, blk_elem.data(), sizeof(int32_t) * blk_elem.size(), cudaMemcpyHostToDevice));
+    RTG_CUDA(cudaMemcpy(d_br, blk_r.data(), sizeof(int32_t) * blk_r.size(), cudaMemcpyHostToDevice));
+    RTG_CUDA(cudaMemcpy(d_bo, blk_off.data(), sizeof(int64_t) * blk_off.size(), cudaMemcpyHostToDevice));
+    RTG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
+    const size_t smem = sizeof(double) * (size_t)max_nn * 2 * max_nn;
+    RTG_CUDA(cudaFuncSetAttribute(build_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    build_block_inverse_kernel<<<(int)blk_elem.size(), 256, smem, st>>>(h->v64, d_be, d_br, d_bo, s->d_inv64,
+                                                                         s->d_inv32, d_status);
+    RTG_CUDA(cudaGetLastError());
+    int status = 0;
+    RTG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RTG_CUDA(cudaStreamSynchronize(st));
+    if (status) throw RtgError{RTG_ERR_NONFINITE, "singular element block in the sweep preconditioner"};
+    s->r64 = sw_alloc<double>(s, (size_t)t.ndof);
+    s->z64 = sw_alloc<double>(s, (size_t)t.ndof);
+    s->r32 = sw_alloc<float>(s, (size_t)t.ndof);
+    s->z32 = sw_alloc<float>(s, (size_t)t.ndof);
+    return s;
+}
+
+template <typename T>
+void sweep_levels(const rtg_handle* h, const Sweep* s, const OpView<T>& v, const T* inv, const T* r, T* z,
+                  cudaStream_t st) {
+    const size_t smem = sizeof(T) * (size_t)std::max(s->max_nloc, 1);
+    for (int L = 0; L < s->nlev; ++L) {
+        const int n = s->lev_start[L + 1] - s->lev_start[L];
+        if (n == 0) continue;
+        sweep_level_kernel<T><<<n, kSweepThreads, smem, st>>>(v, s->d_lev_elems + s->lev_start[L], s->d_active,
+                                                             inv, s->d_inv_off, r, z);
+    }
+}
+
+// z = P^{-1} r (full-length vectors; inflow-boundary entries of z are zero).
+template <typename T>
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
+    Sweep* s = get_sweep(h, st);
+    const bool f64 = sizeof(T) == 8;
+    cudaGraphExec_t& g = f64 ? s->g64 : s->g32;
+    T* rb = f64 ? (T*)s->r64 : (T*)s->r32;
+    T* zb = f64 ? (T*)s->z64 : (T*)s->z32;
+    const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
+    const OpView<T>& v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
+    if (!g) {
+        cudaStream_t cap;
+        RTG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        RTG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        sweep_levels<T>(h, s, v, inv, rb, zb, cap);
+        RTG_CUDA(cudaStreamEndCapture(cap, &graph));
+        RTG_CUDA(cudaGraphInstantiate(&g, graph, 0));
+        RTG_CUDA(cudaGraphDestroy(graph));
+        RTG_CUDA(cudaStreamDestroy(cap));
+    }
+    RTG_CUDA(cudaMemcpyAsync(rb, r, sizeof(T) * (size_t)h->host.ndof, cudaMemcpyDeviceToDevice, st));
+    RTG_CUDA(cudaGraphLaunch(g, st));
+    RTG_CUDA(cudaMemcpyAsync(z, zb, sizeof(T) * (size_t)h->host.ndof, cudaMemcpyDeviceToDevice, st));
+}
+
+template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);
+template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t);
+
+int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
+int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
+
+}  // namespace rtg

@@ -62,7 +62,7 @@ class SolveInfo(C.Structure):
     _fields_ = [("converged", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
                 ("fp64_applies", C.c_int32), ("fp32_applies", C.c_int32), ("res0", C.c_double),
                 ("res_f", C.c_double), ("rhs_norm", C.c_double), ("seconds", C.c_double),
-                ("hist_len", C.c_int32)]
+                ("hist_len", C.c_int32), ("sweeps", C.c_int32)]
 
 
 # exported symbol -> (restype, argtypes)

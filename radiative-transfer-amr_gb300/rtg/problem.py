@@ -86,7 +86,7 @@ class DeviceContext:
         if isinstance(v, torch.Tensor):
             t = v.to(device=self.device, dtype=dtype)
         else:
-            t = torch.as_tensor(np.asarray(v), dtype=dtype).to(self.device)
+            t = torch.as_tensor(np.array(v, dtype=np.float64), dtype=dtype).to(self.device)
         t = t.contiguous()
         if t.numel() != self.N:
             raise ValueError("vector length {} != ndof {}".format(t.numel(), self.N))
@@ -331,7 +331,7 @@ class Problem:
         (FP32 GMRES inside FP64 iterative refinement); restart (50), max_it
         (5000), rtol (1e-12; the reference asks PETSc for 1e-15), atol (0),
         x0 ("forcing" = start from f_I as the reference does, or "zero")."""
-        opts = {"verbose": False, "ksp_type": "gmres", "pc_type": "none", "restart": 50,
+        opts = {"verbose": False, "ksp_type": "gmres", "pc_type": "sweep", "restart": 50,
                 "max_it": 5000, "rtol": 1e-12, "atol": 0., "x0": "forcing",
                 "inner_rtol": 1e-6}
         opts.update(kwargs)
@@ -342,10 +342,15 @@ class Problem:
         method = {"gmres": 0, "mixed": 1, "fgmres": 0}.get(opts["ksp_type"])
         if method is None:
             raise ValueError("unsupported ksp_type {}".format(opts["ksp_type"]))
+        # PETSc's "bjacobi" default maps to the sweep, the GPU preconditioner
+        precond = {"none": 0, "sweep": 1, "bjacobi": 1}.get(opts["pc_type"])
+        if precond is None:
+            raise ValueError("unsupported pc_type {}".format(opts["pc_type"]))
         x0 = f_dev if opts["x0"] == "forcing" else None
         u, info = ctx.solve(f_dev, g_dev, method=method, restart=int(opts["restart"]),
                             max_it=int(opts["max_it"]), rtol=float(opts["rtol"]),
-                            atol=float(opts["atol"]), x0=x0, inner_rtol=float(opts["inner_rtol"]))
+                            atol=float(opts["atol"]), x0=x0, inner_rtol=float(opts["inner_rtol"]),
+                            precond=precond)
         uh = Projection(mesh)
         uh.from_vector(u.cpu().numpy())
         hist = info["history"]

@@ -24,6 +24,25 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+def test_unpreconditioned_fp64_gmres(case):
+    name, g, mesh, prob, _ = case
+    if name == "hp_hanging":
+        pytest.skip("unpreconditioned GMRES(50) stagnates on this mesh; covered with the sweep")
+    uh, conv, minfo = prob.solve(mesh, ksp_type="gmres", pc_type="none", rtol=1e-13, max_it=20000)
+    u = uh.to_vector()
+    assert conv["converged_reason"] > 0, conv["res_f"]
+    assert _rel(u, g["u"]) < 1e-10, _rel(u, g["u"])
+
+
+def test_sweep_preconditioner_cuts_iterations(case):
+    name, g, mesh, prob, _ = case
+    _, c0, _ = prob.solve(mesh, pc_type="none", rtol=1e-10, max_it=3000)
+    uh, c1, _ = prob.solve(mesh, pc_type="sweep", rtol=1e-10, max_it=3000)
+    assert c1["converged_reason"] > 0
+    assert c1["iteration_number"] < c0["iteration_number"], (c1["iteration_number"], c0["iteration_number"])
+    assert _rel(uh.to_vector(), g["u"]) < 1e-7
+
+
 def test_plain_fp64_gmres(case):
     name, g, mesh, prob, _ = case
     uh, conv, minfo = prob.solve(mesh, ksp_type="gmres", rtol=1e-14, max_it=20000)
