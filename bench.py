@@ -47,7 +47,42 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="short run for ncu: one warm and one measured solve per method, 3 applies")
     return ap.parse_args()
+
+
+def run_profile(args):
+    """Minimal launch sequence for profiling: set-up, then per method one warm
+    and one measured solve, then three FP32 and three FP64 system applies."""
+    import torch
+    from rtg import Problem, _lib
+    torch.cuda.set_device(0)
+    desc, mesh, spec = workload(args.workload)
+    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    ctx = prob.context(mesh)
+    f_dev = ctx.forcing(spec.f)
+    g_dev = ctx.inflow(spec.bcs_dirac)
+    out = {}
+    for method in (1, 0):
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=1e-9, max_it=20000, precond=1)
+            torch.cuda.synchronize()
+            out["method%d_rep%d" % (method, rep)] = {"s": time.perf_counter() - t0,
+                                                     "iterations": info["iterations"],
+                                                     "sweeps": info["sweeps"]}
+    for prec in (_lib.RTG_FP32, _lib.RTG_FP64):
+        dt = torch.float32 if prec == _lib.RTG_FP32 else torch.float64
+        x = torch.randn(ctx.N, dtype=dt, device=ctx.device)
+        y = torch.empty_like(x)
+        for _ in range(3):
+            ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec)
+    torch.cuda.synchronize()
+    out["ndof"] = ctx.N
+    out["info"] = ctx.info
+    print(json.dumps(out))
 
 
 def workload(name, seed=0):
@@ -332,6 +367,9 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.profile:
+        run_profile(args)
+        return
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:
         print(json.dumps(out))
