@@ -186,6 +186,25 @@ int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u,
               const rtg_solve_opts* opts, rtg_solve_info* info,
               double* hist, int hist_cap, void* stream);
 
+/* allocation-free inner products --------------------------------------------
+ * No counterpart in the reference: this is the two-stage reduction rtg_solve
+ * uses for its Arnoldi inner products and residual norms, offered to callers
+ * that may not allocate device memory (a host whose memory manager owns every
+ * device allocation, or a caller running its own Krylov loop around
+ * rtg_apply where a cudaMalloc would stall or break the surrounding work).
+ * out[q] = sum_{i<n} V[q*ldv + i] * w[i] for q < k, written to the caller's
+ * device array out (k doubles) on `stream`.  V, w, out: device pointers; ldv
+ * >= n when k > 1 (ignored for k == 1).  k must be in [1, 64]: the per-CTA
+ * partial sums live in one static device array of 296 x 64 doubles
+ * (151,552 bytes) that every GPU loading the library holds until exit; k > 64
+ * returns RTG_ERR_SIZE.  Nothing is allocated.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress) with the device
+ * current, so make the first call on each device before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller; each call overwrites every partial sum it reads. */
+int rtg_dots_noalloc(int k, const double* V, int64_t ldv, const double* w, int64_t n,
+                     double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
