@@ -3,6 +3,14 @@
 // (cell-major, then i, j, a), the scattering block is dense over the column's
 // angular nodes and diagonal in the spatial node (i, j), and the streaming
 // terms stay inside one element, so a column is the natural unit of work.
+//
+// Fast path (apply_col_kernel): the column's input is staged in shared memory
+// transposed to [angular row R][spatial node ij] (and, when it fits, the
+// column's angular scattering matrix W), then every output DOF is computed
+// from shared memory and written in global order (coalesced).  Columns too
+// large for shared memory use apply_global_kernel, which reads its operands
+// from global memory.
+#include <algorithm>
 #include <cstdio>
 
 #include "rtg_internal.h"
@@ -12,37 +20,225 @@ namespace rtg {
 namespace {
 
 constexpr int kApplyThreads = 256;
+constexpr int kMaxCellsStaged = 64;
+constexpr size_t kSmemBudget = 200 * 1024;
 
 __device__ __forceinline__ int gofs(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
 
 template <typename T>
 __device__ __forceinline__ T tabs(T v) { return v < T(0) ? -v : v; }
 
-// y = Op(flags) x for the DOFs of one column.
-// kParity: apply the reference's drop rules (|entry| <= 1e-14 in the (M - S)
-// blocks, |entry| <= 1e-15 in the face terms, skip of cross-cell scattering
-// where |wx wy sigma| <= 1e-14) so FP64 results match the assembled matrices.
+__device__ __forceinline__ bool bdry_node(int bm, int i, int j, int nx, int ny) {
+    return ((bm & 1) && i == nx - 1) || ((bm & 2) && j == ny - 1) || ((bm & 4) && i == 0) ||
+           ((bm & 8) && j == 0);
+}
+
+// Face terms of one output node: outflow diagonal or inflow mortar couplings
+// to neighbour elements (rt/boundary_convection_matrix.py:258-524).
+// xself: the node's own input value.
+template <typename T, typename TX, bool kParity>
+__device__ __forceinline__ T face_terms(const OpView<T>& v, const ColDev& C, const ElemDev& E, int e, int i,
+                                        int j, int r, T xself, const TX* __restrict__ x) {
+    const T bctol = T(kBcTol);
+    const int nth = E.nth;
+    const T* A = v.ang + E.ang;
+    T acc = T(0);
+    for (int F = 0; F < 4; ++F) {
+        const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                        (F == 3 && j == 0);
+        if (!on) continue;
+        if (E.flags & (1 << F)) {
+            const T dc = (F % 2 == 0) ? v.econst[4 * e + 2] : v.econst[4 * e + 1];
+            const T w = (F % 2 == 0) ? v.lglw[C.ny * kMaxNodes + j] : v.lglw[C.nx * kMaxNodes + i];
+            const T val = dc * w * A[r] * A[(3 + F) * nth + r];
+            if (!kParity || tabs(val) > bctol) acc += val * xself;
+            continue;
+        }
+        const int q = (F % 2 == 0) ? j : i;
+        const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+        for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+            const CplDev cp = v.cpls[k];
+            if (cp.face != F) continue;
+            const ElemDev E1 = v.elems[cp.nbr];
+            const ColDev C1 = v.cols[E1.col];
+            const int nth1 = E1.nth;
+            const T* Es = v.mort + cp.es;
+            const T* Et = v.mort + cp.et;
+            const T dc = v.cplc[k];
+            int64_t base, stride;
+            int m1;
+            if (F % 2 == 0) {
+                base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
+                stride = nth1;
+                m1 = C1.ny;
+            } else {
+                base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
+                stride = (int64_t)C1.ny * nth1;
+                m1 = C1.nx;
+            }
+            for (int jj = 0; jj < m1; ++jj) {
+                const T es = Es[jj * n0 + q];
+                const TX* xl = x + base + jj * stride;
+                if (kParity) {
+                    for (int a = 0; a < nth1; ++a) {
+                        const T val = dc * es * Et[a * nth + r];
+                        if (tabs(val) > bctol) acc += val * T(xl[a]);
+                    }
+                } else {
+                    T s = T(0);
+                    for (int a = 0; a < nth1; ++a) s += Et[a * nth + r] * T(xl[a]);
+                    acc += dc * es * s;
+                }
+            }
+        }
+    }
+    return acc;
+}
+
+struct ApplyFlags {
+    bool scat, mass, merged, ic, bc, mask_rows;
+    float ic_sign;
+};
+
+__device__ __forceinline__ ApplyFlags decode(uint32_t flags) {
+    ApplyFlags f;
+    const bool sys = flags & RTG_SYSTEM;
+    f.scat = sys || (flags & RTG_SCAT);
+    f.mass = sys || (flags & RTG_MASS);
+    f.merged = f.scat && f.mass;   // (M - S) block with the joint drop rule
+    f.ic = sys || (flags & RTG_IC);
+    f.ic_sign = sys ? -1.f : 1.f;
+    f.bc = sys || (flags & RTG_BC);
+    f.mask_rows = flags & RTG_MASK_ROWS;
+    return f;
+}
+
+// ---------------------------------------------------------------- fast path
+// Shared memory: Xs[Nth][nij] | Ws[Nth][ldw] (optional) | cell tables.
 template <typename T, typename TX, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
-apply_kernel(OpView<T> v, uint32_t flags, const TX* __restrict__ x, TX* __restrict__ y) {
-    const int ci = blockIdx.x;
+apply_col_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols, int stage_w,
+                 const TX* __restrict__ x, TX* __restrict__ y) {
+    extern __shared__ unsigned char smraw[];
+    const int ci = cols[blockIdx.x];
     const ColDev C = v.cols[ci];
-    const bool sys = flags & RTG_SYSTEM;
-    const bool do_scat = sys || (flags & RTG_SCAT);
-    const bool do_mass = sys || (flags & RTG_MASS);
-    const bool merged = do_scat && do_mass;   // (M - S) block with the joint drop rule
-    const bool do_ic = sys || (flags & RTG_IC);
-    const T ic_sign = sys ? T(-1) : T(1);
-    const bool do_bc = sys || (flags & RTG_BC);
-    const bool mask_rows = flags & RTG_MASK_ROWS;
-    const T small = T(kSmall), bctol = T(kBcTol);
-    const T* W = v.W + v.W_off[C.sig];
-    const T* wxs = v.lglw + C.nx * kMaxNodes;
-    const T* wys = v.lglw + C.ny * kMaxNodes;
+    const ApplyFlags fl = decode(flags);
+    const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
+    const int ldw = Nth | 1;   // odd row stride: rows of W land in different banks
+    T* Xs = reinterpret_cast<T*>(smraw);
+    T* Ws = Xs + (size_t)Nth * nij;
+    int* cbeg = reinterpret_cast<int*>(Ws + (stage_w ? (size_t)Nth * ldw : 0));  // [ncell+1] local DOF start
+    int* crow = cbeg + ncell + 1;                                                // [ncell] first row
+    __shared__ T s_dxdy8;
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int k = 0; k < ncell; ++k) {
+            const ElemDev E = v.elems[C.elem_begin + k];
+            cbeg[k] = off;
+            crow[k] = E.row;
+            off += nij * E.nth;
+        }
+        cbeg[ncell] = off;
+        s_dxdy8 = v.colc[ci];
+    }
+    __syncthreads();
+    const TX* xc = x + C.dof_off;
+    // stage x transposed: Xs[(row_e + a) * nij + ij] = x[off_e + ij*nth + a]
+    for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
+        int k = 0;
+        while (d >= cbeg[k + 1]) ++k;
+        const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
+        const int l = d - cbeg[k];
+        Xs[(crow[k] + l % nth) * nij + l / nth] = T(xc[d]);
+    }
+    const T* Wg = v.W + v.W_off[C.sig];
+    if (stage_w)
+        for (int t = threadIdx.x; t < Nth * Nth; t += blockDim.x) Ws[(t / Nth) * ldw + (t % Nth)] = Wg[t];
+    __syncthreads();
+    const T small = T(kSmall);
+    const T dxdy8 = s_dxdy8;
     const T* Gx = v.G + gofs(C.nx);
     const T* Gy = v.G + gofs(C.ny);
-    const T dxdy8 = T(C.dx * C.dy / 8.);
+    TX* yc = y + C.dof_off;
+    for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
+        int k = 0;
+        while (d >= cbeg[k + 1]) ++k;
+        const int e = C.elem_begin + k;
+        const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
+        const int l = d - cbeg[k];
+        const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+        const ElemDev E = v.elems[e];
+        const int bm = E.flags >> 4;
+        if (fl.mask_rows && bdry_node(bm, i, j, C.nx, C.ny)) {
+            yc[d] = TX(0);
+            continue;
+        }
+        const int R = crow[k] + r;
+        const T* A = v.ang + E.ang;
+        const T xself = Xs[R * nij + ij];
+        const int node = C.node_off + ij;
+        T acc = T(0);
+        if (fl.scat) {
+            const T swv = v.sw[node];
+            const T cw = dxdy8 * swv;
+            const T mself = fl.merged ? v.econst[4 * e] * A[r] * v.kw[node] : T(0);
+            if (kParity) {
+                // reference drop rules (rt/preconditioner_matrix.py:450-495)
+                const bool skip_cross = !(tabs(swv) > small);
+                const int c0 = skip_cross ? crow[k] : 0;
+                const int c1 = skip_cross ? crow[k] + nth : Nth;
+                for (int c = c0; c < c1; ++c) {
+                    const T wv = stage_w ? Ws[R * ldw + c] : Wg[(int64_t)R * Nth + c];
+                    T val = -cw * wv;
+                    if (c == R) val += mself;
+                    if (tabs(val) > small) acc += val * Xs[c * nij + ij];
+                }
+            } else {
+                T s = T(0);
+                if (stage_w) {
+                    const T* wr = Ws + R * ldw;
+#pragma unroll 4
+                    for (int c = 0; c < Nth; ++c) s += wr[c] * Xs[c * nij + ij];
+                } else {
+                    const T* wr = Wg + (int64_t)R * Nth;
+#pragma unroll 4
+                    for (int c = 0; c < Nth; ++c) s += wr[c] * Xs[c * nij + ij];
+                }
+                acc = -cw * s + mself * xself;
+            }
+        }
+        if (fl.mass && !fl.merged) acc += v.econst[4 * e] * A[r] * v.kw[node] * xself;
+        if (fl.ic) {
+            // interior streaming, sum-factorised (rt/interior_convection_matrix.py:161-243)
+            const T* xr = Xs + R * nij;
+            T t1 = T(0), t2 = T(0);
+            const T* gy = Gy + j * C.ny;
+            for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
+            const T* gx = Gx + i * C.nx;
+            for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * xr[ii * C.ny + j];
+            const T ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
+                         v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
+            acc += T(fl.ic_sign) * ic;
+        }
+        if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1))
+            acc += face_terms<T, TX, kParity>(v, C, E, e, i, j, r, xself, x);
+        yc[d] = TX(acc);
+    }
+}
 
+// ------------------------------------------------------------ global path
+template <typename T, typename TX, bool kParity>
+__global__ void __launch_bounds__(kApplyThreads)
+apply_global_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols,
+                    const TX* __restrict__ x, TX* __restrict__ y) {
+    const int ci = cols[blockIdx.x];
+    const ColDev C = v.cols[ci];
+    const ApplyFlags fl = decode(flags);
+    const T small = T(kSmall);
+    const T* W = v.W + v.W_off[C.sig];
+    const T* Gx = v.G + gofs(C.nx);
+    const T* Gy = v.G + gofs(C.ny);
+    const T dxdy8 = v.colc[ci];
     for (int e = C.elem_begin; e < C.elem_end; ++e) {
         const ElemDev E = v.elems[e];
         const int nth = E.nth;
@@ -50,25 +246,20 @@ apply_kernel(OpView<T> v, uint32_t flags, const TX* __restrict__ x, TX* __restri
         const TX* xe = x + E.dof_off;
         const T* A = v.ang + E.ang;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-            const int r = l % nth;
-            const int ij = l / nth;
-            const int j = ij % C.ny;
-            const int i = ij / C.ny;
-            const int bm = E.flags >> 4;
-            const bool bdry = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) ||
-                              ((bm & 4) && i == 0) || ((bm & 8) && j == 0);
-            if (mask_rows && bdry) {
+            const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+            if (fl.mask_rows && bdry_node(E.flags >> 4, i, j, C.nx, C.ny)) {
                 y[E.dof_off + l] = TX(0);
                 continue;
             }
             T acc = T(0);
             const int node = C.node_off + ij;
-            // ---- extinction and scattering (rt/preconditioner_matrix.py:363-514)
-            if (do_scat) {
+            const T xself = T(xe[l]);
+            if (fl.scat) {
                 const T swv = v.sw[node];
                 const T cw = dxdy8 * swv;
                 const T* Wr = W + (int64_t)(E.row + r) * C.nth_col;
                 const bool skip_cross = kParity && !(tabs(swv) > small);
+                const T mself = fl.merged ? v.econst[4 * e] * A[r] * v.kw[node] : T(0);
                 for (int e1 = C.elem_begin; e1 < C.elem_end; ++e1) {
                     if (skip_cross && e1 != e) continue;
                     const ElemDev E1 = v.elems[e1];
@@ -76,18 +267,14 @@ apply_kernel(OpView<T> v, uint32_t flags, const TX* __restrict__ x, TX* __restri
                     const T* W1 = Wr + E1.row;
                     for (int a = 0; a < E1.nth; ++a) {
                         T val = -cw * W1[a];
-                        if (merged && e1 == e && a == r)
-                            val += dxdy8 * T(E.dth) * A[r] * v.kw[node];
+                        if (e1 == e && a == r) val += mself;
                         if (kParity && !(tabs(val) > small)) continue;
                         acc += val * T(x1[a]);
                     }
                 }
             }
-            if (do_mass && !merged) {
-                acc += dxdy8 * T(E.dth) * A[r] * v.kw[node] * T(xe[l]);
-            }
-            // ---- interior streaming (rt/interior_convection_matrix.py:161-243)
-            if (do_ic) {
+            if (fl.mass && !fl.merged) acc += v.econst[4 * e] * A[r] * v.kw[node] * xself;
+            if (fl.ic) {
                 T t1 = T(0), t2 = T(0);
                 const T* gy = Gy + j * C.ny;
                 const TX* xi = xe + (int64_t)i * C.ny * nth + r;
@@ -95,62 +282,12 @@ apply_kernel(OpView<T> v, uint32_t flags, const TX* __restrict__ x, TX* __restri
                 const T* gx = Gx + i * C.nx;
                 const TX* xj = xe + (int64_t)j * nth + r;
                 for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * T(xj[(int64_t)ii * C.ny * nth]);
-                const T ic = T(C.dx * E.dth / 4.) * wxs[i] * A[nth + r] * t1 +
-                             T(C.dy * E.dth / 4.) * wys[j] * A[2 * nth + r] * t2;
-                acc += ic_sign * ic;
+                const T ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
+                             v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
+                acc += T(fl.ic_sign) * ic;
             }
-            // ---- face terms (rt/boundary_convection_matrix.py:258-524)
-            if (do_bc) {
-                for (int F = 0; F < 4; ++F) {
-                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) ||
-                                    (F == 2 && i == 0) || (F == 3 && j == 0);
-                    if (!on) continue;
-                    if (E.flags & (1 << F)) {
-                        const T dc = (F % 2 == 0) ? T(C.dy * E.dth / 4.) : T(C.dx * E.dth / 4.);
-                        const T w = (F % 2 == 0) ? wys[j] : wxs[i];
-                        const T val = dc * w * A[r] * A[(3 + F) * nth + r];
-                        if (!kParity || tabs(val) > bctol) acc += val * T(xe[l]);
-                        continue;
-                    }
-                    const int q = (F % 2 == 0) ? j : i;
-                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
-                    for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
-                        const CplDev cp = v.cpls[k];
-                        if (cp.face != F) continue;
-                        const ElemDev E1 = v.elems[cp.nbr];
-                        const ColDev C1 = v.cols[E1.col];
-                        const int nth1 = E1.nth;
-                        const T* Es = v.mort + cp.es;
-                        const T* Et = v.mort + cp.et;
-                        const T dc = T(cp.dcoeff);
-                        int64_t base, stride;
-                        int m1;
-                        if (F % 2 == 0) {
-                            const int xi1 = (F == 0) ? 0 : C1.nx - 1;
-                            base = E1.dof_off + (int64_t)xi1 * C1.ny * nth1;
-                            stride = nth1;
-                            m1 = C1.ny;
-                        } else {
-                            const int yi1 = (F == 1) ? 0 : C1.ny - 1;
-                            base = E1.dof_off + (int64_t)yi1 * nth1;
-                            stride = (int64_t)C1.ny * nth1;
-                            m1 = C1.nx;
-                        }
-                        for (int jj = 0; jj < m1; ++jj) {
-                            const T es = dc * Es[jj * n0 + q];
-                            const TX* xl = x + base + jj * stride;
-                            for (int a = 0; a < nth1; ++a) {
-                                if (kParity) {
-                                    const T val = T(cp.dcoeff) * Es[jj * n0 + q] * Et[a * nth + r];
-                                    if (tabs(val) > bctol) acc += val * T(xl[a]);
-                                } else {
-                                    acc += es * Et[a * nth + r] * T(xl[a]);
-                                }
-                            }
-                        }
-                    }
-                }
-            }
+            if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1))
+                acc += face_terms<T, TX, kParity>(v, C, E, e, i, j, r, xself, x);
             y[E.dof_off + l] = TX(acc);
         }
     }
@@ -160,10 +297,7 @@ __device__ __forceinline__ bool is_bdry(const ElemDev& E, const ColDev& C, int l
     const int bm = E.flags >> 4;
     if (!bm) return false;
     const int ij = l / E.nth;
-    const int j = ij % C.ny;
-    const int i = ij / C.ny;
-    return ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) || ((bm & 4) && i == 0) ||
-           ((bm & 8) && j == 0);
+    return bdry_node(bm, ij / C.ny, ij % C.ny, C.nx, C.ny);
 }
 
 // One CTA per element for the elementwise kernels.
@@ -205,13 +339,84 @@ __global__ void weight_forcing_kernel(OpView<double> v, const double* f, double*
 
 }  // namespace
 
+// Column partition of the fast path, per precision: columns whose staged input
+// (and W when it fits) stay within the shared-memory budget, sorted by work
+// (largest first) so the long columns start early.
+struct ApplyPlan {
+    int32_t* d_fast = nullptr;
+    int32_t* d_slow = nullptr;
+    int nfast = 0, nslow = 0;
+    size_t smem = 0;
+    int stage_w = 0;
+    std::vector<void*> allocs;
+};
+
 template <typename T>
-void launch_apply(const rtg_handle* h, const OpView<T>& v, uint32_t flags, const T* x, T* y,
+static ApplyPlan* make_plan(const rtg_handle* h) {
+    const HostTables& t = h->host;
+    ApplyPlan* p = new ApplyPlan();
+    std::vector<std::pair<int64_t, int32_t>> fast;
+    std::vector<int32_t> slow;
+    size_t need_x = 0, need_w = 0;
+    for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
+        const ColDev& C = t.cols[ci];
+        const int ncell = C.elem_end - C.elem_begin;
+        const size_t sx = sizeof(T) * (size_t)C.ndof + sizeof(int) * (2 * ncell + 2) + 16;
+        const size_t sw = sizeof(T) * (size_t)C.nth_col * (C.nth_col | 1);
+        if (sx <= kSmemBudget && ncell <= kMaxCellsStaged) {
+            fast.push_back({(int64_t)C.ndof * (C.nth_col + C.nx + C.ny), ci});
+            need_x = std::max(need_x, sx);
+            need_w = std::max(need_w, sw);
+        } else {
+            slow.push_back(ci);
+        }
+    }
+    std::sort(fast.begin(), fast.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    p->stage_w = (need_x + need_w <= kSmemBudget) ? 1 : 0;
+    p->smem = need_x + (p->stage_w ? need_w : 0);
+    std::vector<int32_t> f32;
+    for (auto& pr : fast) f32.push_back(pr.second);
+    p->nfast = (int)f32.size();
+    p->nslow = (int)slow.size();
+    auto up = [&](const std::vector<int32_t>& v) -> int32_t* {
+        void* d = nullptr;
+        RTG_CUDA(cudaMalloc(&d, sizeof(int32_t) * std::max<size_t>(v.size(), 1)));
+        p->allocs.push_back(d);
+        if (!v.empty()) RTG_CUDA(cudaMemcpy(d, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice));
+        return (int32_t*)d;
+    };
+    p->d_fast = up(f32);
+    p->d_slow = up(slow);
+    return p;
+}
+
+void free_apply_plans(rtg_handle* h) {
+    for (ApplyPlan* p : {h->plan64, h->plan32}) {
+        if (!p) continue;
+        for (void* d : p->allocs) cudaFree(d);
+        delete p;
+    }
+    h->plan64 = h->plan32 = nullptr;
+}
+
+template <typename T>
+void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, const T* x, T* y,
                   cudaStream_t s) {
-    if (sizeof(T) == 8)
-        apply_kernel<T, T, true><<<v.ncols, kApplyThreads, 0, s>>>(v, flags, x, y);
-    else
-        apply_kernel<T, T, false><<<v.ncols, kApplyThreads, 0, s>>>(v, flags, x, y);
+    rtg_handle* h = const_cast<rtg_handle*>(hc);
+    constexpr bool f64 = sizeof(T) == 8;
+    ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
+    if (!plan) {
+        plan = make_plan<T>(h);
+        if (plan->smem > 48 * 1024) {
+            RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)plan->smem));
+        }
+    }
+    if (plan->nfast)
+        apply_col_kernel<T, T, f64><<<plan->nfast, kApplyThreads, plan->smem, s>>>(v, flags, plan->d_fast,
+                                                                                  plan->stage_w, x, y);
+    if (plan->nslow)
+        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, flags, plan->d_slow, x, y);
     RTG_CUDA(cudaGetLastError());
 }
 

@@ -563,6 +563,22 @@ void build_tables(const rtg_mesh_desc* m, const rtg_coeffs* c, HostTables& t) {
         }
     }
     (void)goff;
+    // per-element, per-column and per-coupling constants in the kernels' own precision
+    t.econst.assign(4 * (size_t)ne, 0.);
+    for (int e = 0; e < ne; ++e) {
+        const ElemDev& E = t.elems[e];
+        const ColDev& C = t.cols[E.col];
+        t.econst[4 * e + 0] = C.dx * C.dy * E.dth / 8.;
+        t.econst[4 * e + 1] = C.dx * E.dth / 4.;
+        t.econst[4 * e + 2] = C.dy * E.dth / 4.;
+    }
+    t.colc.resize(nc);
+    for (int ci = 0; ci < nc; ++ci) {
+        t.colc[ci] = t.cols[ci].dx * t.cols[ci].dy / 8.;
+        t.max_cells_col = std::max(t.max_cells_col, t.cols[ci].elem_end - t.cols[ci].elem_begin);
+    }
+    t.cplc.resize(t.cpls.size());
+    for (size_t k = 0; k < t.cpls.size(); ++k) t.cplc[k] = t.cpls[k].dcoeff;
 }
 
 }  // namespace rtg

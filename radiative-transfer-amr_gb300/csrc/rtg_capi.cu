@@ -112,6 +112,9 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
         a.G = upload(h, t.G);
         a.lglw = upload(h, t.lglw);
         a.mort = upload(h, t.mort);
+        a.econst = upload(h, t.econst);
+        a.colc = upload(h, t.colc);
+        a.cplc = upload(h, t.cplc);
         a.ncols = (int32_t)t.cols.size();
         a.nelem = (int32_t)t.elems.size();
         OpView<float>& b = h->v32;
@@ -126,6 +129,9 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
         b.G = upload(h, to_f32(t.G));
         b.lglw = upload(h, to_f32(t.lglw));
         b.mort = upload(h, to_f32(t.mort));
+        b.econst = upload(h, to_f32(t.econst));
+        b.colc = upload(h, to_f32(t.colc));
+        b.cplc = upload(h, to_f32(t.cplc));
         b.ncols = a.ncols;
         b.nelem = a.nelem;
         // index of every unknown in the full vector
@@ -157,6 +163,7 @@ void rtg_destroy(rtg_handle* h) {
     cudaSetDevice(h->device);
     free_workspace(h);
     free_sweep(h);
+    free_apply_plans(h);
     for (void* p : h->allocs) cudaFree(p);
     delete h;
 }

@@ -79,6 +79,9 @@ struct OpView {
     const T* G;           // G[n][p][i] = l'_p(x_i) w_i for n nodes, offset n*n*... see gofs
     const T* lglw;        // [kMaxNodes+1][kMaxNodes] LGL weights
     const T* mort;        // spatial + angular mortar matrices
+    const T* econst;      // per element: dx dy dth/8, dx dth/4, dy dth/4, 0
+    const T* colc;        // per column: dx dy / 8
+    const T* cplc;        // per coupling: dcoeff
     int32_t ncols;
     int32_t nelem;
 };
@@ -87,11 +90,11 @@ struct HostTables {
     std::vector<ColDev> cols;
     std::vector<ElemDev> elems;
     std::vector<CplDev> cpls;
-    std::vector<double> kw, sw, ang, W, G, lglw, mort;
+    std::vector<double> kw, sw, ang, W, G, lglw, mort, econst, colc, cplc;
     std::vector<int64_t> W_off;
     std::vector<int32_t> sig_nth;
     int64_t ndof = 0, ndof_interior = 0;
-    int32_t max_col_ndof = 0, max_nth_col = 0;
+    int32_t max_col_ndof = 0, max_nth_col = 0, max_cells_col = 0;
 };
 
 struct DevBuf {
@@ -101,6 +104,7 @@ struct DevBuf {
 
 struct Workspace;  // Krylov workspace (rtg_krylov.cu)
 struct Sweep;      // sweep preconditioner (rtg_sweep.cu)
+struct ApplyPlan;  // column partition of the apply kernels (rtg_apply.cu)
 
 }  // namespace rtg
 
@@ -115,6 +119,8 @@ struct rtg_handle {
     int64_t* d_interior_index = nullptr;   // [ndof_interior] full index of each unknown
     rtg::Workspace* ws = nullptr;
     rtg::Sweep* sweep = nullptr;
+    rtg::ApplyPlan* plan64 = nullptr;
+    rtg::ApplyPlan* plan32 = nullptr;
 };
 
 namespace rtg {
@@ -132,6 +138,7 @@ void launch_interior_mask(const rtg_handle* h, uint8_t* mask, cudaStream_t s);
 void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* out,
                         cudaStream_t s);
 void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s);
+void free_apply_plans(rtg_handle* h);
 
 // Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
 template <typename T>

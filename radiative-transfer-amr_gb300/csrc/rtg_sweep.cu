@@ -126,10 +126,13 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
             if (i != k) M[i * ld + k] = 0.;
         __syncthreads();
     }
+    // stored transposed, [input node k][output node ij], so that the sweep's
+    // threads (consecutive ij, same angular node) read consecutive entries
     double* o64 = inv64 + blk_off[b];
     float* o32 = inv32 + blk_off[b];
     for (int t = threadIdx.x; t < nn * nn; t += blockDim.x) {
-        const double val = M[(t / nn) * ld + nn + (t % nn)];
+        const int k = t / nn, ij = t % nn;
+        const double val = M[ij * ld + nn + k];
         o64[t] = val;
         o32[t] = (float)val;
     }
@@ -190,13 +193,16 @@ sweep_level_kernel(OpView<T> v, const int32_t* __restrict__ level_elems, const u
         rhs[l] = acc;
     }
     __syncthreads();
+    // z[ij, r] = sum_k B_r[ij][k] rhs[k, r]; threads r-major so that the
+    // transposed block B_r[k][ij] is read contiguously across the warp
     const T* B = inv + inv_elem_off[e];
-    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-        const int r = l % nth, ij = l / nth;
-        const T* row = B + ((int64_t)r * nn + ij) * nn;
+    for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+        const int r = t / nn, ij = t % nn;
+        const T* col = B + (int64_t)r * nn * nn + ij;
         T acc = T(0);
-        for (int k = 0; k < nn; ++k) acc += row[k] * rhs[k * nth + r];
-        z[E.dof_off + l] = acc;
+#pragma unroll 4
+        for (int k = 0; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
+        z[E.dof_off + (int64_t)ij * nth + r] = acc;
     }
 }
 
