@@ -73,12 +73,24 @@ def run_profile(args):
             out["method%d_rep%d" % (method, rep)] = {"s": time.perf_counter() - t0,
                                                      "iterations": info["iterations"],
                                                      "sweeps": info["sweeps"]}
+    stream = torch.cuda.current_stream()
     for prec in (_lib.RTG_FP32, _lib.RTG_FP64):
         dt = torch.float32 if prec == _lib.RTG_FP32 else torch.float64
+        nm = "fp32" if prec == _lib.RTG_FP32 else "fp64"
         x = torch.randn(ctx.N, dtype=dt, device=ctx.device)
         y = torch.empty_like(x)
-        for _ in range(3):
-            ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec)
+        for what, fn in (("apply", lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec)),
+                         ("sweep", lambda: ctx.precondition(x, y, prec=prec))):
+            fn()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            out["%s_%s_us" % (what, nm)] = 1e3 * e0.elapsed_time(e1) / 3
     torch.cuda.synchronize()
     out["ndof"] = ctx.N
     out["info"] = ctx.info

@@ -174,6 +174,12 @@ int rtg_mask_vector(rtg_handle* h, int part, const double* x, double* out, void*
 int rtg_split_vector(rtg_handle* h, const double* x, double* x_int, void* stream);
 int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, double* x,
                       void* stream);
+/* z = P^{-1} r: the upwind transport sweep rtg_solve uses as its right
+ * preconditioner (the GPU counterpart of the PETSc PC of rt/solve.py:125-127).
+ * r, z: device arrays of N doubles (RTG_FP64) or floats (RTG_FP32); entries
+ * of z at inflow-boundary DOFs are zero.  The first call builds the element
+ * block inverses (device memory owned by the handle). */
+int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream);
 /* out_beta = (dx dy dth / 8) wx_i wy_j wth_a * fvals_beta (device doubles). */
 int rtg_weight_forcing(rtg_handle* h, const double* fvals, double* out, void* stream);
 

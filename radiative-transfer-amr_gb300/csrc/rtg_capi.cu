@@ -211,6 +211,20 @@ int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y, v
     });
 }
 
+int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream) {
+    return guard("rtg_precondition", [&] {
+        if (!h || !r || !z) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (r == z) throw RtgError{RTG_ERR_ARG, "r and z alias"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64)
+            apply_sweep<double>(h, (const double*)r, (double*)z, s);
+        else if (prec == RTG_FP32)
+            apply_sweep<float>(h, (const float*)r, (float*)z, s);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
 int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream) {
     return guard("rtg_interior_mask", [&] {
         if (!h || !mask) throw RtgError{RTG_ERR_ARG, "null argument"};

@@ -146,6 +146,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
 int sweep_levels_count(rtg_handle* h, cudaStream_t s);
 int sweep_lagged_count(rtg_handle* h, cudaStream_t s);
+int sweep_status(rtg_handle* h, cudaStream_t s);
 void free_sweep(rtg_handle* h);
 
 // Solver (rtg_krylov.cu)

@@ -419,6 +419,8 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.fp64_applies += applies64;
     inf.fp32_applies += applies32;
     inf.sweeps = sweeps;
+    if (pc && sweep_status(h, s) != RTG_OK)
+        throw RtgError{RTG_ERR_TIMEOUT, "a sweep wait gave up; the solution is not valid"};
     inf.res_f = res;
     inf.converged = res <= tol ? 1 : 0;
     // u = x on the unknowns, g on the inflow-boundary DOFs (rt/solve.py:163)

@@ -11,8 +11,8 @@
 // Elements are ordered by Kahn levels of the "depends on the upwind
 // neighbour" graph over all angular cells at once; where the graph has a
 // cycle (cells that lie in no single quadrant couple on every face) the
-// couplings that close it are dropped from P.  Each level is one launch with
-// one CTA per element; the levels of a sweep are captured in a CUDA graph.
+// couplings that close it are dropped from P.  One persistent launch applies
+// P^{-1}: CTAs take elements in level order and wait on per-element flags.
 // Applying P^{-1} is exact for the transport part of an acyclic mesh; the
 // cross-cell scattering is left to the Krylov iteration.
 #include <algorithm>
@@ -138,71 +138,116 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
     }
 }
 
-// One level of the sweep: z_e = B_e^{-1} (rin_e - sum_upwind C_ee' z_e').
+// Persistent wavefront sweep: z_e = B_e^{-1} (rin_e - sum_upwind C_ee' z_e').
+// CTAs claim elements in topological order from an atomic counter.  An
+// element waits (bounded) until every upwind element it couples to has
+// published the current epoch in done[]; those elements come earlier in the
+// order, so they were claimed by CTAs that are already running and the wait
+// always ends unless a CTA gave up.  A CTA that gives up sets *status and
+// every other CTA stops waiting as soon as it sees the status.
+constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
+
 template <typename T>
 __global__ void __launch_bounds__(kSweepThreads)
-sweep_level_kernel(OpView<T> v, const int32_t* __restrict__ level_elems, const uint8_t* __restrict__ active,
-                   const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
-                   const T* __restrict__ rin, T* __restrict__ z) {
+sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
+                        const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
+                        const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
+                        unsigned int epoch, unsigned int* __restrict__ next, int* __restrict__ status) {
     extern __shared__ unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);
-    const int e = level_elems[blockIdx.x];
-    const ElemDev E = v.elems[e];
-    const ColDev C = v.cols[E.col];
-    const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
-    const int bm = E.flags >> 4;
-    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-        const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-        const bool bd = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) || ((bm & 4) && i == 0) ||
-                        ((bm & 8) && j == 0);
-        T acc = bd ? T(0) : rin[E.dof_off + l];
-        if (!bd) {
-            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
-                if (!active[k]) continue;
-                const CplDev cp = v.cpls[k];
-                const int F = cp.face;
-                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                (F == 3 && j == 0);
-                if (!on) continue;
-                const ElemDev E1 = v.elems[cp.nbr];
-                const ColDev C1 = v.cols[E1.col];
-                const int nth1 = E1.nth;
-                const int q = (F % 2 == 0) ? j : i;
-                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
-                const T* Es = v.mort + cp.es;
-                const T* Et = v.mort + cp.et;
-                int64_t base, stride;
-                int m1;
-                if (F % 2 == 0) {
-                    base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
-                    stride = nth1;
-                    m1 = C1.ny;
-                } else {
-                    base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
-                    stride = (int64_t)C1.ny * nth1;
-                    m1 = C1.nx;
+    __shared__ int s_idx;
+    __shared__ int s_abort;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_idx = (int)atomicAdd(next, 1u);
+            s_abort = 0;
+        }
+        __syncthreads();
+        const int idx = s_idx;
+        if (idx >= ne) break;
+        const int e = order[idx];
+        const ElemDev E = v.elems[e];
+        // wait for the upwind elements this one reads
+        for (int k = E.cpl_begin + threadIdx.x; k < E.cpl_end; k += blockDim.x) {
+            if (!active[k]) continue;
+            const int nb = v.cpls[k].nbr;
+            const long long t0 = clock64();
+            while (atomicAdd(&done[nb], 0u) != epoch) {
+                if (atomicAdd((unsigned int*)status, 0u) != 0u) {
+                    s_abort = 1;
+                    break;
                 }
-                const T dc = T(cp.dcoeff);
-                for (int jj = 0; jj < m1; ++jj) {
-                    const T es = dc * Es[jj * n0 + q];
-                    const T* zl = z + base + jj * stride;
-                    for (int a = 0; a < nth1; ++a) acc -= es * Et[a * nth + r] * zl[a];
+                if (clock64() - t0 > kSpinLimitCycles) {
+                    atomicExch(status, RTG_ERR_TIMEOUT);
+                    s_abort = 1;
+                    break;
                 }
+                __nanosleep(64);
             }
         }
-        rhs[l] = acc;
-    }
-    __syncthreads();
-    // z[ij, r] = sum_k B_r[ij][k] rhs[k, r]; threads r-major so that the
-    // transposed block B_r[k][ij] is read contiguously across the warp
-    const T* B = inv + inv_elem_off[e];
-    for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
-        const int r = t / nn, ij = t % nn;
-        const T* col = B + (int64_t)r * nn * nn + ij;
-        T acc = T(0);
+        __syncthreads();
+        if (s_abort) break;
+        __threadfence();
+        const ColDev C = v.cols[E.col];
+        const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
+        const int bm = E.flags >> 4;
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+            const bool bd = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) || ((bm & 4) && i == 0) ||
+                            ((bm & 8) && j == 0);
+            T acc = bd ? T(0) : rin[E.dof_off + l];
+            if (!bd && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
+                for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                    if (!active[k]) continue;
+                    const CplDev cp = v.cpls[k];
+                    const int F = cp.face;
+                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                    (F == 3 && j == 0);
+                    if (!on) continue;
+                    const ElemDev E1 = v.elems[cp.nbr];
+                    const ColDev C1 = v.cols[E1.col];
+                    const int nth1 = E1.nth;
+                    const int q = (F % 2 == 0) ? j : i;
+                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    const T* Es = v.mort + cp.es;
+                    const T* Et = v.mort + cp.et;
+                    int64_t base, stride;
+                    int m1;
+                    if (F % 2 == 0) {
+                        base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
+                        stride = nth1;
+                        m1 = C1.ny;
+                    } else {
+                        base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
+                        stride = (int64_t)C1.ny * nth1;
+                        m1 = C1.nx;
+                    }
+                    const T dc = v.cplc[k];
+                    for (int jj = 0; jj < m1; ++jj) {
+                        const T es = dc * Es[jj * n0 + q];
+                        const T* zl = z + base + jj * stride;
+                        T sacc = T(0);
+                        for (int a = 0; a < nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
+                        acc -= es * sacc;
+                    }
+                }
+            }
+            rhs[l] = acc;
+        }
+        __syncthreads();
+        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij])
+        const T* B = inv + inv_elem_off[e];
+        for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+            const int r = t / nn, ij = t % nn;
+            const T* col = B + (int64_t)r * nn * nn + ij;
+            T acc = T(0);
 #pragma unroll 4
-        for (int k = 0; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
-        z[E.dof_off + (int64_t)ij * nth + r] = acc;
+            for (int k = 0; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
+            __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicExch(&done[e], epoch);
     }
 }
 
@@ -220,10 +265,11 @@ struct Sweep {
     int max_nloc = 0;
     int n_lagged = 0;
     std::vector<void*> allocs;
-    // captured graphs per precision
-    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
-    double *r64 = nullptr, *z64 = nullptr;
-    float *r32 = nullptr, *z32 = nullptr;
+    unsigned int* d_done = nullptr;      // per element: epoch of the last sweep that finished it
+    unsigned int* d_next = nullptr;      // work counter
+    int* d_status = nullptr;             // RTG_ERR_TIMEOUT if a wait gave up
+    unsigned int epoch = 0;
+    int grid = 0;
 };
 
 namespace {
@@ -241,8 +287,6 @@ T* sw_alloc(Sweep* s, size_t n) {
 void free_sweep(rtg_handle* h) {
     Sweep* s = h->sweep;
     if (!s) return;
-    if (s->g64) cudaGraphExecDestroy(s->g64);
-    if (s->g32) cudaGraphExecDestroy(s->g32);
     for (void* p : s->allocs) cudaFree(p);
     delete s;
     h->sweep = nullptr;
@@ -362,23 +406,16 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     RTG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     RTG_CUDA(cudaStreamSynchronize(st));
     if (status) throw RtgError{RTG_ERR_NONFINITE, "singular element block in the sweep preconditioner"};
-    s->r64 = sw_alloc<double>(s, (size_t)t.ndof);
-    s->z64 = sw_alloc<double>(s, (size_t)t.ndof);
-    s->r32 = sw_alloc<float>(s, (size_t)t.ndof);
-    s->z32 = sw_alloc<float>(s, (size_t)t.ndof);
+    s->d_done = sw_alloc<unsigned int>(s, ne);
+    s->d_next = sw_alloc<unsigned int>(s, 1);
+    s->d_status = sw_alloc<int>(s, 1);
+    RTG_CUDA(cudaMemset(s->d_done, 0, sizeof(unsigned int) * ne));
+    RTG_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
+    int dev = 0, nsm = 0;
+    RTG_CUDA(cudaGetDevice(&dev));
+    RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    s->grid = std::max(1, std::min(ne, 4 * nsm));
     return s;
-}
-
-template <typename T>
-void sweep_levels(const rtg_handle* h, const Sweep* s, const OpView<T>& v, const T* inv, const T* r, T* z,
-                  cudaStream_t st) {
-    const size_t smem = sizeof(T) * (size_t)std::max(s->max_nloc, 1);
-    for (int L = 0; L < s->nlev; ++L) {
-        const int n = s->lev_start[L + 1] - s->lev_start[L];
-        if (n == 0) continue;
-        sweep_level_kernel<T><<<n, kSweepThreads, smem, st>>>(v, s->d_lev_elems + s->lev_start[L], s->d_active,
-                                                             inv, s->d_inv_off, r, z);
-    }
 }
 
 // z = P^{-1} r (full-length vectors; inflow-boundary entries of z are zero).
@@ -386,25 +423,29 @@ template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
-    cudaGraphExec_t& g = f64 ? s->g64 : s->g32;
-    T* rb = f64 ? (T*)s->r64 : (T*)s->r32;
-    T* zb = f64 ? (T*)s->z64 : (T*)s->z32;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     const OpView<T>& v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
-    if (!g) {
-        cudaStream_t cap;
-        RTG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-        cudaGraph_t graph;
-        RTG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        sweep_levels<T>(h, s, v, inv, rb, zb, cap);
-        RTG_CUDA(cudaStreamEndCapture(cap, &graph));
-        RTG_CUDA(cudaGraphInstantiate(&g, graph, 0));
-        RTG_CUDA(cudaGraphDestroy(graph));
-        RTG_CUDA(cudaStreamDestroy(cap));
+    if (++s->epoch == 0) {   // epoch wrapped: reset the flags
+        RTG_CUDA(cudaMemsetAsync(s->d_done, 0, sizeof(unsigned int) * h->host.elems.size(), st));
+        s->epoch = 1;
     }
-    RTG_CUDA(cudaMemcpyAsync(rb, r, sizeof(T) * (size_t)h->host.ndof, cudaMemcpyDeviceToDevice, st));
-    RTG_CUDA(cudaGraphLaunch(g, st));
-    RTG_CUDA(cudaMemcpyAsync(z, zb, sizeof(T) * (size_t)h->host.ndof, cudaMemcpyDeviceToDevice, st));
+    RTG_CUDA(cudaMemsetAsync(s->d_next, 0, sizeof(unsigned int), st));
+    const size_t smem = sizeof(T) * (size_t)std::max(s->max_nloc, 1);
+    sweep_persistent_kernel<T><<<s->grid, kSweepThreads, smem, st>>>(
+        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done, s->epoch,
+        s->d_next, s->d_status);
+    RTG_CUDA(cudaGetLastError());
+}
+
+// RTG_OK, or RTG_ERR_TIMEOUT if a sweep wait gave up since the last check.
+int sweep_status(rtg_handle* h, cudaStream_t st) {
+    Sweep* s = h->sweep;
+    if (!s) return RTG_OK;
+    int status = 0;
+    RTG_CUDA(cudaMemcpyAsync(&status, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RTG_CUDA(cudaStreamSynchronize(st));
+    if (status) RTG_CUDA(cudaMemsetAsync(s->d_status, 0, sizeof(int), st));
+    return status;
 }
 
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "rtg_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
     "rtg_apply": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_interior_mask": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_precondition": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_mask_vector": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_split_vector": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_merge_vectors": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -102,6 +102,17 @@ class DeviceContext:
                                       C.c_void_p(y.data_ptr()), _stream_ptr(stream)))
         return y
 
+    def precondition(self, r, z=None, prec=_lib.RTG_FP64, stream=None):
+        """z = P^{-1} r with the upwind transport sweep."""
+        torch = self.torch
+        dt = torch.float64 if prec == _lib.RTG_FP64 else torch.float32
+        r = self.to_device(r, dt)
+        if z is None:
+            z = torch.empty(self.N, dtype=dt, device=self.device)
+        _lib.check(self.lib.rtg_precondition(self.h, prec, C.c_void_p(r.data_ptr()),
+                                             C.c_void_p(z.data_ptr()), _stream_ptr(stream)))
+        return z
+
     def interior_mask(self):
         if self._mask is None:
             torch = self.torch

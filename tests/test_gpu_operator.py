@@ -109,3 +109,23 @@ def test_to_scipy_small():
     B = prob.boundary_convection_matrix(mesh).to_scipy()
     D = (B - g["BC"]).toarray()
     assert np.abs(D).max() <= 1e-14 * abs(g["BC"]).max()
+
+
+def test_sweep_preconditioner_properties(case):
+    """P^{-1} r: finite, zero at inflow-boundary DOFs, repeatable across calls
+    (per-element epoch flags), FP32 within 1e-4 of FP64, linear."""
+    import torch
+    from rtg import _lib
+    name, g, mesh, prob = case
+    ctx = prob.context(mesh)
+    rng = np.random.default_rng(5)
+    r = np.where(g["mask"], rng.standard_normal(len(g["f"])), 0.)
+    z1 = ctx.precondition(r).cpu().numpy()
+    z2 = ctx.precondition(r).cpu().numpy()
+    assert np.all(np.isfinite(z1))
+    np.testing.assert_array_equal(z1, z2)
+    assert np.all(z1[~g["mask"]] == 0.)
+    z32 = ctx.precondition(r, prec=_lib.RTG_FP32).cpu().numpy()
+    assert np.linalg.norm(z32 - z1) <= 1e-4 * np.linalg.norm(z1)
+    z3 = ctx.precondition(2.5 * r).cpu().numpy()
+    assert np.linalg.norm(z3 - 2.5 * z1) <= 1e-12 * np.linalg.norm(z3)
