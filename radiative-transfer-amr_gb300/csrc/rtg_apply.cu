@@ -59,23 +59,12 @@ __device__ __forceinline__ T face_terms(const OpView<T>& v, const ColDev& C, con
         for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
             const CplDev cp = v.cpls[k];
             if (cp.face != F) continue;
-            const ElemDev E1 = v.elems[cp.nbr];
-            const ColDev C1 = v.cols[E1.col];
-            const int nth1 = E1.nth;
+            const CplGeo g = v.cgeo[k];
+            const int nth1 = g.nth1, m1 = g.m1;
+            const int64_t base = g.base, stride = g.stride;
             const T* Es = v.mort + cp.es;
             const T* Et = v.mort + cp.et;
             const T dc = v.cplc[k];
-            int64_t base, stride;
-            int m1;
-            if (F % 2 == 0) {
-                base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
-                stride = nth1;
-                m1 = C1.ny;
-            } else {
-                base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
-                stride = (int64_t)C1.ny * nth1;
-                m1 = C1.nx;
-            }
             for (int jj = 0; jj < m1; ++jj) {
                 const T es = Es[jj * n0 + q];
                 const TX* xl = x + base + jj * stride;
@@ -114,22 +103,27 @@ __device__ __forceinline__ ApplyFlags decode(uint32_t flags) {
 }
 
 // ---------------------------------------------------------------- fast path
-// Shared memory: Xs[Nth][nij] | Ws[Nth][ldw] (optional) | cell tables.
+// Work item: outputs [begin, end) of one column (columns are split into
+// chunks so that the heaviest columns do not serialise the launch).
+// Shared memory: Xs[Nth][nij] | Ws[Nth][ldw] (optional) | Wf (FP32 copy of
+// Ws, FP64 parity path only) | cell tables.
 template <typename T, typename TX, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
-apply_col_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols, int stage_w,
-                 const TX* __restrict__ x, TX* __restrict__ y) {
+apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, uint32_t flags, const int4* __restrict__ items,
+                 int stage_w, const TX* __restrict__ x, TX* __restrict__ y) {
     extern __shared__ unsigned char smraw[];
-    const int ci = cols[blockIdx.x];
+    const int4 it = items[blockIdx.x];
+    const int ci = it.x;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
     const int ldw = Nth | 1;   // odd row stride: rows of W land in different banks
     T* Xs = reinterpret_cast<T*>(smraw);
     T* Ws = Xs + (size_t)Nth * nij;
-    int* cbeg = reinterpret_cast<int*>(Ws + (stage_w ? (size_t)Nth * ldw : 0));  // [ncell+1] local DOF start
-    int* crow = cbeg + ncell + 1;                                                // [ncell] first row
-    __shared__ T s_dxdy8;
+    float* Wf = reinterpret_cast<float*>(Ws + (stage_w ? (size_t)Nth * ldw : 0));
+    const bool stage_f = kParity && stage_w;
+    int* cbeg = reinterpret_cast<int*>(Wf + (stage_f ? (size_t)Nth * ldw : 0));  // [ncell+1] local DOF start
+    int* crow = cbeg + ncell + 1;                                                  // [ncell] first row
     if (threadIdx.x == 0) {
         int off = 0;
         for (int k = 0; k < ncell; ++k) {
@@ -139,7 +133,6 @@ apply_col_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols, 
             off += nij * E.nth;
         }
         cbeg[ncell] = off;
-        s_dxdy8 = v.colc[ci];
     }
     __syncthreads();
     const TX* xc = x + C.dof_off;
@@ -152,15 +145,20 @@ apply_col_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols, 
         Xs[(crow[k] + l % nth) * nij + l / nth] = T(xc[d]);
     }
     const T* Wg = v.W + v.W_off[C.sig];
+    const float* Wgf = Wf32 + v.W_off[C.sig];
     if (stage_w)
-        for (int t = threadIdx.x; t < Nth * Nth; t += blockDim.x) Ws[(t / Nth) * ldw + (t % Nth)] = Wg[t];
+        for (int t = threadIdx.x; t < Nth * Nth; t += blockDim.x) {
+            const int row = t / Nth, col = t % Nth;
+            Ws[row * ldw + col] = Wg[t];
+            if (stage_f) Wf[row * ldw + col] = Wgf[t];
+        }
     __syncthreads();
     const T small = T(kSmall);
-    const T dxdy8 = s_dxdy8;
+    const T dxdy8 = v.colc[ci];
     const T* Gx = v.G + gofs(C.nx);
     const T* Gy = v.G + gofs(C.ny);
     TX* yc = y + C.dof_off;
-    for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
+    for (int d = it.y + threadIdx.x; d < it.z; d += blockDim.x) {
         int k = 0;
         while (d >= cbeg[k + 1]) ++k;
         const int e = C.elem_begin + k;
@@ -183,16 +181,29 @@ apply_col_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols, 
             const T cw = dxdy8 * swv;
             const T mself = fl.merged ? v.econst[4 * e] * A[r] * v.kw[node] : T(0);
             if (kParity) {
-                // reference drop rules (rt/preconditioner_matrix.py:450-495)
+                // Reference drop rules (rt/preconditioner_matrix.py:450-495):
+                // keep -cw*W[R][c] iff |cw*W[R][c]| > 1e-14; cross-cell terms
+                // only where |wx wy sigma| > 1e-14; the diagonal joins the
+                // extinction term before its test.  The test runs in FP32 and
+                // falls back to FP64 within 1e-6 (relative) of the threshold,
+                // so the FP64 pipe does one FMA per term.
                 const bool skip_cross = !(tabs(swv) > small);
                 const int c0 = skip_cross ? crow[k] : 0;
                 const int c1 = skip_cross ? crow[k] + nth : Nth;
+                const float cwf = fabsf((float)cw);
+                const float hi = 1.e-14f * (1.f + 1.e-6f), lo = 1.e-14f * (1.f - 1.e-6f);
+                T s = T(0);
                 for (int c = c0; c < c1; ++c) {
                     const T wv = stage_w ? Ws[R * ldw + c] : Wg[(int64_t)R * Nth + c];
-                    T val = -cw * wv;
-                    if (c == R) val += mself;
-                    if (tabs(val) > small) acc += val * Xs[c * nij + ij];
+                    const float wf = stage_f ? Wf[R * ldw + c] : Wgf[(int64_t)R * Nth + c];
+                    const float pf = cwf * fabsf(wf);
+                    bool keep = pf > hi;
+                    if (!keep && pf >= lo) keep = tabs(cw * wv) > small;
+                    s = fma(keep && c != R ? wv : T(0), Xs[c * nij + ij], s);
                 }
+                const T wd = stage_w ? Ws[R * ldw + R] : Wg[(int64_t)R * Nth + R];
+                const T vd = mself - cw * wd;
+                acc = -cw * s + (tabs(vd) > small ? vd : T(0)) * xself;
             } else {
                 T s = T(0);
                 if (stage_w) {
@@ -339,13 +350,15 @@ __global__ void weight_forcing_kernel(OpView<double> v, const double* f, double*
 
 }  // namespace
 
-// Column partition of the fast path, per precision: columns whose staged input
-// (and W when it fits) stay within the shared-memory budget, sorted by work
-// (largest first) so the long columns start early.
+// Work partition of the fast path, per precision: columns whose staged input
+// (and W when it fits) stay within the shared-memory budget, cut into chunks
+// of at most kChunk outputs, heaviest chunks first.
+constexpr int kChunk = 1024;
+
 struct ApplyPlan {
-    int32_t* d_fast = nullptr;
+    int4* d_items = nullptr;
     int32_t* d_slow = nullptr;
-    int nfast = 0, nslow = 0;
+    int nitems = 0, nslow = 0;
     size_t smem = 0;
     int stage_w = 0;
     std::vector<void*> allocs;
@@ -354,39 +367,46 @@ struct ApplyPlan {
 template <typename T>
 static ApplyPlan* make_plan(const rtg_handle* h) {
     const HostTables& t = h->host;
+    constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
-    std::vector<std::pair<int64_t, int32_t>> fast;
+    std::vector<std::pair<int64_t, int4>> items;
     std::vector<int32_t> slow;
     size_t need_x = 0, need_w = 0;
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
         const ColDev& C = t.cols[ci];
         const int ncell = C.elem_end - C.elem_begin;
         const size_t sx = sizeof(T) * (size_t)C.ndof + sizeof(int) * (2 * ncell + 2) + 16;
-        const size_t sw = sizeof(T) * (size_t)C.nth_col * (C.nth_col | 1);
+        const size_t sw = (sizeof(T) + (parity ? sizeof(float) : 0)) * (size_t)C.nth_col * (C.nth_col | 1);
         if (sx <= kSmemBudget && ncell <= kMaxCellsStaged) {
-            fast.push_back({(int64_t)C.ndof * (C.nth_col + C.nx + C.ny), ci});
+            const int nch = (C.ndof + kChunk - 1) / kChunk;
+            const int per = (C.ndof + nch - 1) / nch;
+            for (int q = 0; q < nch; ++q) {
+                const int b0 = q * per, b1 = std::min(C.ndof, b0 + per);
+                items.push_back({(int64_t)(b1 - b0) * (C.nth_col + C.nx + C.ny) + C.ndof, make_int4(ci, b0, b1, 0)});
+            }
             need_x = std::max(need_x, sx);
             need_w = std::max(need_w, sw);
         } else {
             slow.push_back(ci);
         }
     }
-    std::sort(fast.begin(), fast.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    std::stable_sort(items.begin(), items.end(), [](auto& a, auto& b) { return a.first > b.first; });
     p->stage_w = (need_x + need_w <= kSmemBudget) ? 1 : 0;
     p->smem = need_x + (p->stage_w ? need_w : 0);
-    std::vector<int32_t> f32;
-    for (auto& pr : fast) f32.push_back(pr.second);
-    p->nfast = (int)f32.size();
+    std::vector<int4> it4;
+    for (auto& pr : items) it4.push_back(pr.second);
+    p->nitems = (int)it4.size();
     p->nslow = (int)slow.size();
-    auto up = [&](const std::vector<int32_t>& v) -> int32_t* {
-        void* d = nullptr;
-        RTG_CUDA(cudaMalloc(&d, sizeof(int32_t) * std::max<size_t>(v.size(), 1)));
-        p->allocs.push_back(d);
-        if (!v.empty()) RTG_CUDA(cudaMemcpy(d, v.data(), sizeof(int32_t) * v.size(), cudaMemcpyHostToDevice));
-        return (int32_t*)d;
-    };
-    p->d_fast = up(f32);
-    p->d_slow = up(slow);
+    void* d = nullptr;
+    RTG_CUDA(cudaMalloc(&d, sizeof(int4) * std::max<size_t>(it4.size(), 1)));
+    p->allocs.push_back(d);
+    if (!it4.empty()) RTG_CUDA(cudaMemcpy(d, it4.data(), sizeof(int4) * it4.size(), cudaMemcpyHostToDevice));
+    p->d_items = (int4*)d;
+    d = nullptr;
+    RTG_CUDA(cudaMalloc(&d, sizeof(int32_t) * std::max<size_t>(slow.size(), 1)));
+    p->allocs.push_back(d);
+    if (!slow.empty()) RTG_CUDA(cudaMemcpy(d, slow.data(), sizeof(int32_t) * slow.size(), cudaMemcpyHostToDevice));
+    p->d_slow = (int32_t*)d;
     return p;
 }
 
@@ -412,9 +432,9 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
                                           (int)plan->smem));
         }
     }
-    if (plan->nfast)
-        apply_col_kernel<T, T, f64><<<plan->nfast, kApplyThreads, plan->smem, s>>>(v, flags, plan->d_fast,
-                                                                                  plan->stage_w, x, y);
+    if (plan->nitems)
+        apply_col_kernel<T, T, f64><<<plan->nitems, kApplyThreads, plan->smem, s>>>(v, h->v32.W, flags, plan->d_items,
+                                                                                   plan->stage_w, x, y);
     if (plan->nslow)
         apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, flags, plan->d_slow, x, y);
     RTG_CUDA(cudaGetLastError());

@@ -578,7 +578,25 @@ void build_tables(const rtg_mesh_desc* m, const rtg_coeffs* c, HostTables& t) {
         t.max_cells_col = std::max(t.max_cells_col, t.cols[ci].elem_end - t.cols[ci].elem_begin);
     }
     t.cplc.resize(t.cpls.size());
-    for (size_t k = 0; k < t.cpls.size(); ++k) t.cplc[k] = t.cpls[k].dcoeff;
+    t.cgeo.resize(t.cpls.size());
+    for (size_t k = 0; k < t.cpls.size(); ++k) {
+        const CplDev& cp = t.cpls[k];
+        t.cplc[k] = cp.dcoeff;
+        const ElemDev& E1 = t.elems[cp.nbr];
+        const ColDev& C1 = t.cols[E1.col];
+        CplGeo g{};
+        g.nth1 = E1.nth;
+        if (cp.face % 2 == 0) {   // x-faces: neighbour's facing column of nodes, along y
+            g.base = E1.dof_off + (int64_t)((cp.face == 0) ? 0 : C1.nx - 1) * C1.ny * E1.nth;
+            g.stride = E1.nth;
+            g.m1 = C1.ny;
+        } else {                  // y-faces: neighbour's facing row of nodes, along x
+            g.base = E1.dof_off + (int64_t)((cp.face == 1) ? 0 : C1.ny - 1) * E1.nth;
+            g.stride = C1.ny * E1.nth;
+            g.m1 = C1.nx;
+        }
+        t.cgeo[k] = g;
+    }
 }
 
 }  // namespace rtg

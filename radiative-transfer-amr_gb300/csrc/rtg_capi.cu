@@ -100,6 +100,9 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
         ElemDev* elems = upload(h, t.elems);
         CplDev* cpls = upload(h, t.cpls);
         int64_t* woff = upload(h, t.W_off);
+        CplGeo* cgeo = upload(h, t.cgeo);
+        h->v64.cgeo = cgeo;
+        h->v32.cgeo = cgeo;
         OpView<double>& a = h->v64;
         a.cols = cols;
         a.elems = elems;

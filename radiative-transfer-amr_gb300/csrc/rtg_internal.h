@@ -65,6 +65,16 @@ struct CplDev {
     int32_t et;           // angular mortar offset ([nth1][nth0] row-major)
 };
 
+// Where a coupling reads its neighbour's facing node line: entry (jj, a) of
+// the line is x[base + jj*stride + a], jj < m1, a < nth1.
+struct CplGeo {
+    int64_t base;
+    int32_t stride;
+    int32_t m1;
+    int32_t nth1;
+    int32_t pad;
+};
+
 // Device-side view passed to kernels by value.
 template <typename T>
 struct OpView {
@@ -82,6 +92,7 @@ struct OpView {
     const T* econst;      // per element: dx dy dth/8, dx dth/4, dy dth/4, 0
     const T* colc;        // per column: dx dy / 8
     const T* cplc;        // per coupling: dcoeff
+    const CplGeo* cgeo;   // per coupling: neighbour line addressing
     int32_t ncols;
     int32_t nelem;
 };
@@ -90,6 +101,7 @@ struct HostTables {
     std::vector<ColDev> cols;
     std::vector<ElemDev> elems;
     std::vector<CplDev> cpls;
+    std::vector<CplGeo> cgeo;
     std::vector<double> kw, sw, ang, W, G, lglw, mort, econst, colc, cplc;
     std::vector<int64_t> W_off;
     std::vector<int32_t> sig_nth;

@@ -31,6 +31,11 @@ constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
 __device__ __forceinline__ int gofs_s(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
 
+__device__ __forceinline__ bool bdry_node_s(int bm, int i, int j, int nx, int ny) {
+    return ((bm & 1) && i == nx - 1) || ((bm & 2) && j == ny - 1) || ((bm & 4) && i == 0) ||
+           ((bm & 8) && j == 0);
+}
+
 // One CTA per (element, angular node): assemble the element block for that
 // node in shared memory as [A | I] and invert it by Gauss-Jordan elimination
 // with partial pivoting.  Rows of inflow-boundary nodes become identity rows.
@@ -167,6 +172,15 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         if (idx >= ne) break;
         const int e = order[idx];
         const ElemDev E = v.elems[e];
+        const ColDev C = v.cols[E.col];
+        const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
+        const int bm = E.flags >> 4;
+        // the element's own residual does not depend on the sweep: load it
+        // before waiting so its latency overlaps the wait
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            const int ij = l / nth;
+            rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
+        }
         // wait for the upwind elements this one reads
         for (int k = E.cpl_begin + threadIdx.x; k < E.cpl_end; k += blockDim.x) {
             if (!active[k]) continue;
@@ -182,67 +196,57 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                     s_abort = 1;
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __syncthreads();
         if (s_abort) break;
         __threadfence();
-        const ColDev C = v.cols[E.col];
-        const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
-        const int bm = E.flags >> 4;
+        // subtract the upwind face couplings on the element's face nodes
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-            const bool bd = ((bm & 1) && i == C.nx - 1) || ((bm & 2) && j == C.ny - 1) || ((bm & 4) && i == 0) ||
-                            ((bm & 8) && j == 0);
-            T acc = bd ? T(0) : rin[E.dof_off + l];
-            if (!bd && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
-                for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
-                    if (!active[k]) continue;
-                    const CplDev cp = v.cpls[k];
-                    const int F = cp.face;
-                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                    (F == 3 && j == 0);
-                    if (!on) continue;
-                    const ElemDev E1 = v.elems[cp.nbr];
-                    const ColDev C1 = v.cols[E1.col];
-                    const int nth1 = E1.nth;
-                    const int q = (F % 2 == 0) ? j : i;
-                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
-                    const T* Es = v.mort + cp.es;
-                    const T* Et = v.mort + cp.et;
-                    int64_t base, stride;
-                    int m1;
-                    if (F % 2 == 0) {
-                        base = E1.dof_off + (int64_t)((F == 0) ? 0 : C1.nx - 1) * C1.ny * nth1;
-                        stride = nth1;
-                        m1 = C1.ny;
-                    } else {
-                        base = E1.dof_off + (int64_t)((F == 1) ? 0 : C1.ny - 1) * nth1;
-                        stride = (int64_t)C1.ny * nth1;
-                        m1 = C1.nx;
-                    }
-                    const T dc = v.cplc[k];
-                    for (int jj = 0; jj < m1; ++jj) {
-                        const T es = dc * Es[jj * n0 + q];
-                        const T* zl = z + base + jj * stride;
-                        T sacc = T(0);
-                        for (int a = 0; a < nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
-                        acc -= es * sacc;
-                    }
+            if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
+            if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+            T acc = T(0);
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                if (!active[k]) continue;
+                const CplDev cp = v.cpls[k];
+                const int F = cp.face;
+                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                (F == 3 && j == 0);
+                if (!on) continue;
+                const CplGeo g = v.cgeo[k];
+                const int q = (F % 2 == 0) ? j : i;
+                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                const T* Es = v.mort + cp.es;
+                const T* Et = v.mort + cp.et;
+                const T dc = v.cplc[k];
+                for (int jj = 0; jj < g.m1; ++jj) {
+                    const T* zl = z + g.base + (int64_t)jj * g.stride;
+                    T sacc = T(0);
+                    for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
+                    acc += dc * Es[jj * n0 + q] * sacc;
                 }
             }
-            rhs[l] = acc;
+            rhs[l] -= acc;
         }
         __syncthreads();
-        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij])
+        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij]);
+        // 16 independent loads in flight per thread
         const T* B = inv + inv_elem_off[e];
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
             const T* col = B + (int64_t)r * nn * nn + ij;
             T acc = T(0);
-#pragma unroll 4
-            for (int k = 0; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
+            int k = 0;
+            for (; k + 16 <= nn; k += 16) {
+                T bv[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) bv[u] = col[(int64_t)(k + u) * nn];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) acc += bv[u] * rhs[(k + u) * nth + r];
+            }
+            for (; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
             __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
         }
         __threadfence();
