@@ -26,7 +26,8 @@ namespace rtg {
 
 namespace {
 
-constexpr int kSweepThreads = 128;
+constexpr int kSweepThreads = 256;
+constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse
 constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
 __device__ __forceinline__ int gofs_s(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
@@ -157,9 +158,11 @@ __global__ void __launch_bounds__(kSweepThreads)
 sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
                         const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
-                        unsigned int epoch, unsigned int* __restrict__ next, int* __restrict__ status) {
+                        unsigned int epoch, unsigned int* __restrict__ next, int* __restrict__ status,
+                        int rhs_cap, int bcap) {
     extern __shared__ unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);
+    T* Bs = rhs + rhs_cap;
     __shared__ int s_idx;
     __shared__ int s_abort;
     for (;;) {
@@ -175,8 +178,13 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         const ColDev C = v.cols[E.col];
         const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
         const int bm = E.flags >> 4;
-        // the element's own residual does not depend on the sweep: load it
-        // before waiting so its latency overlaps the wait
+        // the element's residual and block inverse do not depend on the
+        // sweep: load them before waiting so their latency overlaps the wait
+        const T* B = inv + inv_elem_off[e];
+        const int bsize = nth * nn * nn;
+        const bool staged = bsize <= bcap;
+        if (staged)
+            for (int t = threadIdx.x; t < bsize; t += blockDim.x) Bs[t] = __ldg(B + t);
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
             rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
@@ -231,10 +239,17 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             rhs[l] -= acc;
         }
         __syncthreads();
-        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij]);
-        // 16 independent loads in flight per thread
-        const T* B = inv + inv_elem_off[e];
-        for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij])
+        if (staged) {
+            for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+                const int r = t / nn, ij = t % nn;
+                const T* col = Bs + r * nn * nn + ij;
+                T acc = T(0);
+#pragma unroll 4
+                for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
+                __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
+            }
+        } else for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
             const T* col = B + (int64_t)r * nn * nn + ij;
             T acc = T(0);
@@ -267,13 +282,15 @@ struct Sweep {
     int64_t* d_inv_off = nullptr;
     int64_t inv_entries = 0;
     int max_nloc = 0;
+    int64_t max_b = 0;
+    size_t smem64 = 0, smem32 = 0;
+    int bcap64 = 0, bcap32 = 0, grid64 = 0, grid32 = 0;
     int n_lagged = 0;
     std::vector<void*> allocs;
     unsigned int* d_done = nullptr;      // per element: epoch of the last sweep that finished it
     unsigned int* d_next = nullptr;      // work counter
     int* d_status = nullptr;             // RTG_ERR_TIMEOUT if a wait gave up
     unsigned int epoch = 0;
-    int grid = 0;
 };
 
 namespace {
@@ -415,10 +432,12 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     s->d_status = sw_alloc<int>(s, 1);
     RTG_CUDA(cudaMemset(s->d_done, 0, sizeof(unsigned int) * ne));
     RTG_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
-    int dev = 0, nsm = 0;
-    RTG_CUDA(cudaGetDevice(&dev));
-    RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    s->grid = std::max(1, std::min(ne, 4 * nsm));
+    int64_t max_b = 0;
+    for (int e = 0; e < ne; ++e) {
+        const ColDev& C = t.cols[t.elems[e].col];
+        max_b = std::max<int64_t>(max_b, (int64_t)t.elems[e].nth * C.nx * C.ny * C.nx * C.ny);
+    }
+    s->max_b = max_b;
     return s;
 }
 
@@ -434,10 +453,27 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
         s->epoch = 1;
     }
     RTG_CUDA(cudaMemsetAsync(s->d_next, 0, sizeof(unsigned int), st));
-    const size_t smem = sizeof(T) * (size_t)std::max(s->max_nloc, 1);
-    sweep_persistent_kernel<T><<<s->grid, kSweepThreads, smem, st>>>(
+    size_t& smem = f64 ? s->smem64 : s->smem32;
+    int& bcap = f64 ? s->bcap64 : s->bcap32;
+    int& grid = f64 ? s->grid64 : s->grid32;
+    const int rhs_cap = std::max(s->max_nloc, 1);
+    if (grid == 0) {
+        const size_t rhs_bytes = sizeof(T) * (size_t)rhs_cap;
+        const int64_t fit = (int64_t)((kSweepSmemBudget - rhs_bytes) / sizeof(T));
+        bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
+        smem = rhs_bytes + sizeof(T) * (size_t)bcap;
+        RTG_CUDA(cudaFuncSetAttribute(sweep_persistent_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        int per_sm = 0, dev = 0, nsm = 0;
+        RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
+                                                               smem));
+        RTG_CUDA(cudaGetDevice(&dev));
+        RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
+    }
+    sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
         v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done, s->epoch,
-        s->d_next, s->d_status);
+        s->d_next, s->d_status, rhs_cap, bcap);
     RTG_CUDA(cudaGetLastError());
 }
 
