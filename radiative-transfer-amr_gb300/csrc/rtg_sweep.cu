@@ -28,6 +28,7 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse
+constexpr int kMaxCplStaged = 32;               // active couplings staged per element
 constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
 __device__ __forceinline__ int gofs_s(int n) { return (n - 1) * n * (2 * n - 1) / 6; }
@@ -159,12 +160,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                         const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
                         unsigned int epoch, unsigned int* __restrict__ next, int* __restrict__ status,
-                        int rhs_cap, int bcap) {
+                        int rhs_cap, int bcap, int ccap) {
     extern __shared__ unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);
     T* Bs = rhs + rhs_cap;
+    T* cs = Bs + bcap;   // staged couplings: per active coupling Es | Et | upwind face line
     __shared__ int s_idx;
     __shared__ int s_abort;
+    __shared__ int s_nc;
+    __shared__ int s_k[kMaxCplStaged];
+    __shared__ int s_off[kMaxCplStaged + 1];
     for (;;) {
         if (threadIdx.x == 0) {
             s_idx = (int)atomicAdd(next, 1u);
@@ -189,6 +194,33 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             const int ij = l / nth;
             rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
         }
+        // table of the active couplings and their staging offsets
+        if (threadIdx.x == 0) {
+            int nc = 0, off = 0;
+            for (int k = E.cpl_begin; k < E.cpl_end && nc < kMaxCplStaged; ++k) {
+                if (!active[k]) continue;
+                const CplGeo g = v.cgeo[k];
+                const int n0 = (v.cpls[k].face % 2 == 0) ? C.ny : C.nx;
+                s_k[nc] = k;
+                s_off[nc] = off;
+                off += g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1;
+                ++nc;
+            }
+            s_off[nc] = off;
+            s_nc = (off <= ccap && nc < kMaxCplStaged) ? nc : -1;   // -1: read from global memory
+        }
+        __syncthreads();
+        // stage the mortar matrices now (they do not depend on the sweep)
+        const int ncs = s_nc;
+        for (int c = 0; c < ncs; ++c) {
+            const int k = s_k[c];
+            const CplDev cp = v.cpls[k];
+            const CplGeo g = v.cgeo[k];
+            const int n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+            T* dst = cs + s_off[c];
+            for (int t = threadIdx.x; t < g.m1 * n0; t += blockDim.x) dst[t] = __ldg(v.mort + cp.es + t);
+            for (int t = threadIdx.x; t < g.nth1 * nth; t += blockDim.x) dst[g.m1 * n0 + t] = __ldg(v.mort + cp.et + t);
+        }
         // wait for the upwind elements this one reads
         for (int k = E.cpl_begin + threadIdx.x; k < E.cpl_end; k += blockDim.x) {
             if (!active[k]) continue;
@@ -210,33 +242,75 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         __syncthreads();
         if (s_abort) break;
         __threadfence();
-        // subtract the upwind face couplings on the element's face nodes
-        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-            const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-            if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
-            if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
-            T acc = T(0);
-            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
-                if (!active[k]) continue;
-                const CplDev cp = v.cpls[k];
-                const int F = cp.face;
-                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                (F == 3 && j == 0);
-                if (!on) continue;
+        if (ncs >= 0) {
+            // stage every upwind face line with one round of parallel loads
+            for (int c = 0; c < ncs; ++c) {
+                const int k = s_k[c];
                 const CplGeo g = v.cgeo[k];
-                const int q = (F % 2 == 0) ? j : i;
-                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
-                const T* Es = v.mort + cp.es;
-                const T* Et = v.mort + cp.et;
-                const T dc = v.cplc[k];
-                for (int jj = 0; jj < g.m1; ++jj) {
-                    const T* zl = z + g.base + (int64_t)jj * g.stride;
-                    T sacc = T(0);
-                    for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
-                    acc += dc * Es[jj * n0 + q] * sacc;
+                const int n0 = (v.cpls[k].face % 2 == 0) ? C.ny : C.nx;
+                T* dst = cs + s_off[c] + g.m1 * n0 + g.nth1 * nth;
+                const int len = g.m1 * g.nth1;
+                for (int t = threadIdx.x; t < len; t += blockDim.x) {
+                    const int jj = t / g.nth1, a = t % g.nth1;
+                    dst[t] = __ldcg(z + g.base + (int64_t)jj * g.stride + a);
                 }
             }
-            rhs[l] -= acc;
+            __syncthreads();
+            // subtract the upwind face couplings on the element's face nodes
+            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+                const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+                if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
+                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+                T acc = T(0);
+                for (int c = 0; c < ncs; ++c) {
+                    const int k = s_k[c];
+                    const int F = v.cpls[k].face;
+                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                    (F == 3 && j == 0);
+                    if (!on) continue;
+                    const CplGeo g = v.cgeo[k];
+                    const int q = (F % 2 == 0) ? j : i;
+                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    const T* Es = cs + s_off[c];
+                    const T* Et = Es + g.m1 * n0;
+                    const T* zl = Et + g.nth1 * nth;
+                    const T dc = v.cplc[k];
+                    for (int jj = 0; jj < g.m1; ++jj) {
+                        T sacc = T(0);
+                        for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * zl[jj * g.nth1 + a];
+                        acc += dc * Es[jj * n0 + q] * sacc;
+                    }
+                }
+                rhs[l] -= acc;
+            }
+        } else {
+            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+                const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+                if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
+                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+                T acc = T(0);
+                for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                    if (!active[k]) continue;
+                    const CplDev cp = v.cpls[k];
+                    const int F = cp.face;
+                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                    (F == 3 && j == 0);
+                    if (!on) continue;
+                    const CplGeo g = v.cgeo[k];
+                    const int q = (F % 2 == 0) ? j : i;
+                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    const T* Es = v.mort + cp.es;
+                    const T* Et = v.mort + cp.et;
+                    const T dc = v.cplc[k];
+                    for (int jj = 0; jj < g.m1; ++jj) {
+                        const T* zl = z + g.base + (int64_t)jj * g.stride;
+                        T sacc = T(0);
+                        for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
+                        acc += dc * Es[jj * n0 + q] * sacc;
+                    }
+                }
+                rhs[l] -= acc;
+            }
         }
         __syncthreads();
         // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij])
@@ -282,7 +356,7 @@ struct Sweep {
     int64_t* d_inv_off = nullptr;
     int64_t inv_entries = 0;
     int max_nloc = 0;
-    int64_t max_b = 0;
+    int64_t max_b = 0, max_c = 0;
     size_t smem64 = 0, smem32 = 0;
     int bcap64 = 0, bcap32 = 0, grid64 = 0, grid32 = 0;
     int n_lagged = 0;
@@ -438,6 +512,20 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         max_b = std::max<int64_t>(max_b, (int64_t)t.elems[e].nth * C.nx * C.ny * C.nx * C.ny);
     }
     s->max_b = max_b;
+    int64_t max_c = 0;
+    for (int e = 0; e < ne; ++e) {
+        const ElemDev& E = t.elems[e];
+        const ColDev& C = t.cols[E.col];
+        int64_t c = 0;
+        for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+            if (!active[k]) continue;
+            const CplGeo& g = t.cgeo[k];
+            const int n0 = (t.cpls[k].face % 2 == 0) ? C.ny : C.nx;
+            c += (int64_t)g.m1 * n0 + (int64_t)g.nth1 * E.nth + (int64_t)g.m1 * g.nth1;
+        }
+        max_c = std::max(max_c, c);
+    }
+    s->max_c = max_c;
     return s;
 }
 
@@ -458,8 +546,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     int& grid = f64 ? s->grid64 : s->grid32;
     const int rhs_cap = std::max(s->max_nloc, 1);
     if (grid == 0) {
-        const size_t rhs_bytes = sizeof(T) * (size_t)rhs_cap;
-        const int64_t fit = (int64_t)((kSweepSmemBudget - rhs_bytes) / sizeof(T));
+        const size_t rhs_bytes = sizeof(T) * (size_t)(rhs_cap + s->max_c);
+        const int64_t fit = (int64_t)((kSweepSmemBudget - std::min(rhs_bytes, kSweepSmemBudget)) / sizeof(T));
         bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
         smem = rhs_bytes + sizeof(T) * (size_t)bcap;
         RTG_CUDA(cudaFuncSetAttribute(sweep_persistent_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -473,7 +561,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     }
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
         v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done, s->epoch,
-        s->d_next, s->d_status, rhs_cap, bcap);
+        s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c);
     RTG_CUDA(cudaGetLastError());
 }
 
