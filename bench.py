@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu: one warm and one measured solve per method, 3 applies")
@@ -58,12 +58,24 @@ def run_profile(args):
     import torch
     from rtg import Problem, _lib
     torch.cuda.set_device(0)
+    out = {}
+    t0 = time.perf_counter()
     desc, mesh, spec = workload(args.workload)
+    out["mesh_s"] = time.perf_counter() - t0
     prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    t0 = time.perf_counter()
     ctx = prob.context(mesh)
+    torch.cuda.synchronize()
+    out["context_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
     f_dev = ctx.forcing(spec.f)
     g_dev = ctx.inflow(spec.bcs_dirac)
-    out = {}
+    torch.cuda.synchronize()
+    out["vectors_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.precondition(torch.zeros(ctx.N, dtype=torch.float64, device=ctx.device))
+    torch.cuda.synchronize()
+    out["sweep_setup_s"] = time.perf_counter() - t0
     for method in (1, 0):
         for rep in range(2):
             torch.cuda.synchronize()
@@ -101,6 +113,9 @@ def workload(name, seed=0):
     from rtg import workloads as W
     if name == "cfg1":
         return ("manufactured 4x4x4 cells n=4 (4096 DOF)", W.config1_mesh(), W.manufactured_problem())
+    if name == "cfg5":
+        return ("two strong scatterers on [0,2]^2, disc-edge hp refinement seed %d, 5..9 nodes/dim "
+                "(~9.4e6 DOF)" % seed, W.config5_mesh(seed=seed), W.two_disc_problem())
     return ("gaussian-bump adaptive hp, seed %d (~2.2e5 DOF)" % seed, W.config2_mesh(seed=seed),
             W.gaussian_bump_problem())
 

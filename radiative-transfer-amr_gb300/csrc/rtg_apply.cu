@@ -37,8 +37,9 @@ __device__ __forceinline__ bool bdry_node(int bm, int i, int j, int nx, int ny) 
 // to neighbour elements (rt/boundary_convection_matrix.py:258-524).
 // xself: the node's own input value.
 template <typename T, typename TX, bool kParity>
-__device__ __forceinline__ T face_terms(const OpView<T>& v, const ColDev& C, const ElemDev& E, int e, int i,
-                                        int j, int r, T xself, const TX* __restrict__ x) {
+__device__ __forceinline__ T face_terms(const OpView<T>& v, const float* __restrict__ mortf, const ColDev& C,
+                                        const ElemDev& E, int e, int i, int j, int r, T xself,
+                                        const TX* __restrict__ x) {
     const T bctol = T(kBcTol);
     const int nth = E.nth;
     const T* A = v.ang + E.ang;
@@ -69,10 +70,20 @@ __device__ __forceinline__ T face_terms(const OpView<T>& v, const ColDev& C, con
                 const T es = Es[jj * n0 + q];
                 const TX* xl = x + base + jj * stride;
                 if (kParity) {
+                    // keep dcoeff*Es*Et iff |.| > 1e-15, tested in FP32 with an
+                    // FP64 fallback within 1e-6 of the threshold; one FMA per term
+                    const T des = dc * es;
+                    const float fdes = fabsf((float)des);
+                    const float hi = 1.e-15f * (1.f + 1.e-6f), lo = 1.e-15f * (1.f - 1.e-6f);
+                    T s = T(0);
                     for (int a = 0; a < nth1; ++a) {
-                        const T val = dc * es * Et[a * nth + r];
-                        if (tabs(val) > bctol) acc += val * T(xl[a]);
+                        const T et = Et[a * nth + r];
+                        const float pf = fdes * fabsf(mortf[cp.et + a * nth + r]);
+                        bool keep = pf > hi;
+                        if (!keep && pf >= lo) keep = tabs(des * et) > bctol;
+                        s = fma(keep ? et : T(0), T(xl[a]), s);
                     }
+                    acc += des * s;
                 } else {
                     T s = T(0);
                     for (int a = 0; a < nth1; ++a) s += Et[a * nth + r] * T(xl[a]);
@@ -109,7 +120,8 @@ __device__ __forceinline__ ApplyFlags decode(uint32_t flags) {
 // Ws, FP64 parity path only) | cell tables.
 template <typename T, typename TX, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
-apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, uint32_t flags, const int4* __restrict__ items,
+apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __restrict__ mortf, uint32_t flags,
+                 const int4* __restrict__ items,
                  int stage_w, const TX* __restrict__ x, TX* __restrict__ y) {
     extern __shared__ unsigned char smraw[];
     const int4 it = items[blockIdx.x];
@@ -232,7 +244,7 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, uint32_t flags, co
             acc += T(fl.ic_sign) * ic;
         }
         if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1))
-            acc += face_terms<T, TX, kParity>(v, C, E, e, i, j, r, xself, x);
+            acc += face_terms<T, TX, kParity>(v, mortf, C, E, e, i, j, r, xself, x);
         yc[d] = TX(acc);
     }
 }
@@ -240,7 +252,7 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, uint32_t flags, co
 // ------------------------------------------------------------ global path
 template <typename T, typename TX, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
-apply_global_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ cols,
+apply_global_kernel(OpView<T> v, const float* __restrict__ mortf, uint32_t flags, const int32_t* __restrict__ cols,
                     const TX* __restrict__ x, TX* __restrict__ y) {
     const int ci = cols[blockIdx.x];
     const ColDev C = v.cols[ci];
@@ -298,7 +310,7 @@ apply_global_kernel(OpView<T> v, uint32_t flags, const int32_t* __restrict__ col
                 acc += T(fl.ic_sign) * ic;
             }
             if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1))
-                acc += face_terms<T, TX, kParity>(v, C, E, e, i, j, r, xself, x);
+                acc += face_terms<T, TX, kParity>(v, mortf, C, E, e, i, j, r, xself, x);
             y[E.dof_off + l] = TX(acc);
         }
     }
@@ -351,16 +363,22 @@ __global__ void weight_forcing_kernel(OpView<double> v, const double* f, double*
 }  // namespace
 
 // Work partition of the fast path, per precision: columns whose staged input
-// (and W when it fits) stay within the shared-memory budget, cut into chunks
-// of at most kChunk outputs, heaviest chunks first.
+// stays within the shared-memory budget, cut into chunks of at most kChunk
+// outputs, heaviest chunks first, in two launch groups: with the column's W
+// staged too, or (large angular meshes) with W read through L2.
 constexpr int kChunk = 1024;
 
-struct ApplyPlan {
+struct ApplyGroup {
     int4* d_items = nullptr;
-    int32_t* d_slow = nullptr;
-    int nitems = 0, nslow = 0;
+    int nitems = 0;
     size_t smem = 0;
     int stage_w = 0;
+};
+
+struct ApplyPlan {
+    ApplyGroup g[2];            // 0: input and W staged; 1: input staged, W read through L2
+    int32_t* d_slow = nullptr;
+    int nslow = 0;
     std::vector<void*> allocs;
 };
 
@@ -369,44 +387,46 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
     const HostTables& t = h->host;
     constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
-    std::vector<std::pair<int64_t, int4>> items;
+    std::vector<std::pair<int64_t, int4>> items[2];
     std::vector<int32_t> slow;
-    size_t need_x = 0, need_w = 0;
+    size_t need[2] = {0, 0};
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
         const ColDev& C = t.cols[ci];
         const int ncell = C.elem_end - C.elem_begin;
         const size_t sx = sizeof(T) * (size_t)C.ndof + sizeof(int) * (2 * ncell + 2) + 16;
         const size_t sw = (sizeof(T) + (parity ? sizeof(float) : 0)) * (size_t)C.nth_col * (C.nth_col | 1);
-        if (sx <= kSmemBudget && ncell <= kMaxCellsStaged) {
-            const int nch = (C.ndof + kChunk - 1) / kChunk;
-            const int per = (C.ndof + nch - 1) / nch;
-            for (int q = 0; q < nch; ++q) {
-                const int b0 = q * per, b1 = std::min(C.ndof, b0 + per);
-                items.push_back({(int64_t)(b1 - b0) * (C.nth_col + C.nx + C.ny) + C.ndof, make_int4(ci, b0, b1, 0)});
-            }
-            need_x = std::max(need_x, sx);
-            need_w = std::max(need_w, sw);
-        } else {
+        if (sx > kSmemBudget || ncell > kMaxCellsStaged) {
             slow.push_back(ci);
+            continue;
+        }
+        const int grp = (sx + sw <= kSmemBudget) ? 0 : 1;
+        need[grp] = std::max(need[grp], grp == 0 ? sx + sw : sx);
+        const int nch = (C.ndof + kChunk - 1) / kChunk;
+        const int per = (C.ndof + nch - 1) / nch;
+        for (int q = 0; q < nch; ++q) {
+            const int b0 = q * per, b1 = std::min(C.ndof, b0 + per);
+            items[grp].push_back({(int64_t)(b1 - b0) * (C.nth_col + C.nx + C.ny) + C.ndof, make_int4(ci, b0, b1, 0)});
         }
     }
-    std::stable_sort(items.begin(), items.end(), [](auto& a, auto& b) { return a.first > b.first; });
-    p->stage_w = (need_x + need_w <= kSmemBudget) ? 1 : 0;
-    p->smem = need_x + (p->stage_w ? need_w : 0);
-    std::vector<int4> it4;
-    for (auto& pr : items) it4.push_back(pr.second);
-    p->nitems = (int)it4.size();
+    auto up = [&](const void* src, size_t bytes) -> void* {
+        void* d = nullptr;
+        RTG_CUDA(cudaMalloc(&d, std::max<size_t>(bytes, 16)));
+        p->allocs.push_back(d);
+        if (bytes) RTG_CUDA(cudaMemcpy(d, src, bytes, cudaMemcpyHostToDevice));
+        return d;
+    };
+    for (int grp = 0; grp < 2; ++grp) {
+        std::stable_sort(items[grp].begin(), items[grp].end(), [](auto& a, auto& b) { return a.first > b.first; });
+        std::vector<int4> it4;
+        for (auto& pr : items[grp]) it4.push_back(pr.second);
+        ApplyGroup& G = p->g[grp];
+        G.nitems = (int)it4.size();
+        G.stage_w = grp == 0 ? 1 : 0;
+        G.smem = need[grp];
+        G.d_items = (int4*)up(it4.data(), sizeof(int4) * it4.size());
+    }
     p->nslow = (int)slow.size();
-    void* d = nullptr;
-    RTG_CUDA(cudaMalloc(&d, sizeof(int4) * std::max<size_t>(it4.size(), 1)));
-    p->allocs.push_back(d);
-    if (!it4.empty()) RTG_CUDA(cudaMemcpy(d, it4.data(), sizeof(int4) * it4.size(), cudaMemcpyHostToDevice));
-    p->d_items = (int4*)d;
-    d = nullptr;
-    RTG_CUDA(cudaMalloc(&d, sizeof(int32_t) * std::max<size_t>(slow.size(), 1)));
-    p->allocs.push_back(d);
-    if (!slow.empty()) RTG_CUDA(cudaMemcpy(d, slow.data(), sizeof(int32_t) * slow.size(), cudaMemcpyHostToDevice));
-    p->d_slow = (int32_t*)d;
+    p->d_slow = (int32_t*)up(slow.data(), sizeof(int32_t) * slow.size());
     return p;
 }
 
@@ -427,16 +447,19 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
     ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
     if (!plan) {
         plan = make_plan<T>(h);
-        if (plan->smem > 48 * 1024) {
+        size_t mx = std::max(plan->g[0].smem, plan->g[1].smem);
+        if (mx > 48 * 1024)
             RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)plan->smem));
-        }
+                                          (int)mx));
     }
-    if (plan->nitems)
-        apply_col_kernel<T, T, f64><<<plan->nitems, kApplyThreads, plan->smem, s>>>(v, h->v32.W, flags, plan->d_items,
-                                                                                   plan->stage_w, x, y);
+    for (int grp = 0; grp < 2; ++grp) {
+        const ApplyGroup& G = plan->g[grp];
+        if (G.nitems)
+            apply_col_kernel<T, T, f64><<<G.nitems, kApplyThreads, G.smem, s>>>(v, h->v32.W, h->v32.mort, flags,
+                                                                              G.d_items, G.stage_w, x, y);
+    }
     if (plan->nslow)
-        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, flags, plan->d_slow, x, y);
+        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, h->v32.mort, flags, plan->d_slow, x, y);
     RTG_CUDA(cudaGetLastError());
 }
 

@@ -41,11 +41,14 @@ __device__ __forceinline__ bool bdry_node_s(int bm, int i, int j, int nx, int ny
 // One CTA per (element, angular node): assemble the element block for that
 // node in shared memory as [A | I] and invert it by Gauss-Jordan elimination
 // with partial pivoting.  Rows of inflow-boundary nodes become identity rows.
-__global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __restrict__ blk_elem,
+// The elimination runs in FP32 (GB300's FP64 rate would make large meshes take
+// minutes); the inverse only defines the preconditioner, a fixed linear
+// operator, so the FP64 solve still converges to FP64 accuracy.
+__global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __restrict__ blk_elem,
                                            const int32_t* __restrict__ blk_r,
                                            const int64_t* __restrict__ blk_off, double* __restrict__ inv64,
                                            float* __restrict__ inv32, int* __restrict__ status) {
-    extern __shared__ double smem[];
+    extern __shared__ float smemf[];
     const int b = blockIdx.x;
     const int e = blk_elem[b];
     const int r = blk_r[b];
@@ -53,46 +56,47 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
     const ColDev C = v.cols[E.col];
     const int nx = C.nx, ny = C.ny, nn = nx * ny, nth = E.nth;
     const int ld = 2 * nn;
-    double* M = smem;                      // nn x 2nn
+    float* M = smemf;                      // nn x 2nn
     __shared__ int piv;
-    __shared__ double pval;
-    const double* A = v.ang + E.ang;
-    const double* W = v.W + v.W_off[C.sig];
-    const double* Gx = v.G + gofs_s(nx);
-    const double* Gy = v.G + gofs_s(ny);
-    const double* wxs = v.lglw + nx * kMaxNodes;
-    const double* wys = v.lglw + ny * kMaxNodes;
-    const double dxdy8 = C.dx * C.dy / 8.;
-    const double wsr = A[nth + r], wcr = A[2 * nth + r], wr = A[r];
-    const double self = W[(int64_t)(E.row + r) * C.nth_col + E.row + r];
+    __shared__ float pval;
+    const float* A = v.ang + E.ang;
+    const float* W = v.W + v.W_off[C.sig];
+    const float* Gx = v.G + gofs_s(nx);
+    const float* Gy = v.G + gofs_s(ny);
+    const float* wxs = v.lglw + nx * kMaxNodes;
+    const float* wys = v.lglw + ny * kMaxNodes;
+    const float dxdy8 = v.colc[E.col];
+    const float mc = v.econst[4 * e], icx = v.econst[4 * e + 1], icy = v.econst[4 * e + 2];
+    const float wsr = A[nth + r], wcr = A[2 * nth + r], wr = A[r];
+    const float self = W[(int64_t)(E.row + r) * C.nth_col + E.row + r];
     const int bm = E.flags >> 4;
     for (int k = threadIdx.x; k < nn * ld; k += blockDim.x) {
         const int row = k / ld, col = k % ld;
         const int p = row / ny, q = row % ny;
         const bool bd = ((bm & 1) && p == nx - 1) || ((bm & 2) && q == ny - 1) || ((bm & 4) && p == 0) ||
                         ((bm & 8) && q == 0);
-        double val = 0.;
+        float val = 0.f;
         if (col >= nn) {
-            val = (col - nn == row) ? 1. : 0.;
+            val = (col - nn == row) ? 1.f : 0.f;
         } else if (bd) {
-            val = (col == row) ? 1. : 0.;
+            val = (col == row) ? 1.f : 0.f;
         } else {
             const int i = col / ny, j = col % ny;
             const int node = C.node_off + col;
             if (col == row) {
-                val += dxdy8 * E.dth * wr * v.kw[node] - dxdy8 * v.sw[node] * self;
+                val += mc * wr * v.kw[node] - dxdy8 * v.sw[node] * self;
                 for (int F = 0; F < 4; ++F) {
                     if (!(E.flags & (1 << F))) continue;
                     const bool on = (F == 0 && p == nx - 1) || (F == 1 && q == ny - 1) || (F == 2 && p == 0) ||
                                     (F == 3 && q == 0);
                     if (!on) continue;
-                    const double dc = (F % 2 == 0) ? C.dy * E.dth / 4. : C.dx * E.dth / 4.;
-                    const double w = (F % 2 == 0) ? wys[q] : wxs[p];
+                    const float dc = (F % 2 == 0) ? icy : icx;
+                    const float w = (F % 2 == 0) ? wys[q] : wxs[p];
                     val += dc * w * wr * A[(3 + F) * nth + r];
                 }
             }
-            if (p == i) val -= (C.dx * E.dth / 4.) * wxs[p] * wsr * Gy[q * ny + j];
-            if (q == j) val -= (C.dy * E.dth / 4.) * wys[q] * wcr * Gx[p * nx + i];
+            if (p == i) val -= icx * wxs[p] * wsr * Gy[q * ny + j];
+            if (q == j) val -= icy * wys[q] * wcr * Gx[p * nx + i];
         }
         M[k] = val;
     }
@@ -100,9 +104,9 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
     for (int k = 0; k < nn; ++k) {
         if (threadIdx.x == 0) {
             int best = k;
-            double bv = fabs(M[k * ld + k]);
+            float bv = fabsf(M[k * ld + k]);
             for (int i = k + 1; i < nn; ++i) {
-                const double a = fabs(M[i * ld + k]);
+                const float a = fabsf(M[i * ld + k]);
                 if (a > bv) {
                     bv = a;
                     best = i;
@@ -110,17 +114,17 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
             }
             piv = best;
             pval = M[best * ld + k];
-            if (!(bv > 0.)) atomicExch(status, 1);
+            if (!(bv > 0.f)) atomicExch(status, 1);
         }
         __syncthreads();
         if (piv != k)
             for (int c = threadIdx.x; c < ld; c += blockDim.x) {
-                const double t = M[k * ld + c];
+                const float t = M[k * ld + c];
                 M[k * ld + c] = M[piv * ld + c];
                 M[piv * ld + c] = t;
             }
         __syncthreads();
-        const double inv = pval != 0. ? 1. / pval : 0.;
+        const float inv = pval != 0.f ? 1.f / pval : 0.f;
         for (int c = threadIdx.x; c < ld; c += blockDim.x) M[k * ld + c] *= inv;
         __syncthreads();
         for (int t = threadIdx.x; t < nn * ld; t += blockDim.x) {
@@ -130,7 +134,7 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
         }
         __syncthreads();
         for (int i = threadIdx.x; i < nn; i += blockDim.x)
-            if (i != k) M[i * ld + k] = 0.;
+            if (i != k) M[i * ld + k] = 0.f;
         __syncthreads();
     }
     // stored transposed, [input node k][output node ij], so that the sweep's
@@ -139,9 +143,9 @@ __global__ void build_block_inverse_kernel(OpView<double> v, const int32_t* __re
     float* o32 = inv32 + blk_off[b];
     for (int t = threadIdx.x; t < nn * nn; t += blockDim.x) {
         const int k = t / nn, ij = t % nn;
-        const double val = M[ij * ld + nn + k];
-        o64[t] = val;
-        o32[t] = (float)val;
+        const float val = M[ij * ld + nn + k];
+        o64[t] = (double)val;
+        o32[t] = val;
     }
 }
 
@@ -491,10 +495,10 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     RTG_CUDA(cudaMemcpy(d_br, blk_r.data(), sizeof(int32_t) * blk_r.size(), cudaMemcpyHostToDevice));
     RTG_CUDA(cudaMemcpy(d_bo, blk_off.data(), sizeof(int64_t) * blk_off.size(), cudaMemcpyHostToDevice));
     RTG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
-    const size_t smem = sizeof(double) * (size_t)max_nn * 2 * max_nn;
+    const size_t smem = sizeof(float) * (size_t)max_nn * 2 * max_nn;
     RTG_CUDA(cudaFuncSetAttribute(build_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-    build_block_inverse_kernel<<<(int)blk_elem.size(), 256, smem, st>>>(h->v64, d_be, d_br, d_bo, s->d_inv64,
+    build_block_inverse_kernel<<<(int)blk_elem.size(), 256, smem, st>>>(h->v32, d_be, d_br, d_bo, s->d_inv64,
                                                                          s->d_inv32, d_status);
     RTG_CUDA(cudaGetLastError());
     int status = 0;

@@ -302,6 +302,62 @@ def small_random_mesh(mesh_cls=Mesh, seed=3):
                           mesh_cls=mesh_cls)
 
 
+def disc_edge_mesh(mesh_cls=Mesh, seed=0, rounds=3, n0=4, nth0=4, n_max=9, nref_ang=3,
+                   nref_spt=3, p_prob=0.35, ang_prob=0.35, max_ang_lv=5, discs=((0.6, 0.6), (1.4, 1.4)),
+                   radius=0.2, Ls=(2., 2.), ndof_cap=None):
+    """Two-strong-scatterer mesh: uniform start, then seeded refinement of the
+    columns that straddle a disc edge (h with probability 1 - p_prob, else p
+    up to ``n_max`` nodes) and of the angular cells of those columns (h up to
+    level ``max_ang_lv`` or p), all through ref_col/ref_cell (2:1 balance)."""
+    rng = np.random.default_rng(seed)
+    mesh = mesh_cls(list(Ls), [False, False], [n0, n0, nth0], True)
+    for _ in range(nref_ang):
+        mesh.ref_mesh(kind="ang", form="h")
+    for _ in range(nref_spt):
+        mesh.ref_mesh(kind="spt", form="h")
+
+    def near_edge(col):
+        x0, y0, x1, y1 = col.pos
+        cx, cy = (x0 + x1) / 2., (y0 + y1) / 2.
+        half = 0.5 * max(x1 - x0, y1 - y0) * 1.5
+        return any(abs(np.hypot(cx - dx, cy - dy) - radius) < half for dx, dy in discs)
+
+    for _ in range(rounds):
+        for ck in sorted(mesh.cols.keys()):
+            if ck not in mesh.cols or not near_edge(mesh.cols[ck]):
+                continue
+            col = mesh.cols[ck]
+            if rng.random() < p_prob:
+                if col.ndofs[0] < n_max:
+                    mesh.ref_col(ck, kind="spt", form="p")
+            else:
+                mesh.ref_col(ck, kind="spt", form="h")
+        for ck in sorted(mesh.cols.keys()):
+            if ck not in mesh.cols or not near_edge(mesh.cols[ck]):
+                continue
+            for kk in sorted(mesh.cols[ck].cells.keys()):
+                if ck not in mesh.cols or kk not in mesh.cols[ck].cells or rng.random() >= ang_prob:
+                    continue
+                cell = mesh.cols[ck].cells[kk]
+                if rng.random() < 0.5 and cell.ndofs[0] < n_max:
+                    mesh.ref_cell(ck, kk, form="p")
+                elif cell.lv < max_ang_lv:
+                    mesh.ref_cell(ck, kk, form="h")
+        if ndof_cap is not None and mesh.get_ndof() >= ndof_cap:
+            break
+    return mesh
+
+
+def config5_mesh(mesh_cls=Mesh, seed=0, scale=1.0):
+    """Large two-strong-scatterer mesh on [0,2]^2: refinement concentrated at
+    the disc edges, up to 9 nodes per dimension (degree 8), about 1e7 DOF at
+    scale 1 (``scale`` < 1 gives the same recipe with fewer refinement rounds
+    for tests)."""
+    rounds = 5 if scale >= 1.0 else max(1, int(round(5 * scale)))
+    return disc_edge_mesh(mesh_cls=mesh_cls, seed=seed, rounds=rounds, n0=5, nth0=5, n_max=9,
+                          nref_ang=3, nref_spt=4, ang_prob=0.42)
+
+
 def config2_mesh(mesh_cls=Mesh, seed=0):
     """Single adaptive problem mesh: [0,3]x[0,2], six rounds of seeded random
     hp refinement, nodes per dimension in [3, 7] (degree 2..6), about 2e5 DOF."""
