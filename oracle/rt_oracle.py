@@ -720,3 +720,144 @@ def solve_gmres(A, MS, f, g, mask, L, rtol=1e-10, restart=50, maxiter=5000, x0=N
     u[I] = x
     u[B] = g[B]
     return u, count[0]
+
+
+# -------------------------------------------------------------------- sweep
+def element_of_dof(L):
+    """Element index (global order) of every DOF."""
+    eid = np.zeros(L.N, dtype=np.int64)
+    for e, key in enumerate(L.elems):
+        o = L.off[key]
+        col = L.mesh.cols[key[0]]
+        n = col.ndofs[0] * col.ndofs[1] * col.cells[key[1]].ndofs[0]
+        eid[o:o + n] = e
+    return eid
+
+
+def sweep_levels(L, BC):
+    """Kahn levels of the graph "element depends on the upwind element it couples
+    to" read off the off-element blocks of BC; ready elements are taken lowest
+    level first, then lowest index, and a cycle is broken by forcing the
+    lowest-index unprocessed element.  This is the order the GPU sweep uses."""
+    import heapq
+    eid = element_of_dof(L)
+    C = BC.tocoo()
+    keep = eid[C.row] != eid[C.col]
+    pairs = set(zip(eid[C.col][keep].tolist(), eid[C.row][keep].tolist()))   # (upwind, element)
+    ne = len(L.elems)
+    succ = [[] for _ in range(ne)]
+    indeg = np.zeros(ne, dtype=np.int64)
+    for p, e in pairs:
+        succ[p].append(e)
+        indeg[e] += 1
+    level = np.full(ne, -1, dtype=np.int64)
+    lvl_pred = np.zeros(ne, dtype=np.int64)
+    done = np.zeros(ne, dtype=bool)
+    heap = [(0, e) for e in range(ne) if indeg[e] == 0]
+    heapq.heapify(heap)
+    processed, forced = 0, 0
+    while processed < ne:
+        if not heap:
+            while done[forced]:
+                forced += 1
+            indeg[forced] = 0
+            heapq.heappush(heap, (int(lvl_pred[forced]), forced))
+        _, e = heapq.heappop(heap)
+        if done[e]:
+            continue
+        done[e] = True
+        level[e] = lvl_pred[e]
+        processed += 1
+        for q in succ[e]:
+            if done[q]:
+                continue
+            lvl_pred[q] = max(lvl_pred[q], level[e] + 1)
+            indeg[q] -= 1
+            if indeg[q] == 0:
+                heapq.heappush(heap, (int(lvl_pred[q]), q))
+    return level, eid
+
+
+class SweepPreconditioner:
+    """z = P^{-1} r for the upwind transport sweep: element blocks per angular
+    node (extinction minus the self-scattering diagonal, minus interior
+    streaming, plus outflow face terms; identity rows at inflow-boundary
+    nodes) and the inflow couplings to elements on earlier levels."""
+
+    def __init__(self, o, L):
+        import scipy.linalg as sla
+        self.L = L
+        mask = o["mask"]
+        BC, IC, MS = o["BC"].tocsr(), o["IC"].tocsr(), o["MS"].tocsr()
+        self.level, eid = sweep_levels(L, BC)
+        T = (BC - IC).tocsr()
+        msd = MS.diagonal()
+        ne = len(L.elems)
+        self.order = sorted(range(ne), key=lambda e: (self.level[e], e))
+        self.blocks = []
+        self.cpl = []
+        for e, key in enumerate(L.elems):
+            col = L.mesh.cols[key[0]]
+            nx, ny, nth = col.ndofs[0], col.ndofs[1], col.cells[key[1]].ndofs[0]
+            o0 = L.off[key]
+            n = nx * ny * nth
+            sl = np.arange(o0, o0 + n)
+            Tee = T[sl][:, sl].toarray()
+            facs = []
+            for r in range(nth):
+                idx = np.arange(nx * ny) * nth + r
+                B = Tee[np.ix_(idx, idx)] + np.diag(msd[o0 + idx])
+                bd = ~mask[o0 + idx]
+                B[bd, :] = 0.
+                B[bd, bd] = 1.
+                facs.append((idx, sla.lu_factor(B)))
+            self.blocks.append((o0, n, facs, mask[sl]))
+            # couplings to upwind elements on earlier levels
+            rows = T[sl]
+            cols_e = eid[rows.indices]
+            ups = sorted(set(cols_e.tolist()) - {e})
+            cl = []
+            for u in ups:
+                if self.level[u] < self.level[e]:
+                    ku = L.elems[u]
+                    cu = L.mesh.cols[ku[0]]
+                    ou = L.off[ku]
+                    nu = cu.ndofs[0] * cu.ndofs[1] * cu.cells[ku[1]].ndofs[0]
+                    cl.append((ou, nu, BC[sl][:, ou:ou + nu].tocsr()))
+            self.cpl.append(cl)
+
+    def __call__(self, r):
+        import scipy.linalg as sla
+        z = np.zeros_like(r)
+        for e in self.order:
+            o0, n, facs, m = self.blocks[e]
+            rhs = np.where(m, r[o0:o0 + n], 0.)
+            for ou, nu, Bk in self.cpl[e]:
+                rhs -= np.where(m, Bk @ z[ou:ou + nu], 0.)
+            ze = np.zeros(n)
+            for idx, lu in facs:
+                ze[idx] = sla.lu_solve(lu, rhs[idx])
+            z[o0:o0 + n] = ze
+        return z
+
+
+def solve_sweep_gmres(o, L, rtol=1e-10, restart=50, maxiter=200):
+    """Split system solved by scipy GMRES(restart) with the sweep as
+    preconditioner -- the GPU plain method's algorithm on the CPU."""
+    A_II, _, rhs, I, B = split_system(o["A"], o["f"], o["g"], o["mask"])
+    P = SweepPreconditioner(o, L)
+    N = len(o["mask"])
+
+    def pre(v):
+        full = np.zeros(N)
+        full[I] = v
+        return P(full)[I]
+
+    M = spla.LinearOperator(A_II.shape, matvec=pre, dtype=np.float64)
+    cnt = [0]
+    x, info = spla.gmres(A_II.tocsr(), rhs, rtol=rtol, atol=0., restart=restart, maxiter=maxiter,
+                         M=M, callback=lambda _: cnt.__setitem__(0, cnt[0] + 1), callback_type="pr_norm")
+    u = np.zeros(N)
+    u[I] = x
+    u[B] = o["g"][B]
+    return u, cnt[0], info

@@ -102,19 +102,31 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
     }
     __syncthreads();
     for (int k = 0; k < nn; ++k) {
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            // partial pivoting: warp-wide arg-max of |M[i][k]| over i >= k
+            // (ties go to the lowest row, as a serial scan would)
+            float bv = -1.f;
             int best = k;
-            float bv = fabsf(M[k * ld + k]);
-            for (int i = k + 1; i < nn; ++i) {
+            for (int i = k + threadIdx.x; i < nn; i += 32) {
                 const float a = fabsf(M[i * ld + k]);
                 if (a > bv) {
                     bv = a;
                     best = i;
                 }
             }
-            piv = best;
-            pval = M[best * ld + k];
-            if (!(bv > 0.f)) atomicExch(status, 1);
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ov = __shfl_down_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_down_sync(0xffffffffu, best, o);
+                if (ov > bv || (ov == bv && oi < best)) {
+                    bv = ov;
+                    best = oi;
+                }
+            }
+            if (threadIdx.x == 0) {
+                piv = best;
+                pval = M[best * ld + k];
+                if (!(bv > 0.f)) atomicExch(status, 1);
+            }
         }
         __syncthreads();
         if (piv != k)

@@ -69,3 +69,14 @@ def test_manufactured_error_cfg1():
     ue = spec.u_exact(X, Y, T)
     err = np.sqrt(np.sum(w * (g["u"] - ue) ** 2) / np.sum(w * ue ** 2))
     np.testing.assert_allclose(err, float(g["rel_l2_err_exact"]), rtol=1e-10)
+
+
+@pytest.mark.parametrize("name", ["cfg1", "small_random", "hp_hanging"])
+def test_oracle_sweep_gmres_reaches_reference_solution(name):
+    g = golden_io.load(name)
+    mesh_fn, prob_fn = golden_io.problem(name)
+    spec = prob_fn()
+    o = O.assemble(mesh_fn(), spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    u, its, info = O.solve_sweep_gmres(o, o["layout"], rtol=1e-12)
+    assert info == 0 and its < 40
+    assert np.linalg.norm(u - g["u"]) / np.linalg.norm(g["u"]) < 1e-10
