@@ -780,18 +780,18 @@ def sweep_levels(L, BC):
 
 class SweepPreconditioner:
     """z = P^{-1} r for the upwind transport sweep: element blocks per angular
-    node (extinction minus the self-scattering diagonal, minus interior
-    streaming, plus outflow face terms; identity rows at inflow-boundary
-    nodes) and the inflow couplings to elements on earlier levels."""
+    node (extinction, minus interior streaming, plus outflow face terms;
+    identity rows at inflow-boundary nodes; no scattering) and the inflow
+    couplings to elements on earlier levels."""
 
     def __init__(self, o, L):
         import scipy.linalg as sla
         self.L = L
         mask = o["mask"]
-        BC, IC, MS = o["BC"].tocsr(), o["IC"].tocsr(), o["MS"].tocsr()
+        BC, IC = o["BC"].tocsr(), o["IC"].tocsr()
         self.level, eid = sweep_levels(L, BC)
         T = (BC - IC).tocsr()
-        msd = MS.diagonal()
+        msd = o["M"].diagonal()
         ne = len(L.elems)
         self.order = sorted(range(ne), key=lambda e: (self.level[e], e))
         self.blocks = []

@@ -1,11 +1,14 @@
 // Upwind block transport sweep used as the preconditioner of the RT solve.
 //
-// P is the block-lower-triangular part of the transport-plus-self-scattering
-// operator in an upwind element order:
+// P is the block-lower-triangular part of the transport operator (streaming
+// plus total extinction, no scattering) in an upwind element order:
 //   * element-diagonal block, per angular node r of the element: the
-//     (nx ny) x (nx ny) matrix of extinction minus the r == a self-scattering
-//     term, minus interior streaming, plus the outflow face terms (the same
-//     entries rtg_apply uses with RTG_SYSTEM);
+//     (nx ny) x (nx ny) matrix of extinction, minus interior streaming, plus
+//     the outflow face terms (the same entries rtg_apply uses with
+//     RTG_SYSTEM).  All scattering, including the same-direction term, is
+//     left to the Krylov iteration: with a forward-peaked phase function on a
+//     coarse angular cell the same-direction term can exceed the extinction
+//     and make the block singular;
 //   * off-diagonal blocks: the inflow face couplings to neighbour elements
 //     that come earlier in the order.
 // Elements are ordered by Kahn levels of the "depends on the upwind
@@ -60,15 +63,12 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
     __shared__ int piv;
     __shared__ float pval;
     const float* A = v.ang + E.ang;
-    const float* W = v.W + v.W_off[C.sig];
     const float* Gx = v.G + gofs_s(nx);
     const float* Gy = v.G + gofs_s(ny);
     const float* wxs = v.lglw + nx * kMaxNodes;
     const float* wys = v.lglw + ny * kMaxNodes;
-    const float dxdy8 = v.colc[E.col];
     const float mc = v.econst[4 * e], icx = v.econst[4 * e + 1], icy = v.econst[4 * e + 2];
     const float wsr = A[nth + r], wcr = A[2 * nth + r], wr = A[r];
-    const float self = W[(int64_t)(E.row + r) * C.nth_col + E.row + r];
     const int bm = E.flags >> 4;
     for (int k = threadIdx.x; k < nn * ld; k += blockDim.x) {
         const int row = k / ld, col = k % ld;
@@ -84,7 +84,7 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
             const int i = col / ny, j = col % ny;
             const int node = C.node_off + col;
             if (col == row) {
-                val += mc * wr * v.kw[node] - dxdy8 * v.sw[node] * self;
+                val += mc * wr * v.kw[node];
                 for (int F = 0; F < 4; ++F) {
                     if (!(E.flags & (1 << F))) continue;
                     const bool on = (F == 0 && p == nx - 1) || (F == 1 && q == ny - 1) || (F == 2 && p == 0) ||
