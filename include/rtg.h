@@ -192,6 +192,22 @@ int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u,
               const rtg_solve_opts* opts, rtg_solve_info* info,
               double* hist, int hist_cap, void* stream);
 
+/* Batched solve of independent problems held by one handle.  The handle's mesh
+ * is the concatenation of nbatch instances' meshes (no couplings between
+ * them; each instance with its own coefficients), instance b owning DOFs
+ * [inst_off[b], inst_off[b+1]) (inst_off: host array of nbatch+1 offsets,
+ * inst_off[0] = 0, inst_off[nbatch] = N).  Every operator apply and sweep
+ * covers all instances in one launch; the Krylov state (inner products,
+ * Hessenberg, Givens, convergence) is per instance and lives on the device;
+ * one GMRES restart cycle is captured in a CUDA graph and replayed.
+ * opts->method must be 1 (FP32 sweep-preconditioned GMRES inside FP64
+ * iterative refinement); rtol/atol apply per instance.  infos (host, may be
+ * NULL) receives nbatch entries.  Counterpart in the reference: a loop of
+ * rt.Problem.solve calls (rt/solve.py:21-181), one per instance. */
+int rtg_solve_batched(rtg_handle* h, int nbatch, const int64_t* inst_off, const double* f,
+                      const double* g, double* u, const rtg_solve_opts* opts,
+                      rtg_solve_info* infos, void* stream);
+
 /* allocation-free inner products --------------------------------------------
  * No counterpart in the reference: this is the two-stage reduction rtg_solve
  * uses for its Arnoldi inner products and residual norms, offered to callers

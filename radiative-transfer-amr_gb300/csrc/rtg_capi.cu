@@ -164,6 +164,7 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
 void rtg_destroy(rtg_handle* h) {
     if (!h) return;
     cudaSetDevice(h->device);
+    free_batch(h);
     free_workspace(h);
     free_sweep(h);
     free_apply_plans(h);
@@ -268,6 +269,17 @@ int rtg_weight_forcing(rtg_handle* h, const double* fvals, double* out, void* st
         if (!h || !fvals || !out) throw RtgError{RTG_ERR_ARG, "null argument"};
         launch_weight_forcing(h, fvals, out, (cudaStream_t)stream);
     });
+}
+
+int rtg_solve_batched(rtg_handle* h, int nbatch, const int64_t* inst_off, const double* f, const double* g,
+                      double* u, const rtg_solve_opts* opts, rtg_solve_info* infos, void* stream) {
+    int inner = RTG_OK;
+    const int rc = guard("rtg_solve_batched", [&] {
+        if (!h || !inst_off || !f || !g || !u || !opts) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (opts->restart < 1 || opts->restart > 60) throw RtgError{RTG_ERR_ARG, "restart outside [1, 60]"};
+        inner = solve_batched(h, nbatch, inst_off, f, g, u, opts, infos, (cudaStream_t)stream);
+    });
+    return rc != RTG_OK ? rc : inner;
 }
 
 int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* opts,

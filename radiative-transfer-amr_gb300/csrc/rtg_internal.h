@@ -117,6 +117,7 @@ struct DevBuf {
 struct Workspace;  // Krylov workspace (rtg_krylov.cu)
 struct Sweep;      // sweep preconditioner (rtg_sweep.cu)
 struct ApplyPlan;  // column partition of the apply kernels (rtg_apply.cu)
+struct BatchWs;    // batched-solve workspace (rtg_batch.cu)
 
 }  // namespace rtg
 
@@ -133,6 +134,7 @@ struct rtg_handle {
     rtg::Sweep* sweep = nullptr;
     rtg::ApplyPlan* plan64 = nullptr;
     rtg::ApplyPlan* plan32 = nullptr;
+    rtg::BatchWs* bws = nullptr;
 };
 
 namespace rtg {
@@ -165,5 +167,10 @@ void free_sweep(rtg_handle* h);
 int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,
           rtg_solve_info* info, double* hist, int hist_cap, cudaStream_t s);
 void free_workspace(rtg_handle* h);
+
+// Batched solve (rtg_batch.cu)
+int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* f, const double* g, double* u,
+                  const rtg_solve_opts* o, rtg_solve_info* infos, cudaStream_t s);
+void free_batch(rtg_handle* h);
 
 }  // namespace rtg

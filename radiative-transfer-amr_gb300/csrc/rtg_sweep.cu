@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(kSweepThreads)
 sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
                         const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
-                        unsigned int epoch, unsigned int* __restrict__ next, int* __restrict__ status,
+                        const unsigned int* __restrict__ epoch_ptr, unsigned int* __restrict__ next,
+                        int* __restrict__ status,
                         int rhs_cap, int bcap, int ccap) {
     extern __shared__ unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);
@@ -186,6 +187,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     __shared__ int s_nc;
     __shared__ int s_k[kMaxCplStaged];
     __shared__ int s_off[kMaxCplStaged + 1];
+    const unsigned int epoch = __ldcg(epoch_ptr);   // set by sweep_begin_kernel
     for (;;) {
         if (threadIdx.x == 0) {
             s_idx = (int)atomicAdd(next, 1u);
@@ -360,6 +362,15 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     }
 }
 
+// Starts a sweep: advance the epoch (never 0, the flags' initial value) and
+// reset the work counter.  Device-side so that a captured graph can replay it.
+__global__ void sweep_begin_kernel(unsigned int* epoch, unsigned int* next) {
+    unsigned int e = *epoch + 1u;
+    if (e == 0u) e = 1u;
+    *epoch = e;
+    *next = 0u;
+}
+
 }  // namespace
 
 struct Sweep {
@@ -379,8 +390,8 @@ struct Sweep {
     std::vector<void*> allocs;
     unsigned int* d_done = nullptr;      // per element: epoch of the last sweep that finished it
     unsigned int* d_next = nullptr;      // work counter
+    unsigned int* d_epoch = nullptr;     // current epoch
     int* d_status = nullptr;             // RTG_ERR_TIMEOUT if a wait gave up
-    unsigned int epoch = 0;
 };
 
 namespace {
@@ -519,6 +530,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     if (status) throw RtgError{RTG_ERR_NONFINITE, "singular element block in the sweep preconditioner"};
     s->d_done = sw_alloc<unsigned int>(s, ne);
     s->d_next = sw_alloc<unsigned int>(s, 1);
+    s->d_epoch = sw_alloc<unsigned int>(s, 1);
+    RTG_CUDA(cudaMemset(s->d_epoch, 0, sizeof(unsigned int)));
     s->d_status = sw_alloc<int>(s, 1);
     RTG_CUDA(cudaMemset(s->d_done, 0, sizeof(unsigned int) * ne));
     RTG_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
@@ -552,11 +565,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     const bool f64 = sizeof(T) == 8;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     const OpView<T>& v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
-    if (++s->epoch == 0) {   // epoch wrapped: reset the flags
-        RTG_CUDA(cudaMemsetAsync(s->d_done, 0, sizeof(unsigned int) * h->host.elems.size(), st));
-        s->epoch = 1;
-    }
-    RTG_CUDA(cudaMemsetAsync(s->d_next, 0, sizeof(unsigned int), st));
+    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_epoch, s->d_next);
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
     int& grid = f64 ? s->grid64 : s->grid32;
@@ -576,8 +585,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
         grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
     }
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
-        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done, s->epoch,
-        s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c);
+        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done,
+        s->d_epoch, s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c);
     RTG_CUDA(cudaGetLastError());
 }
 

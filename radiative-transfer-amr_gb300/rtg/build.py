@@ -16,8 +16,8 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "librtg.so")
-SOURCES = ["rtg_build.cpp", "rtg_apply.cu", "rtg_krylov.cu", "rtg_sweep.cu", "rtg_capi.cu",
-           "rtg_noalloc.cu"]
+SOURCES = ["rtg_build.cpp", "rtg_apply.cu", "rtg_krylov.cu", "rtg_sweep.cu", "rtg_batch.cu",
+           "rtg_capi.cu", "rtg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

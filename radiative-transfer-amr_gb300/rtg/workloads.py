@@ -358,6 +358,48 @@ def config5_mesh(mesh_cls=Mesh, seed=0, scale=1.0):
                           nref_ang=3, nref_spt=4, ang_prob=0.42)
 
 
+def batch_instance(seed, mesh_cls=Mesh, max_cols=64, max_cells=16, n_range=(2, 8)):
+    """One instance of the batched workload, drawn from ``seed``: [0,1]^2,
+    8..64 spatial columns (random leaf h-refinement of a 2x2 start), 4..16
+    angular cells per column (at least 4 so that every cell lies in one
+    quadrant), a single degree p in [1, 7] (2..8 nodes) for x, y and th,
+    sigma_t ~ U(0.5, 5), sigma_s / sigma_t ~ U(0.1, 0.99), HG g ~ U(0, 0.95),
+    Gaussian isotropic source, vacuum inflow."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(n_range[0], n_range[1] + 1))
+    target_cols = int(rng.integers(8, max_cols + 1))
+    target_cells = int(rng.integers(4, max_cells + 1))
+    mesh = mesh_cls([1., 1.], [False, False], [n, n, n], True)
+    mesh.ref_mesh(kind="ang", form="h")
+    mesh.ref_mesh(kind="ang", form="h")
+    mesh.ref_mesh(kind="spt", form="h")
+    while len(mesh.cols) + 3 <= target_cols:
+        keys = sorted(mesh.cols.keys())
+        before = len(mesh.cols)
+        mesh.ref_col(keys[int(rng.integers(len(keys)))], kind="spt", form="h")
+        if len(mesh.cols) > max_cols:
+            break
+        if len(mesh.cols) == before:
+            break
+    # refine the same angular cell in every column until the target count
+    for _ in range(64):
+        c0 = mesh.cols[sorted(mesh.cols.keys())[0]]
+        if len(c0.cells) >= target_cells:
+            break
+        cand = [k for k in sorted(c0.cells.keys()) if c0.cells[k].lv < 4]
+        if not cand:
+            break
+        kk = cand[int(rng.integers(len(cand)))]
+        for ck in sorted(mesh.cols.keys()):
+            if kk in mesh.cols[ck].cells:
+                mesh.ref_cell(ck, kk, form="h")
+    sigma_t = float(rng.uniform(0.5, 5.))
+    ratio = float(rng.uniform(0.1, 0.99))
+    g = float(rng.uniform(0., 0.95))
+    xs, ys = (float(v) for v in rng.uniform(0.3, 0.7, size=2))
+    return mesh, gaussian_source_problem(sigma_t, ratio, g, xs=xs, ys=ys)
+
+
 def config2_mesh(mesh_cls=Mesh, seed=0):
     """Single adaptive problem mesh: [0,3]x[0,2], six rounds of seeded random
     hp refinement, nodes per dimension in [3, 7] (degree 2..6), about 2e5 DOF."""
