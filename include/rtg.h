@@ -67,6 +67,15 @@ extern "C" {
 #define RTG_FP64 0
 #define RTG_FP32 1
 
+/* learned correction of the sweep: network shape and training layouts */
+#define RTG_NN_IN 16           /* physics features per row                      */
+#define RTG_NN_HIDDEN 128      /* width of the two hidden layers                */
+#define RTG_NN_MOM 8           /* moments of z per row (7 used, 1 pad)          */
+#define RTG_NN_OUT 24          /* coefficients per row: C[3][RTG_NN_MOM]        */
+#define RTG_NN_STATS 12        /* training statistics per row (10 used, 2 pad)  */
+/* W1[16][128] b1[128] W2[128][128] b2[128] W3[128][24] b3[24] (FP32, row-major) */
+#define RTG_NN_NPARAM 21784
+
 typedef struct rtg_handle rtg_handle;
 
 /* Flattened hp mesh.  Columns in sorted-key order; elements (leaf cells) in
@@ -124,7 +133,11 @@ typedef struct rtg_solve_opts {
     int32_t max_it;        /* total inner iterations cap (reference: 5000)      */
     double  rtol;          /* relative residual target on ||r||/||b||           */
     double  atol;          /* absolute residual target                           */
-    int32_t precond;       /* 0 none, 1 upwind transport sweep (right precond.) */
+    int32_t precond;       /* 0 none, 1 upwind transport sweep (right precond.),
+                              2 sweep + column diffusion correction (two-level,
+                              FGMRES), 3 sweep + learned correction (FGMRES;
+                              needs rtg_nn_set_params), falling back to 1 on a
+                              stall */
     int32_t nonzero_guess; /* 1: start from x (reference: x0 = f_I)             */
     double  inner_rtol;    /* method 1: inner FP32 reduction per outer step     */
     int32_t max_outer;     /* method 1: cap on refinement steps                 */
@@ -143,6 +156,9 @@ typedef struct rtg_solve_info {
     double  seconds;       /* wall time inside rtg_solve                       */
     int32_t hist_len;      /* residual history entries written                 */
     int32_t sweeps;        /* preconditioner (sweep) applications              */
+    int32_t learned;       /* applications of the learned correction           */
+    int32_t fallbacks;     /* precond 3: switches to the sweep alone (stalls)  */
+    int32_t coarse;        /* applications of the diffusion correction         */
 } rtg_solve_info;
 
 /* library / quadrature ------------------------------------------------------ */
@@ -207,6 +223,46 @@ int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u,
 int rtg_solve_batched(rtg_handle* h, int nbatch, const int64_t* inst_off, const double* f,
                       const double* g, double* u, const rtg_solve_opts* opts,
                       rtg_solve_info* infos, void* stream);
+
+/* learned correction of the sweep --------------------------------------------
+ * No counterpart in the reference.  rtg_solve with precond 2 runs FGMRES with
+ * M(r) = z + L z, z = P^{-1} r (the sweep), L linear in z:
+ *   a row is one (element, spatial node ij) pair, rows in element order then
+ *   ij = i*ny + j;  m(z) = [m0, m1c, m1s, phi, em, cm, nm, 0] per row (angular
+ *   moments of z at the node, the column's angular mean phi, the element mean
+ *   of m0, the column mean of phi, its mean over the neighbour columns);
+ *   o = C m with C (3 x 8) from a 16-128-128-24 ReLU network of 16 physics
+ *   features of the row;  (L z) = o0 + o1 cos th + o2 sin th at the unknowns.
+ * The coefficients C are computed when the network is set.  Training uses
+ * per-row statistics of a target error e with t = (e - z)/s, s = rms(z):
+ *   loss = sum_rows o^T G o - 2 q^T o + c,  o = C m(z)/s.
+ * All array arguments are device pointers (params may also be host memory in
+ * rtg_nn_set_params); prec selects double (RTG_FP64) or float (RTG_FP32)
+ * vectors. */
+int rtg_nn_rows(rtg_handle* h, int64_t* rows);
+/* set the handle's network (RTG_NN_NPARAM floats) and compute its coefficients */
+int rtg_nn_set_params(rtg_handle* h, const float* params, void* stream);
+/* feat[rows][16]: the physics features of the handle's rows */
+int rtg_nn_features(rtg_handle* h, float* feat, void* stream);
+/* mom[rows][8] = m(z)/s and scale[0] = s = rms(z) */
+int rtg_nn_moments(rtg_handle* h, int prec, const void* z, float* mom, float* scale, void* stream);
+/* coef[rows][24] = network(feat); weights rounded to BF16, FP32 accumulation */
+int rtg_nn_forward(const float* params, const float* feat, int64_t rows, float* coef, void* stream);
+/* z += L z with the given coefficients (coef[rows][24]) */
+int rtg_nn_correct(rtg_handle* h, int prec, const float* coef, void* z, void* stream);
+/* stats[rows][12] of t = (e - z)/s times weight: G00 G01 G02 G11 G12 G22 q0 q1 q2 c 0 0 */
+int rtg_nn_targets(rtg_handle* h, int prec, const void* z, const void* e, const float* scale, float weight,
+                   float* stats, void* stream);
+/* floats of scratch rtg_nn_loss_grad needs */
+int64_t rtg_nn_work_floats(void);
+/* loss (device double, may be NULL) and grad[RTG_NN_NPARAM] over `rows` rows */
+int rtg_nn_loss_grad(const float* params, const float* feat, const float* mom, const float* stats, int64_t rows,
+                     float* work, float* grad, double* loss, void* stream);
+/* one Adam step (bias-corrected, decoupled weight decay wd) on all parameters */
+int rtg_nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
+                float beta2, float eps, float wd, void* stream);
+/* z = M r = (I + L) P^{-1} r with the handle's network (the preconditioner of precond 2) */
+int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream);
 
 /* allocation-free inner products --------------------------------------------
  * No counterpart in the reference: this is the two-stage reduction rtg_solve

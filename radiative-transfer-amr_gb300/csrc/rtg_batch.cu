@@ -128,14 +128,15 @@ __global__ void bcombine_kernel(const BChunk* __restrict__ ch, TX* __restrict__ 
     }
 }
 
-// y = a[b] * x + beta * y  (a per instance; a == nullptr means ascal)
+// y = a[b] * x + beta * y  (a per instance; a == nullptr means ascal); a zero
+// coefficient drops its term without reading it (uninitialised buffers)
 template <typename TX, typename TY>
 __global__ void bscale_kernel(const BChunk* __restrict__ ch, const TX* __restrict__ x, TY* __restrict__ y,
                               const double* __restrict__ a, int lda, double ascal, double beta) {
     const BChunk c = ch[blockIdx.x];
     const double s = a ? a[c.inst * lda] : ascal;
     for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x)
-        y[i] = (TY)(s * (double)x[i] + (beta == 0. ? 0. : beta * (double)y[i]));
+        y[i] = (TY)((s == 0. ? 0. : s * (double)x[i]) + (beta == 0. ? 0. : beta * (double)y[i]));
 }
 
 // Start of a restart cycle, one thread per instance: beta = ||r||, g = (beta, 0...).

@@ -346,6 +346,26 @@ void build_tables(const rtg_mesh_desc* m, const rtg_coeffs* c, HostTables& t) {
             }
     }
     t.ndof = dof;
+    t.nnodes = node;
+
+    // distinct face-neighbour columns (first-seen order, -1 padded) and the
+    // number of faces without a neighbour
+    t.col_nbr_raw.assign(m->col_nbr, m->col_nbr + (size_t)8 * nc);
+    t.col_nbr8.assign((size_t)8 * nc, -1);
+    t.col_free.assign(nc, 0);
+    for (int ci = 0; ci < nc; ++ci) {
+        int cnt = 0;
+        for (int f = 0; f < 4; ++f) {
+            const int a = m->col_nbr[8 * ci + 2 * f], b = m->col_nbr[8 * ci + 2 * f + 1];
+            if (a < 0 && b < 0) ++t.col_free[ci];
+            for (int nb : {a, b}) {
+                if (nb < 0) continue;
+                bool seen = false;
+                for (int q = 0; q < cnt; ++q) seen |= t.col_nbr8[8 * ci + q] == nb;
+                if (!seen) t.col_nbr8[8 * ci + cnt++] = nb;
+            }
+        }
+    }
 
     // coefficients at column nodes: kw = wx wy kappa, sw = wx wy sigma
     t.kw.resize(node);

@@ -165,6 +165,8 @@ void rtg_destroy(rtg_handle* h) {
     if (!h) return;
     cudaSetDevice(h->device);
     free_batch(h);
+    free_coarse(h);
+    free_nn(h);
     free_workspace(h);
     free_sweep(h);
     free_apply_plans(h);
@@ -226,6 +228,113 @@ int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stre
             apply_sweep<float>(h, (const float*)r, (float*)z, s);
         else
             throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
+int rtg_nn_rows(rtg_handle* h, int64_t* rows) {
+    return guard("rtg_nn_rows", [&] {
+        if (!h || !rows) throw RtgError{RTG_ERR_ARG, "null argument"};
+        *rows = nn_rows(h);
+    });
+}
+
+int rtg_nn_set_params(rtg_handle* h, const float* params, void* stream) {
+    return guard("rtg_nn_set_params", [&] {
+        if (!h || !params) throw RtgError{RTG_ERR_ARG, "null argument"};
+        nn_set_params(h, params, (cudaStream_t)stream);
+    });
+}
+
+int rtg_nn_features(rtg_handle* h, float* feat, void* stream) {
+    return guard("rtg_nn_features", [&] {
+        if (!h || !feat) throw RtgError{RTG_ERR_ARG, "null argument"};
+        nn_features(h, feat, (cudaStream_t)stream);
+    });
+}
+
+int rtg_nn_moments(rtg_handle* h, int prec, const void* z, float* mom, float* scale, void* stream) {
+    return guard("rtg_nn_moments", [&] {
+        if (!h || !z || !mom || !scale) throw RtgError{RTG_ERR_ARG, "null argument"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64)
+            nn_moments<double>(h, (const double*)z, mom, scale, s);
+        else if (prec == RTG_FP32)
+            nn_moments<float>(h, (const float*)z, mom, scale, s);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
+int rtg_nn_forward(const float* params, const float* feat, int64_t rows, float* coef, void* stream) {
+    return guard("rtg_nn_forward", [&] {
+        if (rows < 0) throw RtgError{RTG_ERR_ARG, "negative row count"};
+        if (rows > 0 && (!params || !feat || !coef)) throw RtgError{RTG_ERR_ARG, "null argument"};
+        nn_forward(params, feat, rows, coef, (cudaStream_t)stream);
+    });
+}
+
+int rtg_nn_correct(rtg_handle* h, int prec, const float* coef, void* z, void* stream) {
+    return guard("rtg_nn_correct", [&] {
+        if (!h || !coef || !z) throw RtgError{RTG_ERR_ARG, "null argument"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64)
+            nn_correct<double>(h, coef, (double*)z, s);
+        else if (prec == RTG_FP32)
+            nn_correct<float>(h, coef, (float*)z, s);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
+int rtg_nn_targets(rtg_handle* h, int prec, const void* z, const void* e, const float* scale, float weight,
+                   float* stats, void* stream) {
+    return guard("rtg_nn_targets", [&] {
+        if (!h || !z || !e || !scale || !stats) throw RtgError{RTG_ERR_ARG, "null argument"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64)
+            nn_stats<double>(h, (const double*)z, (const double*)e, scale, weight, stats, s);
+        else if (prec == RTG_FP32)
+            nn_stats<float>(h, (const float*)z, (const float*)e, scale, weight, stats, s);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+    });
+}
+
+int64_t rtg_nn_work_floats(void) { return nn_work_floats(); }
+
+int rtg_nn_loss_grad(const float* params, const float* feat, const float* mom, const float* stats, int64_t rows,
+                     float* work, float* grad, double* loss, void* stream) {
+    return guard("rtg_nn_loss_grad", [&] {
+        if (rows < 0) throw RtgError{RTG_ERR_ARG, "negative row count"};
+        if (!params || !work || !grad || (rows > 0 && (!feat || !mom || !stats)))
+            throw RtgError{RTG_ERR_ARG, "null argument"};
+        nn_loss_grad(params, feat, mom, stats, rows, work, grad, loss, (cudaStream_t)stream);
+    });
+}
+
+int rtg_nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
+                float beta2, float eps, float wd, void* stream) {
+    return guard("rtg_nn_adam", [&] {
+        if (!params || !grad || !m || !v) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (step < 1) throw RtgError{RTG_ERR_ARG, "step counts from 1"};
+        nn_adam(params, grad, m, v, step, lr, beta1, beta2, eps, wd, (cudaStream_t)stream);
+    });
+}
+
+int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream) {
+    return guard("rtg_nn_precondition", [&] {
+        if (!h || !r || !z) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (r == z) throw RtgError{RTG_ERR_ARG, "r and z alias"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (prec == RTG_FP64) {
+            apply_sweep<double>(h, (const double*)r, (double*)z, s);
+            apply_learned<double>(h, (double*)z, s);
+        } else if (prec == RTG_FP32) {
+            apply_sweep<float>(h, (const float*)r, (float*)z, s);
+            apply_learned<float>(h, (float*)z, s);
+        } else {
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+        }
     });
 }
 

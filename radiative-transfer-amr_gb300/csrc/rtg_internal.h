@@ -1,6 +1,7 @@
 // Internal definitions of librtg: operator tables on the host and device.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -105,7 +106,11 @@ struct HostTables {
     std::vector<double> kw, sw, ang, W, G, lglw, mort, econst, colc, cplc;
     std::vector<int64_t> W_off;
     std::vector<int32_t> sig_nth;
+    std::vector<int32_t> col_nbr8;   // [ncols][8] distinct neighbour columns, -1 padded
+    std::vector<int32_t> col_nbr_raw;  // [ncols][4 faces][2] neighbour columns as given, -1 none
+    std::vector<int32_t> col_free;   // [ncols] faces without a neighbour
     int64_t ndof = 0, ndof_interior = 0;
+    int32_t nnodes = 0;              // spatial nodes over all columns
     int32_t max_col_ndof = 0, max_nth_col = 0, max_cells_col = 0;
 };
 
@@ -118,6 +123,8 @@ struct Workspace;  // Krylov workspace (rtg_krylov.cu)
 struct Sweep;      // sweep preconditioner (rtg_sweep.cu)
 struct ApplyPlan;  // column partition of the apply kernels (rtg_apply.cu)
 struct BatchWs;    // batched-solve workspace (rtg_batch.cu)
+struct NNWs;       // learned correction of the sweep (rtg_nn.cu)
+struct Coarse;     // coarse-space correction of the two-level preconditioner (rtg_coarse.cu)
 
 }  // namespace rtg
 
@@ -135,6 +142,8 @@ struct rtg_handle {
     rtg::ApplyPlan* plan64 = nullptr;
     rtg::ApplyPlan* plan32 = nullptr;
     rtg::BatchWs* bws = nullptr;
+    rtg::NNWs* nn = nullptr;
+    rtg::Coarse* coarse = nullptr;
 };
 
 namespace rtg {
@@ -162,6 +171,36 @@ int sweep_levels_count(rtg_handle* h, cudaStream_t s);
 int sweep_lagged_count(rtg_handle* h, cudaStream_t s);
 int sweep_status(rtg_handle* h, cudaStream_t s);
 void free_sweep(rtg_handle* h);
+
+// Learned correction of the sweep (rtg_nn.cu)
+NNWs* get_nn(rtg_handle* h);
+void free_nn(rtg_handle* h);
+int64_t nn_rows(rtg_handle* h);
+void nn_set_params(rtg_handle* h, const float* params, cudaStream_t s);
+bool nn_has_params(rtg_handle* h);
+void nn_features(rtg_handle* h, float* feat, cudaStream_t s);
+template <typename T>
+void nn_moments(rtg_handle* h, const T* z, float* mom, float* scale, cudaStream_t s);
+void nn_forward(const float* params, const float* feat, int64_t rows, float* coef, cudaStream_t s);
+template <typename T>
+void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s);
+template <typename T>
+void nn_stats(rtg_handle* h, const T* z, const T* err, const float* scale, float weight, float* S, cudaStream_t s);
+int64_t nn_work_floats();
+void nn_loss_grad(const float* params, const float* feat, const float* mom, const float* stats, int64_t rows,
+                  float* work, float* grad, double* loss, cudaStream_t s);
+void nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float b1, float b2,
+             float eps, float wd, cudaStream_t s);
+template <typename T>
+void apply_learned(rtg_handle* h, T* z, cudaStream_t s);
+
+// Two-level preconditioner (rtg_coarse.cu): column diffusion correction
+void build_coarse(rtg_handle* h, cudaStream_t s);
+void free_coarse(rtg_handle* h);
+int coarse_size(rtg_handle* h);
+void coarse_operator(rtg_handle* h, double* out);
+template <typename T>
+void apply_coarse(rtg_handle* h, const T* v, T* z, cudaStream_t s);
 
 // Solver (rtg_krylov.cu)
 int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,

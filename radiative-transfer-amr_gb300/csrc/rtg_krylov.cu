@@ -8,6 +8,13 @@
 //    correction A d = r is solved with FP32 applies and FP32 basis vectors
 //    whose inner products accumulate in FP64; Hessenberg, Givens and the
 //    convergence test are FP64.
+//  * preconditioners 2 (sweep + column diffusion correction, rtg_coarse.cu)
+//    and 3 (sweep + learned correction, rtg_nn.cu) run flexible GMRES: the
+//    preconditioned vectors Z are kept and x += Z y, so the preconditioner is
+//    applied once per iteration.  With preconditioner 3 a restart cycle that
+//    cuts the residual by less than kStallRatio, or a refinement step whose
+//    FP64 residual falls by less than kOuterStallRatio, switches the rest of
+//    the solve to the sweep alone.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -101,12 +108,14 @@ __global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, c
         out[i] = (T)((double)w[i] * inv);
 }
 
-// y = a*x + b*y over full vectors of possibly different types
+// y = a*x + b*y over full vectors of possibly different types; a zero
+// coefficient drops its term without reading it (the buffer may hold anything,
+// NaN included)
 template <typename TX, typename TY>
 __global__ void axpby_kernel(double a, const TX* __restrict__ x, double b, TY* __restrict__ y, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        y[i] = (TY)(a * (double)x[i] + (b == 0. ? 0. : b * (double)y[i]));
+        y[i] = (TY)((a == 0. ? 0. : a * (double)x[i]) + (b == 0. ? 0. : b * (double)y[i]));
 }
 
 // x += sum_q c[q] V_q (c on device)
@@ -124,6 +133,9 @@ __global__ void combine_kernel(TX* __restrict__ x, const TV* __restrict__ V, int
     }
 }
 
+constexpr double kStallRatio = 0.9;
+constexpr double kOuterStallRatio = 0.5;
+
 inline int grid_for(int64_t n) {
     int64_t g = (n + 255) / 256;
     return (int)std::min<int64_t>(g, 152 * 8);
@@ -139,6 +151,8 @@ struct Workspace {
     double *b = nullptr, *r = nullptr, *x = nullptr, *t = nullptr, *gb = nullptr;
     double *w64 = nullptr, *z64 = nullptr, *t64 = nullptr;
     float *w32 = nullptr, *d32 = nullptr, *z32 = nullptr, *t32 = nullptr, *s32 = nullptr;
+    double* Z64 = nullptr;      // m x N flexible basis (preconditioners 2 and 3)
+    float* Z32 = nullptr;
     double* partial = nullptr;  // kRedBlocks x (m+1)
     double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
@@ -220,13 +234,34 @@ struct GmresResult {
     double res = 0.;
 };
 
+struct PcState {
+    int mode = 0;        // 0 none, 1 sweep, 2 sweep + diffusion, 3 sweep + learned (2, 3 flexible)
+    int sweeps = 0;
+    int coarse = 0;
+    int learned = 0;
+    int fallbacks = 0;
+};
+
+template <typename T>
+T* flex_basis(Workspace* ws, int m);
+template <>
+double* flex_basis<double>(Workspace* ws, int m) {
+    if (!ws->Z64) ws->Z64 = dalloc<double>(ws, (int64_t)m * ws->N);
+    return ws->Z64;
+}
+template <>
+float* flex_basis<float>(Workspace* ws, int m) {
+    if (!ws->Z32) ws->Z32 = dalloc<float>(ws, (int64_t)m * ws->N);
+    return ws->Z32;
+}
+
 // GMRES(m) for A_II d = r0 in precision T starting from d = 0.  rhs is given
 // in T (scaled); stops when the estimated residual <= tol_abs or after
 // max_it iterations.  Returns the solution in xT (T).  hist gets estimates.
 template <typename T>
 GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T* V, int m,
                   double tol_abs, int max_it, std::vector<double>* hist, int* applies,
-                  bool pc, T* zbuf, T* tbuf, int* sweeps, cudaStream_t s) {
+                  PcState& pc, T* zbuf, T* tbuf, cudaStream_t s) {
     const int64_t N = ws->N;
     GmresResult res;
     const OpView<T>& v = view<T>(h);
@@ -260,13 +295,29 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         }
         std::fill(g.begin(), g.end(), 0.);
         g[0] = beta;
+        const int mode = pc.mode;   // fixed for the cycle
+        const bool flex = mode >= 2;
+        T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
         int j = 0;
         for (; j < m && total < max_it; ++j) {
             T* vj = V + (int64_t)j * N;
             T* vn = V + (int64_t)(j + 1) * N;
-            if (pc) {
+            if (flex) {
+                T* zj = Z + (int64_t)j * N;       // flexible: w = A M(v_j), M(v_j) kept
+                apply_sweep<T>(h, vj, zj, s);
+                ++pc.sweeps;
+                if (mode == 2) {
+                    apply_coarse<T>(h, vj, zj, s);
+                    ++pc.coarse;
+                    ++*applies;
+                } else {
+                    apply_learned<T>(h, zj, s);
+                    ++pc.learned;
+                }
+                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zj, wbuf, s);
+            } else if (mode == 1) {
                 apply_sweep<T>(h, vj, zbuf, s);   // right preconditioning: w = A P^{-1} v_j
-                ++*sweeps;
+                ++pc.sweeps;
                 launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zbuf, wbuf, s);
             } else {
                 launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
@@ -321,18 +372,25 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             y[q] = sacc / H[(size_t)q * (m + 1) + q];
         }
         RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
-        if (pc) {
+        if (flex) {
+            // x += Z y
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N);
+        } else if (mode == 1) {
             // x += P^{-1} (V y)
             axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., tbuf, 0., tbuf, N);
             combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(tbuf, V, N, j, ws->hdev, 1., N);
             apply_sweep<T>(h, tbuf, zbuf, s);
-            ++*sweeps;
+            ++pc.sweeps;
             axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., zbuf, 1., xT, N);
         } else {
             combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N);
         }
         res.iters = total;
         if (res.converged) break;
+        if (mode == 3 && !(res.res < kStallRatio * beta)) {
+            pc.mode = 1;   // the learned correction stalled this cycle
+            ++pc.fallbacks;
+        }
     }
     res.iters = total;
     return res;
@@ -375,23 +433,32 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.fp64_applies++;
     inf.res0 = res;
     hv.push_back(res);
-    int applies32 = 0, applies64 = 0, sweeps = 0;
-    const bool pc = o->precond == 1;
-    if (pc) get_sweep(h, s);
+    int applies32 = 0, applies64 = 0;
+    PcState pc;
+    pc.mode = o->precond;
+    if (pc.mode < 0 || pc.mode > 3) throw RtgError{RTG_ERR_ARG, "unknown preconditioner"};
+    if (pc.mode == 3 && !nn_has_params(h))
+        throw RtgError{RTG_ERR_ARG, "preconditioner 3 needs a network (rtg_nn_set_params)"};
+    if (pc.mode >= 1) get_sweep(h, s);
+    if (pc.mode == 2 && !h->coarse) build_coarse(h, s);
 
     if (o->method == 0) {
         // GMRES on the correction: A d = r, x += d, repeated until converged.
         int used = 0;
         while (res > tol && used < o->max_it) {
             GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
-                                           o->max_it - used, &hv, &applies64, pc, ws->z64, ws->t64,
-                                           &sweeps, s);
+                                           o->max_it - used, &hv, &applies64, pc, ws->z64, ws->t64, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N);
+            const double prev = res;
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
             inf.fp64_applies++;
             hv.push_back(res);
             if (gr.iters == 0) break;
+            if (pc.mode == 3 && !(res < kOuterStallRatio * prev)) {
+                pc.mode = 1;
+                ++pc.fallbacks;
+            }
         }
         inf.iterations = used;
     } else {
@@ -405,21 +472,29 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
             const int inner_cap = std::min(o->max_it - used, 20 * m);
             GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, ws->s32, ws->V32, m,
                                           std::max(inner_rtol, tol / res), inner_cap,
-                                          nullptr, &applies32, pc, ws->z32, ws->t32, &sweeps, s);
+                                          nullptr, &applies32, pc, ws->z32, ws->t32, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N);
+            const double prev = res;
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
             inf.fp64_applies++;
             hv.push_back(res);
             ++outer;
+            if (pc.mode == 3 && !(res < kOuterStallRatio * prev)) {
+                pc.mode = 1;   // the FP64 residual stalled: the sweep alone from here on
+                ++pc.fallbacks;
+            }
         }
         inf.iterations = used;
         inf.outer = outer;
     }
     inf.fp64_applies += applies64;
     inf.fp32_applies += applies32;
-    inf.sweeps = sweeps;
-    if (pc && sweep_status(h, s) != RTG_OK)
+    inf.sweeps = pc.sweeps;
+    inf.learned = pc.learned;
+    inf.coarse = pc.coarse;
+    inf.fallbacks = pc.fallbacks;
+    if (o->precond >= 1 && sweep_status(h, s) != RTG_OK)
         throw RtgError{RTG_ERR_TIMEOUT, "a sweep wait gave up; the solution is not valid"};
     inf.res_f = res;
     inf.converged = res <= tol ? 1 : 0;

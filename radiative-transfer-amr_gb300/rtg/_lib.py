@@ -26,6 +26,13 @@ RTG_MASK_ROWS = 32
 RTG_FP64 = 0
 RTG_FP32 = 1
 
+RTG_NN_IN = 16
+RTG_NN_HIDDEN = 128
+RTG_NN_MOM = 8
+RTG_NN_OUT = 24
+RTG_NN_STATS = 12
+RTG_NN_NPARAM = 21784
+
 i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
 f64p = C.POINTER(C.c_double)
@@ -62,7 +69,8 @@ class SolveInfo(C.Structure):
     _fields_ = [("converged", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
                 ("fp64_applies", C.c_int32), ("fp32_applies", C.c_int32), ("res0", C.c_double),
                 ("res_f", C.c_double), ("rhs_norm", C.c_double), ("seconds", C.c_double),
-                ("hist_len", C.c_int32), ("sweeps", C.c_int32)]
+                ("hist_len", C.c_int32), ("sweeps", C.c_int32), ("learned", C.c_int32),
+                ("fallbacks", C.c_int32), ("coarse", C.c_int32)]
 
 
 # exported symbol -> (restype, argtypes)
@@ -86,6 +94,20 @@ SIGNATURES = {
                                     C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.c_void_p]),
     "rtg_dots_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                                    C.c_void_p, C.c_void_p]),
+    "rtg_nn_rows": (C.c_int, [C.c_void_p, i64p]),
+    "rtg_nn_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_nn_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_nn_moments": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_nn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "rtg_nn_correct": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_nn_targets": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                 C.c_void_p, C.c_void_p]),
+    "rtg_nn_work_floats": (C.c_int64, []),
+    "rtg_nn_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_nn_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float,
+                              C.c_float, C.c_float, C.c_float, C.c_void_p]),
+    "rtg_nn_precondition": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

@@ -353,8 +353,10 @@ class Problem:
         method = {"gmres": 0, "mixed": 1, "fgmres": 0}.get(opts["ksp_type"])
         if method is None:
             raise ValueError("unsupported ksp_type {}".format(opts["ksp_type"]))
-        # PETSc's "bjacobi" default maps to the sweep, the GPU preconditioner
-        precond = {"none": 0, "sweep": 1, "bjacobi": 1}.get(opts["pc_type"])
+        # PETSc's "bjacobi" default maps to the sweep, the GPU preconditioner;
+        # "dsa" adds the column diffusion correction, "learned" the learned
+        # correction (a network set with rtg.learned.set_params)
+        precond = {"none": 0, "sweep": 1, "bjacobi": 1, "dsa": 2, "learned": 3}.get(opts["pc_type"])
         if precond is None:
             raise ValueError("unsupported pc_type {}".format(opts["pc_type"]))
         x0 = f_dev if opts["x0"] == "forcing" else None

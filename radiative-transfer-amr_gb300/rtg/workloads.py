@@ -406,3 +406,23 @@ def config2_mesh(mesh_cls=Mesh, seed=0):
     return random_hp_mesh([3., 2.], 3, 3, rounds=6, seed=seed, frac_spt=0.3,
                           frac_ang=0.12, p_prob=0.5, n_max=7, nref_ang=2,
                           nref_spt=2, mesh_cls=mesh_cls)
+
+
+def config4_instance(seed, mesh_cls=Mesh, rounds=3, n_max=6):
+    """One problem of the learned-preconditioner family (config-2 type): the
+    Gaussian-bump scatterer on [0,3]x[0,2] with seeded amplitude
+    (log-uniform in [0.5, 50]), width (U(0.1, 0.3)), centre
+    (U([0.6, 2.4] x [0.5, 1.5])) and HG g (U(0, 0.95)), sigma_t = sigma_s +
+    0.01, the config-2 beam inflow, on a seeded random hp mesh of the config-2
+    recipe with fewer rounds (about 2e4 to 1e5 DOF at rounds=3)."""
+    rng = np.random.default_rng(7919 + seed)
+    amp = float(np.exp(rng.uniform(np.log(0.5), np.log(50.))))
+    width = float(rng.uniform(0.1, 0.3))
+    xc = float(rng.uniform(0.6, 2.4))
+    yc = float(rng.uniform(0.5, 1.5))
+    g = float(rng.uniform(0., 0.95))
+    mesh = random_hp_mesh([3., 2.], 3, 3, rounds=rounds, seed=seed, frac_spt=0.3, frac_ang=0.12,
+                          p_prob=0.5, n_max=n_max, nref_ang=2, nref_spt=2, mesh_cls=mesh_cls)
+    spec = gaussian_bump_problem(amp=amp, width=width, xc=xc, yc=yc, g=g)
+    spec.meta.update({"amp": amp, "width": width, "xc": xc, "yc": yc, "seed": seed})
+    return mesh, spec
