@@ -196,6 +196,15 @@ int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, doubl
  * of z at inflow-boundary DOFs are zero.  The first call builds the element
  * block inverses (device memory owned by the handle). */
 int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream);
+/* One sweep as rtg_precondition, recording for every element e
+ * trace[8e .. 8e+7] = {claimed, upwind inputs ready, published, CTA, upwind
+ * lines loaded, couplings formed, values stored, fence passed} (device array
+ * of 8*nelem uint64, times in GPU global-timer nanoseconds) and, when
+ * level (host, nelem int32) is not NULL, each element's wavefront level.  A
+ * profiling aid: the sweep's cost is its level count times the per-level
+ * latency these timestamps resolve. */
+int rtg_sweep_trace(rtg_handle* h, int prec, const void* r, void* z, uint64_t* trace, int32_t* level,
+                    void* stream);
 /* out_beta = (dx dy dth / 8) wx_i wy_j wth_a * fvals_beta (device doubles). */
 int rtg_weight_forcing(rtg_handle* h, const double* fvals, double* out, void* stream);
 

@@ -338,6 +338,23 @@ int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* s
     });
 }
 
+int rtg_sweep_trace(rtg_handle* h, int prec, const void* r, void* z, uint64_t* trace, int32_t* level,
+                    void* stream) {
+    return guard("rtg_sweep_trace", [&] {
+        if (!h || !r || !z || !trace) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (r == z) throw RtgError{RTG_ERR_ARG, "r and z alias"};
+        cudaStream_t s = (cudaStream_t)stream;
+        unsigned long long* tr = reinterpret_cast<unsigned long long*>(trace);
+        if (prec == RTG_FP64)
+            apply_sweep<double>(h, (const double*)r, (double*)z, s, tr);
+        else if (prec == RTG_FP32)
+            apply_sweep<float>(h, (const float*)r, (float*)z, s, tr);
+        else
+            throw RtgError{RTG_ERR_ARG, "unknown precision"};
+        if (level) sweep_levels(h, level, s);
+    });
+}
+
 int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream) {
     return guard("rtg_interior_mask", [&] {
         if (!h || !mask) throw RtgError{RTG_ERR_ARG, "null argument"};

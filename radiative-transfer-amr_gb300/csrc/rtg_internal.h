@@ -166,6 +166,9 @@ void free_apply_plans(rtg_handle* h);
 // Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
+template <typename T>
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace);
+void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
 int sweep_levels_count(rtg_handle* h, cudaStream_t s);
 int sweep_lagged_count(rtg_handle* h, cudaStream_t s);

@@ -168,7 +168,29 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
 // order, so they were claimed by CTAs that are already running and the wait
 // always ends unless a CTA gave up.  A CTA that gives up sets *status and
 // every other CTA stops waiting as soon as it sees the status.
+//
+// The critical path of the sweep is the work an element does after its wait,
+// so everything that does not depend on upwind values happens before it: the
+// block inverse, the residual, the mortar matrices and, by linearity,
+//     zpre = B rin                         (before the wait)
+//     z    = zpre - B c,  c = couplings    (after the wait)
+// where c is nonzero only on the face nodes that have active couplings, so the
+// second product runs over those face columns of B only.  The couplings are
+// factorised per neighbour: T[jj][r] = sum_a Et[a][r] zl[jj][a], then
+// c[q][r] = sum_neighbours dcoeff sum_jj Es[jj][q] T[jj][r].
 constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
+constexpr int kMaxFaceNodes = 4 * kMaxNodes;
+constexpr int kTr = 8;   // trace entries per element
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool on_face(int F, int i, int j, int nx, int ny) {
+    return (F == 0 && i == nx - 1) || (F == 1 && j == ny - 1) || (F == 2 && i == 0) || (F == 3 && j == 0);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kSweepThreads)
@@ -177,16 +199,24 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
                         const unsigned int* __restrict__ epoch_ptr, unsigned int* __restrict__ next,
                         int* __restrict__ status,
-                        int rhs_cap, int bcap, int ccap) {
+                        int rhs_cap, int bcap, int ccap, unsigned long long* __restrict__ trace) {
     extern __shared__ unsigned char sraw[];
-    T* rhs = reinterpret_cast<T*>(sraw);
-    T* Bs = rhs + rhs_cap;
-    T* cs = Bs + bcap;   // staged couplings: per active coupling Es | Et | upwind face line
+    T* rhs = reinterpret_cast<T*>(sraw);      // rin, then the couplings c (face nodes)
+    T* zpre = rhs + rhs_cap;                  // B rin
+    T* Bs = zpre + rhs_cap;
+    T* cs = Bs + bcap;   // staged couplings: per active coupling Es | Et | upwind face line | T
     __shared__ int s_idx;
     __shared__ int s_abort;
     __shared__ int s_nc;
+    __shared__ int s_nf;
     __shared__ int s_k[kMaxCplStaged];
     __shared__ int s_off[kMaxCplStaged + 1];
+    __shared__ int s_face[kMaxFaceNodes];     // face nodes (ij) with active couplings
+    // metadata of the staged couplings (read on the critical path)
+    __shared__ int s_F[kMaxCplStaged], s_m1[kMaxCplStaged], s_nt1[kMaxCplStaged], s_n0[kMaxCplStaged];
+    __shared__ int s_str[kMaxCplStaged];
+    __shared__ long long s_base[kMaxCplStaged];
+    __shared__ T s_dc[kMaxCplStaged];
     const unsigned int epoch = __ldcg(epoch_ptr);   // set by sweep_begin_kernel
     for (;;) {
         if (threadIdx.x == 0) {
@@ -197,39 +227,60 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         const int idx = s_idx;
         if (idx >= ne) break;
         const int e = order[idx];
+        if (trace && threadIdx.x == 0) trace[kTr * e] = globaltimer_ns();
         const ElemDev E = v.elems[e];
         const ColDev C = v.cols[E.col];
         const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
         const int bm = E.flags >> 4;
-        // the element's residual and block inverse do not depend on the
-        // sweep: load them before waiting so their latency overlaps the wait
+        // ---- independent of the sweep: block inverse, residual, mortars
         const T* B = inv + inv_elem_off[e];
         const int bsize = nth * nn * nn;
         const bool staged = bsize <= bcap;
         if (staged)
             for (int t = threadIdx.x; t < bsize; t += blockDim.x) Bs[t] = __ldg(B + t);
+        const T* Bv = staged ? Bs : B;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
             rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
         }
-        // table of the active couplings and their staging offsets
         if (threadIdx.x == 0) {
-            int nc = 0, off = 0;
-            for (int k = E.cpl_begin; k < E.cpl_end && nc < kMaxCplStaged; ++k) {
+            int nc = 0, off = 0, fm = 0;
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
                 if (!active[k]) continue;
+                fm |= 1 << v.cpls[k].face;
+                if (nc >= kMaxCplStaged) {
+                    off = ccap + 1;   // too many: read from global memory
+                    continue;
+                }
                 const CplGeo g = v.cgeo[k];
-                const int n0 = (v.cpls[k].face % 2 == 0) ? C.ny : C.nx;
+                const int F = v.cpls[k].face;
+                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
                 s_k[nc] = k;
                 s_off[nc] = off;
-                off += g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1;
+                s_F[nc] = F;
+                s_m1[nc] = g.m1;
+                s_nt1[nc] = g.nth1;
+                s_n0[nc] = n0;
+                s_str[nc] = g.stride;
+                s_base[nc] = g.base;
+                s_dc[nc] = v.cplc[k];
+                off += g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1 + g.m1 * nth;
                 ++nc;
             }
             s_off[nc] = off;
-            s_nc = (off <= ccap && nc < kMaxCplStaged) ? nc : -1;   // -1: read from global memory
+            s_nc = (off <= ccap) ? nc : -1;   // -1: read from global memory
+            int nf = 0;
+            for (int ij = 0; ij < nn && nf < kMaxFaceNodes; ++ij) {
+                const int i = ij / C.ny, j = ij % C.ny;
+                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+                bool hit = false;
+                for (int F = 0; F < 4; ++F) hit |= ((fm >> F) & 1) && on_face(F, i, j, C.nx, C.ny);
+                if (hit) s_face[nf++] = ij;
+            }
+            s_nf = nf;
         }
         __syncthreads();
-        // stage the mortar matrices now (they do not depend on the sweep)
-        const int ncs = s_nc;
+        const int ncs = s_nc, nf = s_nf;
         for (int c = 0; c < ncs; ++c) {
             const int k = s_k[c];
             const CplDev cp = v.cpls[k];
@@ -239,7 +290,17 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             for (int t = threadIdx.x; t < g.m1 * n0; t += blockDim.x) dst[t] = __ldg(v.mort + cp.es + t);
             for (int t = threadIdx.x; t < g.nth1 * nth; t += blockDim.x) dst[g.m1 * n0 + t] = __ldg(v.mort + cp.et + t);
         }
-        // wait for the upwind elements this one reads
+        __syncthreads();
+        // zpre = B rin, block stored as [r][k][ij]
+        for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+            const int r = t / nn, ij = t % nn;
+            const T* col = Bv + r * nn * nn + ij;
+            T acc = T(0);
+#pragma unroll 4
+            for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
+            zpre[ij * nth + r] = acc;
+        }
+        // ---- wait for the upwind elements this one reads
         for (int k = E.cpl_begin + threadIdx.x; k < E.cpl_end; k += blockDim.x) {
             if (!active[k]) continue;
             const int nb = v.cpls[k].nbr;
@@ -260,62 +321,69 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         __syncthreads();
         if (s_abort) break;
         __threadfence();
+        if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
+        // ---- couplings c on the face nodes, into rhs[ij * nth + r]
         if (ncs >= 0) {
-            // stage every upwind face line with one round of parallel loads
             for (int c = 0; c < ncs; ++c) {
-                const int k = s_k[c];
-                const CplGeo g = v.cgeo[k];
-                const int n0 = (v.cpls[k].face % 2 == 0) ? C.ny : C.nx;
-                T* dst = cs + s_off[c] + g.m1 * n0 + g.nth1 * nth;
-                const int len = g.m1 * g.nth1;
-                for (int t = threadIdx.x; t < len; t += blockDim.x) {
-                    const int jj = t / g.nth1, a = t % g.nth1;
-                    dst[t] = __ldcg(z + g.base + (int64_t)jj * g.stride + a);
+                const int m1 = s_m1[c], nt1 = s_nt1[c];
+                T* dst = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth;
+                const T* src = z + s_base[c];
+                const int str = s_str[c];
+                for (int t = threadIdx.x; t < m1 * nt1; t += blockDim.x) {
+                    const int jj = t / nt1, a = t % nt1;
+                    dst[t] = __ldcg(src + (int64_t)jj * str + a);
                 }
             }
             __syncthreads();
-            // subtract the upwind face couplings on the element's face nodes
-            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-                const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-                if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
-                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+            if (trace && threadIdx.x == 0) trace[kTr * e + 4] = globaltimer_ns();
+            // T[jj][r] = sum_a Et[a][r] zl[jj][a], all couplings at once
+            {
+                int c = 0, base = 0;
+                for (int t = threadIdx.x;; t += blockDim.x) {
+                    // advance to the coupling that holds item t
+                    while (c < ncs && t >= base + s_m1[c] * nth) {
+                        base += s_m1[c] * nth;
+                        ++c;
+                    }
+                    if (c >= ncs) break;
+                    const int m1 = s_m1[c], nt1 = s_nt1[c];
+                    const T* Et = cs + s_off[c] + m1 * s_n0[c];
+                    const T* zl = Et + nt1 * nth;
+                    T* Tm = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth + m1 * nt1;
+                    const int q = t - base, jj = q / nth, r = q % nth;
+                    T acc = T(0);
+                    for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
+                    Tm[jj * nth + r] = acc;
+                }
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
+                const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
                 T acc = T(0);
                 for (int c = 0; c < ncs; ++c) {
-                    const int k = s_k[c];
-                    const int F = v.cpls[k].face;
-                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                    (F == 3 && j == 0);
-                    if (!on) continue;
-                    const CplGeo g = v.cgeo[k];
-                    const int q = (F % 2 == 0) ? j : i;
-                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    const int F = s_F[c];
+                    if (!on_face(F, i, j, C.nx, C.ny)) continue;
+                    const int m1 = s_m1[c], n0 = s_n0[c];
+                    const int qq = (F % 2 == 0) ? j : i;
                     const T* Es = cs + s_off[c];
-                    const T* Et = Es + g.m1 * n0;
-                    const T* zl = Et + g.nth1 * nth;
-                    const T dc = v.cplc[k];
-                    for (int jj = 0; jj < g.m1; ++jj) {
-                        T sacc = T(0);
-                        for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * zl[jj * g.nth1 + a];
-                        acc += dc * Es[jj * n0 + q] * sacc;
-                    }
+                    const T* Tm = Es + m1 * n0 + s_nt1[c] * nth + m1 * s_nt1[c];
+                    T sacc = T(0);
+                    for (int jj = 0; jj < m1; ++jj) sacc += Es[jj * n0 + qq] * Tm[jj * nth + r];
+                    acc += s_dc[c] * sacc;
                 }
-                rhs[l] -= acc;
+                rhs[ij * nth + r] = acc;
             }
         } else {
-            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-                const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-                if (!(i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) continue;
-                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+            for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
+                const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
                 T acc = T(0);
                 for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
                     if (!active[k]) continue;
                     const CplDev cp = v.cpls[k];
                     const int F = cp.face;
-                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                    (F == 3 && j == 0);
-                    if (!on) continue;
+                    if (!on_face(F, i, j, C.nx, C.ny)) continue;
                     const CplGeo g = v.cgeo[k];
-                    const int q = (F % 2 == 0) ? j : i;
+                    const int qq = (F % 2 == 0) ? j : i;
                     const int n0 = (F % 2 == 0) ? C.ny : C.nx;
                     const T* Es = v.mort + cp.es;
                     const T* Et = v.mort + cp.et;
@@ -324,41 +392,39 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                         const T* zl = z + g.base + (int64_t)jj * g.stride;
                         T sacc = T(0);
                         for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
-                        acc += dc * Es[jj * n0 + q] * sacc;
+                        acc += dc * Es[jj * n0 + qq] * sacc;
                     }
                 }
-                rhs[l] -= acc;
+                rhs[ij * nth + r] = acc;
             }
         }
         __syncthreads();
-        // z[ij, r] = sum_k B_r[ij][k] rhs[k, r] (block stored as [k][ij])
-        if (staged) {
-            for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
-                const int r = t / nn, ij = t % nn;
-                const T* col = Bs + r * nn * nn + ij;
-                T acc = T(0);
-#pragma unroll 4
-                for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
-                __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
-            }
-        } else for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+        if (trace && threadIdx.x == 0) trace[kTr * e + 5] = globaltimer_ns();
+        // ---- z = zpre - B c over the face columns of B
+        for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
-            const T* col = B + (int64_t)r * nn * nn + ij;
-            T acc = T(0);
-            int k = 0;
-            for (; k + 16 <= nn; k += 16) {
-                T bv[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) bv[u] = col[(int64_t)(k + u) * nn];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) acc += bv[u] * rhs[(k + u) * nth + r];
+            const T* col = Bv + r * nn * nn + ij;
+            T acc = zpre[ij * nth + r];
+            for (int f = 0; f < nf; ++f) {
+                const int k = s_face[f];
+                acc -= col[k * nn] * rhs[k * nth + r];
             }
-            for (; k < nn; ++k) acc += col[(int64_t)k * nn] * rhs[k * nth + r];
             __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
+        }
+        if (trace) {
+            __syncthreads();
+            if (threadIdx.x == 0) trace[kTr * e + 6] = globaltimer_ns();
         }
         __threadfence();
         __syncthreads();
-        if (threadIdx.x == 0) atomicExch(&done[e], epoch);
+        if (threadIdx.x == 0) {
+            if (trace) trace[kTr * e + 7] = globaltimer_ns();
+            atomicExch(&done[e], epoch);
+            if (trace) {
+                trace[kTr * e + 2] = globaltimer_ns();
+                trace[kTr * e + 3] = (unsigned long long)blockIdx.x;
+            }
+        }
     }
 }
 
@@ -376,6 +442,7 @@ __global__ void sweep_begin_kernel(unsigned int* epoch, unsigned int* next) {
 struct Sweep {
     int nlev = 0;
     std::vector<int32_t> lev_start;      // host CSR over levels
+    std::vector<int32_t> h_lev_elems;    // elements in level order (host copy)
     int32_t* d_lev_elems = nullptr;
     uint8_t* d_active = nullptr;
     double* d_inv64 = nullptr;
@@ -476,6 +543,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     for (int L = 0; L < nlev; ++L) s->lev_start[L + 1] += s->lev_start[L];
     std::vector<int32_t> lev_elems(ne), fill(s->lev_start.begin(), s->lev_start.end() - 1);
     for (int e = 0; e < ne; ++e) lev_elems[fill[level[e]]++] = e;
+    s->h_lev_elems = lev_elems;
     // a coupling is active when its upwind element sits on an earlier level
     std::vector<uint8_t> active(t.cpls.size(), 0);
     for (int e = 0; e < ne; ++e)
@@ -550,7 +618,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             if (!active[k]) continue;
             const CplGeo& g = t.cgeo[k];
             const int n0 = (t.cpls[k].face % 2 == 0) ? C.ny : C.nx;
-            c += (int64_t)g.m1 * n0 + (int64_t)g.nth1 * E.nth + (int64_t)g.m1 * g.nth1;
+            c += (int64_t)g.m1 * n0 + (int64_t)g.nth1 * E.nth + (int64_t)g.m1 * g.nth1 + (int64_t)g.m1 * E.nth;
         }
         max_c = std::max(max_c, c);
     }
@@ -559,8 +627,11 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
 }
 
 // z = P^{-1} r (full-length vectors; inflow-boundary entries of z are zero).
+// With trace, element e records [claim, ready, published, cta, upwind lines
+// loaded, couplings formed, values stored, fence passed] (globaltimer ns) in
+// trace[8e .. 8e+7].
 template <typename T>
-void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
@@ -571,7 +642,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     int& grid = f64 ? s->grid64 : s->grid32;
     const int rhs_cap = std::max(s->max_nloc, 1);
     if (grid == 0) {
-        const size_t rhs_bytes = sizeof(T) * (size_t)(rhs_cap + s->max_c);
+        const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
         const int64_t fit = (int64_t)((kSweepSmemBudget - std::min(rhs_bytes, kSweepSmemBudget)) / sizeof(T));
         bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
         smem = rhs_bytes + sizeof(T) * (size_t)bcap;
@@ -586,8 +657,20 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     }
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
         v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done,
-        s->d_epoch, s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c);
+        s->d_epoch, s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c, trace);
     RTG_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
+    apply_sweep<T>(h, r, z, st, nullptr);
+}
+
+// level of each element in the sweep order (host array of nelem)
+void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t st) {
+    Sweep* s = get_sweep(h, st);
+    for (int L = 0; L < s->nlev; ++L)
+        for (int q = s->lev_start[L]; q < s->lev_start[L + 1]; ++q) level[s->h_lev_elems[q]] = L;
 }
 
 // RTG_OK, or RTG_ERR_TIMEOUT if a sweep wait gave up since the last check.
@@ -603,6 +686,8 @@ int sweep_status(rtg_handle* h, cudaStream_t st) {
 
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t);
+template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t, unsigned long long*);
+template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t, unsigned long long*);
 
 int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
 int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
