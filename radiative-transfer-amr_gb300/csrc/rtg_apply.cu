@@ -149,8 +149,9 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
     __syncthreads();
     const TX* xc = x + C.dof_off;
     // stage x transposed: Xs[(row_e + a) * nij + ij] = x[off_e + ij*nth + a]
+    // (d grows per thread, so the cell index k only moves forward)
+    int k = 0;
     for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
-        int k = 0;
         while (d >= cbeg[k + 1]) ++k;
         const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
         const int l = d - cbeg[k];
@@ -170,8 +171,8 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
     const T* Gx = v.G + gofs(C.nx);
     const T* Gy = v.G + gofs(C.ny);
     TX* yc = y + C.dof_off;
+    k = 0;
     for (int d = it.y + threadIdx.x; d < it.z; d += blockDim.x) {
-        int k = 0;
         while (d >= cbeg[k + 1]) ++k;
         const int e = C.elem_begin + k;
         const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
@@ -246,6 +247,215 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
         if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1))
             acc += face_terms<T, TX, kParity>(v, mortf, C, E, e, i, j, r, xself, x);
         yc[d] = TX(acc);
+    }
+}
+
+// ------------------------------------------------------------ tiled path
+// FP32 only (the FP64 path keeps the reference's drop rules).  Work item:
+// whole cells [cell_begin, cell_end) of one column, i.e. the rectangle of
+// angular rows R0 .. R0+M-1 times all nij spatial nodes.  The scattering of the
+// item is the product Y[m][ij] = sum_c W[R0+m][c] X[c][ij] over all Nth angular
+// nodes of the column; it runs from shared memory with 4 x 4 register tiles
+// (16 FMAs per two 16-byte loads).  The epilogue adds extinction, streaming
+// and face terms and writes y in global order.
+// The inflow face fluxes of the item's elements are factorised per coupling
+// (T[jj][r] = sum_a Et[a][r] x_nbr[jj][a], then sum_jj Es[jj][q] T[jj][r]) and
+// accumulated into Fy before the epilogue; T and Fy reuse the W region.
+// Shared memory: Xs[Nth][nijp] | WsT[Nth][Mp] (later T | Fy[Mp][nijp]) |
+// Ys[Mp][nijp] | cell tables.
+struct TileItem {
+    int col, cell_begin, cell_end, row0;
+    int cpl_begin, cpl_end;   // entries of the item's couplings
+    int tsz;                  // floats of T (padded to 4)
+    int wcap;                 // floats of the W region
+    int ttot, ctot;           // work items of the two flux phases
+};
+
+// One coupling of a tiled item: where its neighbour line is, its mortars,
+// and its offsets in the two flux phases.
+struct TileCpl {
+    int64_t base;             // neighbour line: x[base + jj*stride + a]
+    int rowloc, nth, toff, coff;
+    int m1, nt1, n0, face;
+    int stride, es, et;
+    float dc;
+};
+constexpr int kMaxItemCpl = 96;
+
+__global__ void __launch_bounds__(kApplyThreads)
+apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__ items,
+                   const TileCpl* __restrict__ cpl_ent, const float* __restrict__ x, float* __restrict__ y) {
+    extern __shared__ float4 smt4[];
+    __shared__ TileCpl sc[kMaxItemCpl];
+    float* smt = reinterpret_cast<float*>(smt4);
+    const TileItem it = items[blockIdx.x];
+    const int ci = it.col;
+    const ColDev C = v.cols[ci];
+    const ApplyFlags fl = decode(flags);
+    const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
+    const int nijp = (nij + 3) & ~3;
+    const int M = [&] {
+        int m = 0;
+        for (int k = it.cell_begin; k < it.cell_end; ++k) m += v.elems[C.elem_begin + k].nth;
+        return m;
+    }();
+    const int Mp = (M + 3) & ~3;
+    float* Xs = smt;                                  // [Nth][nijp]
+    float* WsT = Xs + (size_t)Nth * nijp;             // [Nth][Mp]
+    float* Ys = WsT + (size_t)it.wcap;                // [Mp][nijp]
+    float* Tb = WsT;                                  // after the product: T
+    float* Fy = WsT + it.tsz;                         //                    Fy[Mp][nijp]
+    int* cbeg = reinterpret_cast<int*>(Ys + (size_t)Mp * nijp);   // [ncell+1] local DOF start
+    int* crow = cbeg + ncell + 1;                                  // [ncell] first row
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int k = 0; k < ncell; ++k) {
+            const ElemDev E = v.elems[C.elem_begin + k];
+            cbeg[k] = off;
+            crow[k] = E.row;
+            off += nij * E.nth;
+        }
+        cbeg[ncell] = off;
+    }
+    const int nent = it.cpl_end - it.cpl_begin;
+    for (int q = threadIdx.x; q < nent; q += blockDim.x) sc[q] = cpl_ent[it.cpl_begin + q];
+    __syncthreads();
+    const float* xc = x + C.dof_off;
+    // stage x transposed: Xs[row][ij]; pad columns are zero (d grows per
+    // thread, so the cell index k only moves forward)
+    {
+        int k = 0;
+        for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
+            while (d >= cbeg[k + 1]) ++k;
+            const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
+            const int l = d - cbeg[k];
+            Xs[(crow[k] + l % nth) * nijp + l / nth] = xc[d];
+        }
+    }
+    if (nijp != nij)
+        for (int t = threadIdx.x; t < Nth * (nijp - nij); t += blockDim.x)
+            Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = 0.f;
+    if (fl.scat) {
+        const float* Wg = v.W + v.W_off[C.sig];
+        for (int t = threadIdx.x; t < Nth * Mp; t += blockDim.x) {
+            const int c = t / Mp, m = t % Mp;
+            WsT[t] = m < M ? __ldg(Wg + (int64_t)(it.row0 + m) * Nth + c) : 0.f;
+        }
+    }
+    __syncthreads();
+    if (fl.scat) {
+        const int tm = Mp / 4, tn = nijp / 4;
+        for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
+            const int m0 = 4 * (tile / tn), j0 = 4 * (tile % tn);
+            float acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll 4
+            for (int c = 0; c < Nth; ++c) {
+                const float4 w = *reinterpret_cast<const float4*>(WsT + c * Mp + m0);
+                const float4 xv = *reinterpret_cast<const float4*>(Xs + c * nijp + j0);
+                const float wv[4] = {w.x, w.y, w.z, w.w};
+                const float xa[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(wv[i], xa[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                *reinterpret_cast<float4*>(Ys + (m0 + i) * nijp + j0) =
+                    make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+        }
+    }
+    __syncthreads();
+    // inflow face fluxes of the item's elements into Fy (the W region is free)
+    if (fl.bc) {
+        for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = 0.f;
+        // T[jj][r] of every coupling, flattened over (coupling, jj, r); t
+        // grows per thread, so the coupling index only moves forward
+        {
+            int c = 0;
+            for (int t = threadIdx.x; t < it.ttot; t += blockDim.x) {
+                while (t >= sc[c].toff + sc[c].m1 * sc[c].nth) ++c;
+                const TileCpl& en = sc[c];
+                const int q = t - en.toff, jj = q / en.nth, r = q % en.nth;
+                const float* Et = v.mort + en.et;
+                const float* xl = x + en.base + (int64_t)jj * en.stride;
+                float acc = 0.f;
+                for (int a = 0; a < en.nt1; ++a) acc = fmaf(Et[a * en.nth + r], xl[a], acc);
+                Tb[t] = acc;
+            }
+        }
+        __syncthreads();
+        {
+            int c = 0;
+            for (int t = threadIdx.x; t < it.ctot; t += blockDim.x) {
+                while (t >= sc[c].coff + sc[c].n0 * sc[c].nth) ++c;
+                const TileCpl& en = sc[c];
+                const int q = (t - en.coff) / en.nth, r = (t - en.coff) % en.nth;
+                const float* Es = v.mort + en.es;
+                float acc = 0.f;
+                for (int jj = 0; jj < en.m1; ++jj) acc = fmaf(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], acc);
+                const int F = en.face;
+                const int i = (F == 0) ? C.nx - 1 : (F == 2 ? 0 : q);
+                const int j = (F == 1) ? C.ny - 1 : (F == 3 ? 0 : q);
+                atomicAdd(&Fy[(en.rowloc + r) * nijp + i * C.ny + j], en.dc * acc);
+            }
+        }
+        __syncthreads();
+    }
+    const float dxdy8 = v.colc[ci];
+    const float* Gx = v.G + gofs(C.nx);
+    const float* Gy = v.G + gofs(C.ny);
+    float* yc = y + C.dof_off;
+    const int d0 = cbeg[it.cell_begin], d1 = cbeg[it.cell_end];
+    int k = it.cell_begin;
+    for (int d = d0 + threadIdx.x; d < d1; d += blockDim.x) {
+        while (d >= cbeg[k + 1]) ++k;
+        const int e = C.elem_begin + k;
+        const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
+        const int l = d - cbeg[k];
+        const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
+        const ElemDev E = v.elems[e];
+        if (fl.mask_rows && bdry_node(E.flags >> 4, i, j, C.nx, C.ny)) {
+            yc[d] = 0.f;
+            continue;
+        }
+        const int R = crow[k] + r;
+        const float* A = v.ang + E.ang;
+        const float xself = Xs[R * nijp + ij];
+        const int node = C.node_off + ij;
+        const float mterm = v.econst[4 * e] * A[r] * v.kw[node];
+        float acc = 0.f;
+        if (fl.scat) acc = -dxdy8 * v.sw[node] * Ys[(R - it.row0) * nijp + ij];
+        if (fl.mass) acc += mterm * xself;
+        if (fl.ic) {
+            const float* xr = Xs + R * nijp;
+            float t1 = 0.f, t2 = 0.f;
+            const float* gy = Gy + j * C.ny;
+            for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
+            const float* gx = Gx + i * C.nx;
+            for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * xr[ii * C.ny + j];
+            const float ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
+                             v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
+            acc += fl.ic_sign * ic;
+        }
+        if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
+            acc += Fy[(R - it.row0) * nijp + ij];
+            // outflow faces: the diagonal term (rt/boundary_convection_matrix.py:276-346)
+            for (int F = 0; F < 4; ++F) {
+                if (!(E.flags & (1 << F))) continue;
+                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                (F == 3 && j == 0);
+                if (!on) continue;
+                const float dc = (F % 2 == 0) ? v.econst[4 * e + 2] : v.econst[4 * e + 1];
+                const float w = (F % 2 == 0) ? v.lglw[C.ny * kMaxNodes + j] : v.lglw[C.nx * kMaxNodes + i];
+                acc += dc * w * A[r] * A[(3 + F) * nth + r] * xself;
+            }
+        }
+        yc[d] = acc;
     }
 }
 
@@ -379,8 +589,24 @@ struct ApplyPlan {
     ApplyGroup g[2];            // 0: input and W staged; 1: input staged, W read through L2
     int32_t* d_slow = nullptr;
     int nslow = 0;
+    TileItem* d_tiles = nullptr;   // FP32: tiled items
+    TileCpl* d_tile_cpl = nullptr; // their coupling entries
+    int ntiles = 0;
+    size_t tile_smem = 0;
     std::vector<void*> allocs;
 };
+
+// Tiled items of the FP32 path: consecutive cells of a column, at most
+// kTileRows angular rows and kTileOut outputs per item, when the column's
+// input, the item's W rows and its products fit in shared memory.
+constexpr int kTileRows = 64;
+constexpr int kTileOut = 2048;
+
+static size_t tile_smem_bytes(int nth_col, int nij, int wcap, int M, int ncell) {
+    const int nijp = (nij + 3) & ~3, Mp = (M + 3) & ~3;
+    return sizeof(float) * ((size_t)nth_col * nijp + (size_t)wcap + (size_t)Mp * nijp) + sizeof(int) * (2 * ncell + 2) +
+           16;
+}
 
 template <typename T>
 static ApplyPlan* make_plan(const rtg_handle* h) {
@@ -388,11 +614,87 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
     constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
     std::vector<std::pair<int64_t, int4>> items[2];
+    std::vector<std::pair<int64_t, TileItem>> tiles;
+    std::vector<std::vector<TileCpl>> tile_cpl;   // coupling entries per tiled item
     std::vector<int32_t> slow;
     size_t need[2] = {0, 0};
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
         const ColDev& C = t.cols[ci];
         const int ncell = C.elem_end - C.elem_begin;
+        const int nij = C.nx * C.ny;
+        if (!parity && ncell <= kMaxCellsStaged) {
+            // split the column into items of whole cells
+            std::vector<TileItem> its;
+            bool fits = true;
+            int k = 0;
+            std::vector<std::vector<TileCpl>> ents;
+            std::vector<size_t> bytes;
+            while (k < ncell && fits) {
+                TileItem ti{ci, k, k, t.elems[C.elem_begin + k].row, 0, 0, 0, 0, 0, 0};
+                int M = 0, ncp = 0;
+                while (k < ncell) {
+                    const ElemDev& E = t.elems[C.elem_begin + k];
+                    const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
+                    if (M > 0 && (M + nth > kTileRows || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl)) break;
+                    M += nth;
+                    ncp += nc;
+                    ++k;
+                }
+                ti.cell_end = k;
+                if (ncp > kMaxItemCpl) fits = false;
+                std::vector<TileCpl> en;
+                int tsz = 0, csz = 0;
+                for (int q = ti.cell_begin; q < ti.cell_end; ++q) {
+                    const ElemDev& E = t.elems[C.elem_begin + q];
+                    for (int kk = E.cpl_begin; kk < E.cpl_end; ++kk) {
+                        const CplGeo& g = t.cgeo[kk];
+                        const CplDev& cp = t.cpls[kk];
+                        TileCpl tc{};
+                        tc.base = g.base;
+                        tc.rowloc = E.row - ti.row0;
+                        tc.nth = E.nth;
+                        tc.toff = tsz;
+                        tc.coff = csz;
+                        tc.m1 = g.m1;
+                        tc.nt1 = g.nth1;
+                        tc.face = cp.face;
+                        tc.n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+                        tc.stride = g.stride;
+                        tc.es = cp.es;
+                        tc.et = cp.et;
+                        tc.dc = (float)t.cplc[kk];
+                        en.push_back(tc);
+                        tsz += g.m1 * E.nth;
+                        csz += tc.n0 * E.nth;
+                    }
+                }
+                ti.ttot = tsz;
+                ti.ctot = csz;
+                const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
+                // Fy and Ys are read and written as float4: keep every region
+                // a multiple of 4 floats from the 16-byte-aligned base
+                ti.tsz = (tsz + 3) & ~3;
+                ti.wcap = std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
+                if ((ti.wcap & 3) || (ti.tsz & 3) || (nijp & 3))
+                    throw RtgError{RTG_ERR_ARG, "tiled apply: unaligned shared-memory region"};
+                const size_t b = tile_smem_bytes(C.nth_col, nij, ti.wcap, M, ncell);
+                if (b > kSmemBudget) fits = false;
+                bytes.push_back(b);
+                ents.push_back(std::move(en));
+                its.push_back(ti);
+            }
+            if (fits) {
+                for (size_t q = 0; q < its.size(); ++q) {
+                    const TileItem& ti = its[q];
+                    int M = 0;
+                    for (int r = ti.cell_begin; r < ti.cell_end; ++r) M += t.elems[C.elem_begin + r].nth;
+                    p->tile_smem = std::max(p->tile_smem, bytes[q]);
+                    tiles.push_back({(int64_t)M * nij * (C.nth_col + C.nx + C.ny) + C.ndof, ti});
+                    tile_cpl.push_back(std::move(ents[q]));
+                }
+                continue;
+            }
+        }
         const size_t sx = sizeof(T) * (size_t)C.ndof + sizeof(int) * (2 * ncell + 2) + 16;
         const size_t sw = (sizeof(T) + (parity ? sizeof(float) : 0)) * (size_t)C.nth_col * (C.nth_col | 1);
         if (sx > kSmemBudget || ncell > kMaxCellsStaged) {
@@ -427,6 +729,21 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
     }
     p->nslow = (int)slow.size();
     p->d_slow = (int32_t*)up(slow.data(), sizeof(int32_t) * slow.size());
+    std::vector<int> perm(tiles.size());
+    for (size_t q = 0; q < perm.size(); ++q) perm[q] = (int)q;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return tiles[a].first > tiles[b].first; });
+    std::vector<TileItem> tv;
+    std::vector<TileCpl> ent;
+    for (int q : perm) {
+        TileItem ti = tiles[q].second;
+        ti.cpl_begin = (int)ent.size();
+        ent.insert(ent.end(), tile_cpl[q].begin(), tile_cpl[q].end());
+        ti.cpl_end = (int)ent.size();
+        tv.push_back(ti);
+    }
+    p->ntiles = (int)tv.size();
+    p->d_tiles = (TileItem*)up(tv.data(), sizeof(TileItem) * tv.size());
+    p->d_tile_cpl = (TileCpl*)up(ent.data(), sizeof(TileCpl) * ent.size());
     return p;
 }
 
@@ -451,6 +768,14 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
         if (mx > 48 * 1024)
             RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)mx));
+        if (!f64 && plan->tile_smem > 48 * 1024)
+            RTG_CUDA(cudaFuncSetAttribute(apply_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)plan->tile_smem));
+    }
+    if constexpr (!f64) {
+        if (plan->ntiles)
+            apply_tiled_kernel<<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
+                h->v32, flags, plan->d_tiles, plan->d_tile_cpl, (const float*)x, (float*)y);
     }
     for (int grp = 0; grp < 2; ++grp) {
         const ApplyGroup& G = plan->g[grp];
