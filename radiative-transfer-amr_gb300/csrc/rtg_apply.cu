@@ -12,6 +12,8 @@
 // from global memory.
 #include <algorithm>
 #include <cstdio>
+#include <map>
+#include <tuple>
 
 #include "rtg_internal.h"
 
@@ -585,6 +587,19 @@ struct ApplyGroup {
     int stage_w = 0;
 };
 
+constexpr int kTileRows = 64;       // default row cap (before tuning)
+constexpr int kTileOut = 2048;
+constexpr int kTuneCaps[] = {16, 32, 64, 128};
+constexpr int kNumTuneCaps = 4;
+
+// Tuning record of one degree class: nx, ny, the column's angular nodes
+// rounded up to a power of two, the chosen row cap, and the measured time (ns)
+// of the class's items with each candidate cap (-1: not run).
+struct TuneRecord {
+    int nx, ny, nthb, cap;
+    int ns[kNumTuneCaps];
+};
+
 struct ApplyPlan {
     ApplyGroup g[2];            // 0: input and W staged; 1: input staged, W read through L2
     int32_t* d_slow = nullptr;
@@ -593,14 +608,14 @@ struct ApplyPlan {
     TileCpl* d_tile_cpl = nullptr; // their coupling entries
     int ntiles = 0;
     size_t tile_smem = 0;
+    std::vector<TuneRecord> tuning;
     std::vector<void*> allocs;
 };
 
 // Tiled items of the FP32 path: consecutive cells of a column, at most
 // kTileRows angular rows and kTileOut outputs per item, when the column's
 // input, the item's W rows and its products fit in shared memory.
-constexpr int kTileRows = 64;
-constexpr int kTileOut = 2048;
+
 
 static size_t tile_smem_bytes(int nth_col, int nij, int wcap, int M, int ncell) {
     const int nijp = (nij + 3) & ~3, Mp = (M + 3) & ~3;
@@ -608,8 +623,11 @@ static size_t tile_smem_bytes(int nth_col, int nij, int wcap, int M, int ncell) 
            16;
 }
 
+// cap: per column, the largest number of angular rows of a tiled item (FP32);
+// include: per column, whether the plan covers it (null: every column).
 template <typename T>
-static ApplyPlan* make_plan(const rtg_handle* h) {
+static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = nullptr,
+                            const std::vector<char>* include = nullptr) {
     const HostTables& t = h->host;
     constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
@@ -619,9 +637,11 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
     std::vector<int32_t> slow;
     size_t need[2] = {0, 0};
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
+        if (include && !(*include)[ci]) continue;
         const ColDev& C = t.cols[ci];
         const int ncell = C.elem_end - C.elem_begin;
         const int nij = C.nx * C.ny;
+        const int rows_cap = cap ? (*cap)[ci] : kTileRows;
         if (!parity && ncell <= kMaxCellsStaged) {
             // split the column into items of whole cells
             std::vector<TileItem> its;
@@ -635,7 +655,7 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
                 while (k < ncell) {
                     const ElemDev& E = t.elems[C.elem_begin + k];
                     const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
-                    if (M > 0 && (M + nth > kTileRows || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl)) break;
+                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl)) break;
                     M += nth;
                     ncp += nc;
                     ++k;
@@ -747,12 +767,179 @@ static ApplyPlan* make_plan(const rtg_handle* h) {
     return p;
 }
 
-void free_apply_plans(rtg_handle* h) {
-    for (ApplyPlan* p : {h->plan64, h->plan32}) {
-        if (!p) continue;
-        for (void* d : p->allocs) cudaFree(d);
-        delete p;
+static void free_plan(ApplyPlan* p) {
+    if (!p) return;
+    for (void* d : p->allocs) cudaFree(d);
+    delete p;
+}
+
+template <typename T>
+static void set_plan_attributes(const ApplyPlan* p) {
+    constexpr bool f64 = sizeof(T) == 8;
+    const size_t mx = std::max(p->g[0].smem, p->g[1].smem);
+    if (mx > 48 * 1024)
+        RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)mx));
+    if (!f64 && p->tile_smem > 48 * 1024)
+        RTG_CUDA(cudaFuncSetAttribute(apply_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)p->tile_smem));
+}
+
+template <typename T>
+static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<float>& v32, uint32_t flags, const T* x,
+                     T* y, cudaStream_t s) {
+    constexpr bool f64 = sizeof(T) == 8;
+    if constexpr (!f64) {
+        if (plan->ntiles)
+            apply_tiled_kernel<<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
+                v32, flags, plan->d_tiles, plan->d_tile_cpl, (const float*)x, (float*)y);
     }
+    for (int grp = 0; grp < 2; ++grp) {
+        const ApplyGroup& G = plan->g[grp];
+        if (G.nitems)
+            apply_col_kernel<T, T, f64><<<G.nitems, kApplyThreads, G.smem, s>>>(v, v32.W, v32.mort, flags,
+                                                                              G.d_items, G.stage_w, x, y);
+    }
+    if (plan->nslow)
+        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y);
+    RTG_CUDA(cudaGetLastError());
+}
+
+// Autotuner of the FP32 path: for every degree class of columns, time the
+// class's items with each candidate row cap (one warm-up, best of three
+// launches, CUDA events) and keep the fastest; then build the plan with the
+// chosen cap per column.
+static ApplyPlan* tune_plan32(rtg_handle* h, cudaStream_t s) {
+    const HostTables& t = h->host;
+    const int nc = (int)t.cols.size();
+    auto pow2 = [](int n) {
+        int b = 1;
+        while (b < n) b <<= 1;
+        return b;
+    };
+    std::map<std::tuple<int, int, int>, std::vector<int>> classes;
+    for (int ci = 0; ci < nc; ++ci) {
+        const ColDev& C = t.cols[ci];
+        classes[std::make_tuple(C.nx, C.ny, pow2(C.nth_col))].push_back(ci);
+    }
+    float *x = nullptr, *y = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<int> cap(nc, kTileRows);
+    std::vector<TuneRecord> recs;
+    try {
+        RTG_CUDA(cudaMalloc(&x, sizeof(float) * std::max<int64_t>(t.ndof, 1)));
+        RTG_CUDA(cudaMalloc(&y, sizeof(float) * std::max<int64_t>(t.ndof, 1)));
+        RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * t.ndof, s));
+        RTG_CUDA(cudaEventCreate(&e0));
+        RTG_CUDA(cudaEventCreate(&e1));
+        const uint32_t flags = RTG_SYSTEM | RTG_MASK_ROWS;
+        for (const auto& kv : classes) {
+            std::vector<char> inc(nc, 0);
+            for (int ci : kv.second) inc[ci] = 1;
+            TuneRecord r{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first), kTileRows, {}};
+            float best = 1e30f;
+            for (int q = 0; q < kNumTuneCaps; ++q) {
+                r.ns[q] = -1;
+                std::vector<int> cq(nc, kTuneCaps[q]);
+                ApplyPlan* p = make_plan<float>(h, &cq, &inc);
+                try {
+                    set_plan_attributes<float>(p);
+                    run_plan<float>(p, h->v32, h->v32, flags, x, y, s);
+                    float tbest = 1e30f;
+                    for (int rep = 0; rep < 3; ++rep) {
+                        RTG_CUDA(cudaEventRecord(e0, s));
+                        run_plan<float>(p, h->v32, h->v32, flags, x, y, s);
+                        RTG_CUDA(cudaEventRecord(e1, s));
+                        RTG_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0.f;
+                        RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                        tbest = std::min(tbest, ms);
+                    }
+                    r.ns[q] = (int)(tbest * 1e6f);
+                    // a larger cap must win by 3% to displace a smaller one
+                    if (tbest < best * 0.97f) {
+                        best = tbest;
+                        r.cap = kTuneCaps[q];
+                    }
+                } catch (...) {
+                    free_plan(p);
+                    throw;
+                }
+                free_plan(p);
+            }
+            for (int ci : kv.second) cap[ci] = r.cap;
+            recs.push_back(r);
+        }
+    } catch (...) {
+        if (x) cudaFree(x);
+        if (y) cudaFree(y);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        throw;
+    }
+    // a class timed alone sees an idle GPU: keep the tuned plan only if the
+    // whole apply is faster with it than with the default item size
+    ApplyPlan* tuned = make_plan<float>(h, &cap, nullptr);
+    ApplyPlan* dflt = nullptr;
+    try {
+        dflt = make_plan<float>(h, nullptr, nullptr);
+        float tt = 1e30f, td = 1e30f;
+        for (ApplyPlan* p : {tuned, dflt}) {
+            set_plan_attributes<float>(p);
+            run_plan<float>(p, h->v32, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+            for (int rep = 0; rep < 3; ++rep) {
+                RTG_CUDA(cudaEventRecord(e0, s));
+                run_plan<float>(p, h->v32, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+                RTG_CUDA(cudaEventRecord(e1, s));
+                RTG_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                (p == tuned ? tt : td) = std::min(p == tuned ? tt : td, ms);
+            }
+        }
+        if (td < tt) {
+            std::swap(tuned, dflt);
+            for (TuneRecord& r : recs) r.cap = -r.cap;   // negative: class choice not used
+        }
+    } catch (...) {
+        free_plan(tuned);
+        free_plan(dflt);
+        cudaFree(x);
+        cudaFree(y);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    free_plan(dflt);
+    cudaFree(x);
+    cudaFree(y);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tuned->tuning = std::move(recs);
+    return tuned;
+}
+
+int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s) {
+    if (!h->plan32) {
+        h->plan32 = tune_plan32(h, s);
+        set_plan_attributes<float>(h->plan32);
+    }
+    const auto& rec = h->plan32->tuning;
+    const int n = (int)rec.size();
+    for (int i = 0; i < std::min(n, cap_rows); ++i) {
+        int32_t* o = out + (size_t)i * (4 + kNumTuneCaps);
+        o[0] = rec[i].nx;
+        o[1] = rec[i].ny;
+        o[2] = rec[i].nthb;
+        o[3] = rec[i].cap;
+        for (int q = 0; q < kNumTuneCaps; ++q) o[4 + q] = rec[i].ns[q];
+    }
+    return n;
+}
+
+void free_apply_plans(rtg_handle* h) {
+    free_plan(h->plan64);
+    free_plan(h->plan32);
     h->plan64 = h->plan32 = nullptr;
 }
 
@@ -763,29 +950,10 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
     constexpr bool f64 = sizeof(T) == 8;
     ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
     if (!plan) {
-        plan = make_plan<T>(h);
-        size_t mx = std::max(plan->g[0].smem, plan->g[1].smem);
-        if (mx > 48 * 1024)
-            RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)mx));
-        if (!f64 && plan->tile_smem > 48 * 1024)
-            RTG_CUDA(cudaFuncSetAttribute(apply_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)plan->tile_smem));
+        plan = f64 ? make_plan<T>(h) : tune_plan32(h, s);
+        set_plan_attributes<T>(plan);
     }
-    if constexpr (!f64) {
-        if (plan->ntiles)
-            apply_tiled_kernel<<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
-                h->v32, flags, plan->d_tiles, plan->d_tile_cpl, (const float*)x, (float*)y);
-    }
-    for (int grp = 0; grp < 2; ++grp) {
-        const ApplyGroup& G = plan->g[grp];
-        if (G.nitems)
-            apply_col_kernel<T, T, f64><<<G.nitems, kApplyThreads, G.smem, s>>>(v, h->v32.W, h->v32.mort, flags,
-                                                                              G.d_items, G.stage_w, x, y);
-    }
-    if (plan->nslow)
-        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, h->v32.mort, flags, plan->d_slow, x, y);
-    RTG_CUDA(cudaGetLastError());
+    run_plan<T>(plan, v, h->v32, flags, x, y, s);
 }
 
 template void launch_apply<double>(const rtg_handle*, const OpView<double>&, uint32_t, const double*,

@@ -355,6 +355,13 @@ int rtg_sweep_trace(rtg_handle* h, int prec, const void* r, void* z, uint64_t* t
     });
 }
 
+int rtg_apply_tuning(rtg_handle* h, int32_t* table, int cap_rows, int* nclasses, void* stream) {
+    return guard("rtg_apply_tuning", [&] {
+        if (!h || !nclasses || (cap_rows > 0 && !table)) throw RtgError{RTG_ERR_ARG, "null argument"};
+        *nclasses = apply_tuning(h, table, cap_rows, (cudaStream_t)stream);
+    });
+}
+
 int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream) {
     return guard("rtg_interior_mask", [&] {
         if (!h || !mask) throw RtgError{RTG_ERR_ARG, "null argument"};

@@ -162,6 +162,9 @@ void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* 
                         cudaStream_t s);
 void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s);
 void free_apply_plans(rtg_handle* h);
+// FP32 apply autotuning table (tunes on first use): rows of [nx, ny, nth_b,
+// cap, ns per candidate cap]; returns the number of degree classes
+int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s);
 
 // Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
 template <typename T>
