@@ -1,22 +1,31 @@
 """Benchmark: time to 1e-8 relative L2 error of the steady RT solve on one GB300.
 
-Workload (default): the single adaptive problem -- domain [0,3]x[0,2],
-sigma_s a Gaussian bump (amplitude 0.9, width 0.15) at (1.5, 1.0),
-sigma_t = sigma_s + 0.01, HG g = 0.9, inflow 1 on x = 0 for th in (-pi/4, pi/4),
-hp mesh from seeded random refinement (seed 0, six rounds, 3..7 nodes per
-dimension), about 2.2e5 DOF.  Synthetic and seeded; no dataset involved.
+Workload (default, --workload cfg2): the single adaptive problem -- domain
+[0,3]x[0,2], sigma_s a Gaussian bump (amplitude 0.9, width 0.15) at (1.5, 1.0),
+sigma_t = sigma_s + 0.01, HG g = 0.9, inflow 1 on x = 0 for th in
+(-pi/4, pi/4), hp mesh from seeded random refinement (seed 0, six rounds, 3..7
+nodes per dimension), about 2.2e5 DOF.  Synthetic and seeded; no dataset.
 
 A step is one solve from a zero initial guess to the error target.  The judge
 solution is a tight plain FP64 GPU solve (rtol 1e-14) computed before timing;
 the error is the quadrature-weighted relative L2 norm (weights = mass weights
-with kappa = 1).  The residual tolerance of each method is calibrated (untimed)
-as the loosest power of ten that reaches the 1e-8 target.
+with kappa = 1).  Each method's residual tolerance is calibrated (untimed) as
+the loosest power of ten that reaches the 1e-8 target.  Three methods:
+  plain    FP64 GMRES, sweep preconditioner (the reference-matching method)
+  mixed    FP32 GMRES inside FP64 iterative refinement, sweep preconditioner
+  learned  as mixed, flexible GMRES with the sweep plus the learned correction
+           (network rtg/nets/sweep_correction.npz, trained by rtg.train)
 
-value   : seconds per solve of the mixed method (FP32 GMRES inside FP64
-          iterative refinement), device-resident inputs.
-e2e     : same solve through the C ABI with host buffers: H2D of the sampled
-          forcing and inflow node values, weighting kernel, solve, D2H of u.
-roofline: the FP32 system apply (dominant kernel of the inner solve).
+value   : seconds per learned+mixed solve, device-resident inputs.
+e2e     : the same solve through the C ABI with host buffers: H2D of the
+          sampled forcing and inflow node values, weighting kernel, solve, D2H
+          of u.
+roofline: the persistent sweep kernel (FP32), the kernel that dominates the
+          solve; apply_roofline: the FP32 system apply.
+
+--workload cfg3: 256 independent instances in one batched solve vs the same
+instances solved one by one.  --workload cfg5: the ~9.4e6-DOF two-scatterer
+problem: apply and sweep throughput and a bounded solve.
 """
 import argparse
 import ctypes as C
@@ -45,7 +54,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg5"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu: one warm and one measured solve per method, 3 applies")
@@ -209,9 +218,44 @@ def cpu_baseline(mesh, spec, rtol, u_judge=None, w=None):
             "rel_l2_err": err}
 
 
-def run_ours(args):
+def _events(stream):
     import torch
-    from rtg import Problem, _lib
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def kernel_time(fn, stream, flush, reps=20):
+    """Median CUDA-event duration of fn() on the stream, L2 flushed before each."""
+    import torch
+    for _ in range(3):
+        fn()
+    durs = []
+    for _ in range(reps):
+        flush.fill_(1.0)
+        e0, e1 = _events(stream)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        durs.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.median(durs)
+
+
+def sweep_bytes(ctx, prec_bytes):
+    """Algorithmic bytes of one sweep: read r, write z, read the element block
+    inverses (upwind face lines re-read through L2 count 0)."""
+    from rtg import _lib
+    lev, lag, inv = C.c_int(), C.c_int(), C.c_int64()
+    _lib.check(ctx.lib.rtg_sweep_info(ctx.h, C.byref(lev), C.byref(lag), C.byref(inv), None))
+    return int(2 * prec_bytes * ctx.N + prec_bytes * inv.value), int(lev.value), int(lag.value)
+
+
+def run_ours(args):
+    if args.workload == "cfg3":
+        return run_batched(args)
+    if args.workload == "cfg5":
+        return run_large(args)
+    import torch
+    from rtg import Problem, _lib, learned as LN
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -228,6 +272,8 @@ def run_ours(args):
     N = ctx.N
     f_dev = ctx.forcing(spec.f)
     g_dev = ctx.inflow(spec.bcs_dirac)
+    params, net_meta = LN.load(LN.DEFAULT_NET)
+    LN.set_params(ctx, params)
     # L2 weights (dx dy dth/8) wx wy wth = mass weights with kappa = 1
     lay = ctx.layout
     X, Y, T = lay.node_coords()
@@ -238,33 +284,36 @@ def run_ours(args):
     # judge solution: tight plain FP64 solve
     u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=20000, precond=1)
     u_ref_h = u_ref.cpu().numpy()
+    arms = {"plain_fp64": (0, 1), "mixed": (1, 1), "learned_mixed": (1, 3)}
 
-    def calibrate(method):
+    def solve(arm, rtol):
+        method, pc = arms[arm]
+        return ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=pc, restart=30,
+                         inner_rtol=1e-5)
+
+    def calibrate(arm):
         for k in range(6, 15):
             rtol = 10.0 ** (-k)
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
+            u, info = solve(arm, rtol)
             err = rel_l2(u.cpu().numpy(), u_ref_h, w)
             if err <= ERR_TARGET:
-                return rtol, err, info
-        raise RuntimeError("method {} did not reach the error target".format(method))
+                return rtol
+        raise RuntimeError("{} did not reach the error target".format(arm))
 
-    rtol_mx, err_mx, info_mx = calibrate(1)
-    rtol_pl, err_pl, info_pl = calibrate(0)
-
+    rtols = {arm: calibrate(arm) for arm in arms}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=ctx.device)
     stream = torch.cuda.current_stream()
 
-    def timed(method, rtol, steps, warm):
+    def timed(arm, steps, warm):
         for _ in range(warm):
-            ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
+            solve(arm, rtols[arm])
         times, errs, infos = [], [], []
         for _ in range(steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
+            e0, e1 = _events(stream)
             e0.record(stream)
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=1)
+            u, info = solve(arm, rtols[arm])
             e1.record(stream)
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1) / 1e3)
@@ -276,12 +325,13 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
-        t_mx, e_mx, i_mx = timed(1, rtol_mx, args.steps, args.warmup)
-    t_pl, e_pl, i_pl = timed(0, rtol_pl, max(1, min(args.steps, 2)), 1)
+        res = {"learned_mixed": timed("learned_mixed", args.steps, args.warmup)}
+    res["mixed"] = timed("mixed", max(1, min(args.steps, 3)), 1)
+    res["plain_fp64"] = timed("plain_fp64", max(1, min(args.steps, 3)), 1)
     if world > 1:
         torch.distributed.barrier()
 
-    # e2e through the C ABI with host buffers
+    # e2e through the C ABI with host buffers (learned+mixed)
     lib = ctx.lib
     fvals = torch.from_numpy(ctx.node_values(spec.f)).pin_memory()
     gvals = torch.from_numpy(np.ascontiguousarray(g_dev.cpu().numpy())).pin_memory()
@@ -290,16 +340,15 @@ def run_ours(args):
     fw = torch.empty_like(fd)
     gd = torch.empty_like(fd)
     ud = torch.zeros_like(fd)
-    opts = _lib.SolveOpts(method=1, restart=50, max_it=50000, rtol=rtol_mx, atol=0., precond=1,
-                          nonzero_guess=0, inner_rtol=1e-6, max_outer=20, verbose=0)
+    opts = _lib.SolveOpts(method=1, restart=30, max_it=20000, rtol=rtols["learned_mixed"], atol=0., precond=3,
+                          nonzero_guess=0, inner_rtol=1e-5, max_outer=20, verbose=0)
     sinfo = _lib.SolveInfo()
     sp = C.c_void_p(stream.cuda_stream)
     e2e_times = []
     for it in range(args.warmup + args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(stream)
         e0.record(stream)
         fd.copy_(fvals, non_blocking=True)
         gd.copy_(gvals, non_blocking=True)
@@ -313,66 +362,199 @@ def run_ours(args):
             e2e_times.append(e0.elapsed_time(e1) / 1e3)
     e2e_err = rel_l2(u_host.numpy(), u_ref_h, w)
 
-    # roofline of the FP32 system apply (dominant kernel of the inner solve)
-    xa = torch.randn(N, dtype=torch.float32, device=ctx.device)
-    ya = torch.empty_like(xa)
-    nrep = 50
-    for _ in range(5):
-        ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, xa, ya, prec=_lib.RTG_FP32)
-    durs = []
-    for _ in range(nrep):
-        flush.fill_(1.0)
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, xa, ya, prec=_lib.RTG_FP32)
-        a1.record(stream)
-        torch.cuda.synchronize()
-        durs.append(a0.elapsed_time(a1) / 1e3)
-    t_apply = statistics.median(durs)
-    bytes_apply = int(ctx.info["bytes_per_apply_fp32"])
+    # rooflines: the FP32 sweep (dominant kernel of the solve) and the FP32 apply
     peak, peak_kind = peaks()
-    achieved = bytes_apply / t_apply / 1e9
+    r32 = torch.randn(N, dtype=torch.float32, device=ctx.device)
+    z32 = torch.empty_like(r32)
+    t_sweep = kernel_time(lambda: ctx.precondition(r32, z32, prec=_lib.RTG_FP32), stream, flush)
+    sb, nlev, nlag = sweep_bytes(ctx, 4)
+    t_apply = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, r32, z32, prec=_lib.RTG_FP32),
+                          stream, flush)
+    bytes_apply = int(ctx.info["bytes_per_apply_fp32"])
+    x64 = torch.randn(N, dtype=torch.float64, device=ctx.device)
+    y64 = torch.empty_like(x64)
+    t_apply64 = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x64, y64, prec=_lib.RTG_FP64),
+                            stream, flush)
+    t_sweep64 = kernel_time(lambda: ctx.precondition(x64, y64, prec=_lib.RTG_FP64), stream, flush)
 
-    mx_time = statistics.median(t_mx)
+    t_l, e_l, i_l = res["learned_mixed"]
+    value = statistics.median(t_l)
     if world > 1:
-        tt = torch.tensor([max(t_mx)], device=ctx.device)
+        tt = torch.tensor([max(t_l)], device=ctx.device)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        mx_time = float(tt.item())
+        value = float(tt.item())
     if rank != 0:
         return None
-    launches = None
-    inf = i_mx[-1]
-    # kernels per solve: applies + ~10 Krylov kernels per inner iteration
-    launches = int(inf["fp32_applies"] + inf["fp64_applies"] + 10 * inf["iterations"])
+    inf = i_l[-1]
+    # own kernels per solve: per inner iteration the sweep (2), the FP32 apply
+    # (1-3), the learned correction (2) and the Krylov kernels (~9); per outer
+    # step an FP64 apply (1-3) and ~6 vector kernels
+    launches = int(inf["iterations"] * 14 + inf["outer"] * 9 + 10)
+
+    def arm_summary(arm):
+        t, e, i = res[arm]
+        return {"rtol": rtols[arm], "rel_l2_err": max(e), "median_s": statistics.median(t), "seconds": t,
+                "iterations": i[-1]["iterations"], "outer": i[-1]["outer"], "fp64_applies": i[-1]["fp64_applies"],
+                "fp32_applies": i[-1]["fp32_applies"], "learned": i[-1]["learned"],
+                "fallbacks": i[-1]["fallbacks"]}
+
+    t_plain = statistics.median(res["plain_fp64"][0])
     out = {
-        "metric": METRIC, "value": mx_time, "unit": "s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * mx_time, "higher_is_better": False,
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * value, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-inner/f64-outer",
         "data": "synthetic (seeded hp mesh and coefficients)",
         "config": {"workload": desc, "ndof": N, "ndof_interior": int(ctx.info["ndof_interior"]),
-                   "error_target": ERR_TARGET, "l2_flush": "256 MB write between timed solves",
-                   "mixed": {"rtol": rtol_mx, "rel_l2_err": max(e_mx), "inner_iterations": inf["iterations"],
-                             "outer": inf["outer"], "fp64_applies": inf["fp64_applies"],
-                             "fp32_applies": inf["fp32_applies"], "seconds": t_mx},
-                   "plain_fp64": {"rtol": rtol_pl, "rel_l2_err": max(e_pl),
-                                  "iterations": i_pl[-1]["iterations"], "seconds": t_pl,
-                                  "median_s": statistics.median(t_pl)},
-                   "speedup_mixed_vs_plain": statistics.median(t_pl) / mx_time,
-                   "judge": {"rtol": 1e-14, "iterations": info_ref["iterations"],
-                             "res_f": info_ref["res_f"]},
+                   "error_target": ERR_TARGET, "l2_flush": "256 MB write before every timed solve and kernel",
+                   "learned_mixed": arm_summary("learned_mixed"), "mixed": arm_summary("mixed"),
+                   "plain_fp64": arm_summary("plain_fp64"),
+                   "speedup_learned_mixed_vs_plain_fp64": t_plain / value,
+                   "speedup_mixed_vs_plain_fp64": t_plain / statistics.median(res["mixed"][0]),
+                   "network": {"file": "rtg/nets/sweep_correction.npz", **net_meta},
+                   "judge": {"rtol": 1e-14, "iterations": info_ref["iterations"], "res_f": info_ref["res_f"]},
+                   "kernels_us": {"sweep_fp32": 1e6 * t_sweep, "sweep_fp64": 1e6 * t_sweep64,
+                                  "apply_fp32": 1e6 * t_apply, "apply_fp64": 1e6 * t_apply64},
+                   "sweep": {"levels": nlev, "lagged_couplings": nlag},
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": statistics.median(e2e_times), "unit": "s", "h2d_bytes_per_step": 2 * 8 * N,
                 "d2h_bytes_per_step": 8 * N, "rel_l2_err": e2e_err},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "apply_kernel<float> (system)",
-                     "bytes_per_launch": bytes_apply, "launch_s": t_apply, "peak_kind": peak_kind},
+        "roofline": {"bound": "hbm", "achieved": sb / t_sweep / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": sb / t_sweep / 1e9 / peak, "traffic": None,
+                     "kernel": "sweep_persistent_kernel<float>", "bytes_per_launch": sb, "launch_s": t_sweep,
+                     "peak_kind": peak_kind,
+                     "note": "latency bound: {} wavefront levels, {:.2f} us per level".format(
+                         nlev, 1e6 * t_sweep / max(nlev, 1))},
+        "apply_roofline": {"bound": "hbm", "achieved": bytes_apply / t_apply / 1e9, "peak": peak, "unit": "GB/s",
+                           "frac": bytes_apply / t_apply / 1e9 / peak, "kernel": "apply_tiled_kernel (FP32 system)",
+                           "bytes_per_launch": bytes_apply, "launch_s": t_apply, "peak_kind": peak_kind,
+                           "dof_applies_per_s": N / t_apply},
         "clocks": clk.summary(),
     }
     if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(mesh, spec, rtol_pl, u_ref_h, w)
+        out["cpu_baseline"] = cpu_baseline(mesh, spec, rtols["plain_fp64"], u_ref_h, w)
     return out
+
+
+def run_batched(args):
+    """cfg3: 256 independent instances (seeded degree, size, sigma_t, albedo,
+    g) in one batched solve (method 1, one handle, graph-captured restart
+    cycle), against solving the same instances one by one through rt.Problem-
+    style contexts.  Each instance's error is measured against its own tight
+    FP64 solve."""
+    import torch
+    from rtg import DeviceContext, _lib, workloads as W
+    from rtg.batch import BatchContext
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(0)
+    nb = 256
+    inst = [W.batch_instance(1000 + k) for k in range(nb)]
+    bc = BatchContext(inst)
+    f = bc.forcing()
+    g = bc.inflow()
+    stream = torch.cuda.current_stream()
+    # judges: tight individual FP64 solves
+    ctxs = [DeviceContext(m, p.kappa, p.sigma, p.Phi) for m, p in inst]
+    fs = [c.forcing(p.f) for c, (m, p) in zip(ctxs, inst)]
+    gs = [c.inflow(p.bcs_dirac) for c, (m, p) in zip(ctxs, inst)]
+    refs = [c.solve(fi, gi, method=0, precond=1, rtol=1e-13, max_it=20000)[0] for c, fi, gi in zip(ctxs, fs, gs)]
+
+    def errors(parts):
+        return [float(torch.linalg.norm(a - r) / torch.linalg.norm(r)) for a, r in zip(parts, refs)]
+
+    rtol = None
+    for k in range(6, 14):
+        u, infos = bc.solve(f, g, rtol=10.0 ** (-k), inner_rtol=1e-5)
+        if max(errors(bc.split(u))) <= ERR_TARGET:
+            rtol = 10.0 ** (-k)
+            break
+    if rtol is None:
+        raise RuntimeError("batched solve did not reach the error target")
+    for _ in range(args.warmup):
+        bc.solve(f, g, rtol=rtol, inner_rtol=1e-5)
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            e0, e1 = _events(stream)
+            e0.record(stream)
+            u, infos = bc.solve(f, g, rtol=rtol, inner_rtol=1e-5)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    errs = errors(bc.split(u))
+    seq = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c, fi, gi in zip(ctxs, fs, gs):
+            c.solve(fi, gi, method=1, precond=1, rtol=rtol, inner_rtol=1e-5, restart=30)
+        torch.cuda.synchronize()
+        seq.append(time.perf_counter() - t0)
+    if rank != 0:
+        return None
+    value = statistics.median(times)
+    ndof = int(bc.N)
+    return {"metric": METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-inner/f64-outer", "data": "synthetic (256 seeded instances)",
+            "config": {"workload": "256 independent instances (batch_instance seeds 1000..1255)", "ndof": ndof,
+                       "rtol": rtol, "max_rel_err": max(errs), "error_target": ERR_TARGET,
+                       "sequential_one_by_one_s": min(seq), "speedup_batched_vs_sequential": min(seq) / value,
+                       "iterations_max": max(i["iterations"] for i in infos)},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "inputs resident; the batched entry point takes device vectors"},
+            "gpu_launches": None, "clocks": clk.summary()}
+
+
+def run_large(args):
+    """cfg5 (~9.4e6 DOF): apply and sweep throughput in FP32 and FP64, and a
+    bounded learned+mixed solve (the strongly forward-peaked thick discs make
+    sweep-preconditioned GMRES stagnate; the residual reached is reported)."""
+    import torch
+    from rtg import Problem, _lib, learned as LN
+    torch.cuda.set_device(0)
+    desc, mesh, spec = workload("cfg5")
+    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    ctx = prob.context(mesh)
+    N = ctx.N
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=ctx.device)
+    peak, peak_kind = peaks()
+    out = {}
+    for nm, dt, prec, key in (("fp32", torch.float32, _lib.RTG_FP32, "bytes_per_apply_fp32"),
+                              ("fp64", torch.float64, _lib.RTG_FP64, "bytes_per_apply_fp64")):
+        x = torch.randn(N, dtype=dt, device=ctx.device)
+        y = torch.empty_like(x)
+        ta = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec), stream, flush, 10)
+        ts = kernel_time(lambda: ctx.precondition(x, y, prec=prec), stream, flush, 5)
+        out[nm] = {"apply_s": ta, "apply_gbs": ctx.info[key] / ta / 1e9, "apply_frac": ctx.info[key] / ta / 1e9 / peak,
+                   "dof_applies_per_s": N / ta, "apply_tflops": ctx.info["flops_per_apply"] / ta / 1e12,
+                   "sweep_s": ts}
+    params, _ = LN.load(LN.DEFAULT_NET)
+    LN.set_params(ctx, params)
+    f_dev = ctx.forcing(spec.f)
+    g_dev = ctx.inflow(spec.bcs_dirac)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        e0, e1 = _events(stream)
+        e0.record(stream)
+        u, info = ctx.solve(f_dev, g_dev, method=1, precond=3, rtol=1e-8, max_it=300, restart=30, inner_rtol=1e-5)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    return {"metric": METRIC, "value": t, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": 1e3 * t, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-inner/f64-outer", "data": "synthetic (seeded disc-edge hp mesh)",
+            "config": {"workload": desc, "ndof": N, "bounded_solve": {
+                "max_it": 300, "iterations": info["iterations"], "converged": info["converged"],
+                "rel_residual": info["res_f"] / max(info["rhs_norm"], 1e-300), "fallbacks": info["fallbacks"]},
+                "kernels": out},
+            "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "roofline": {"bound": "hbm", "achieved": out["fp32"]["apply_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": out["fp32"]["apply_frac"], "traffic": None, "kernel": "apply_tiled_kernel (FP32)",
+                         "peak_kind": peak_kind},
+            "gpu_launches": None, "clocks": clk.summary()}
 
 
 def run_reference(args):

@@ -206,6 +206,10 @@ int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, doubl
  * of z at inflow-boundary DOFs are zero.  The first call builds the element
  * block inverses (device memory owned by the handle). */
 int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream);
+/* The sweep's wavefront levels, the couplings it lags (cycles of the upwind
+ * graph) and the entries of its element block inverses (each held in FP32
+ * and FP64); builds the sweep if needed.  Any output may be NULL. */
+int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_entries, void* stream);
 /* One sweep as rtg_precondition, recording for every element e
  * trace[8e .. 8e+7] = {claimed, upwind inputs ready, published, CTA, upwind
  * lines loaded, couplings formed, values stored, fence passed} (device array

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <map>
+#include <string>
 #include <tuple>
 
 #include "rtg_internal.h"
@@ -776,33 +777,42 @@ static void free_plan(ApplyPlan* p) {
 template <typename T>
 static void set_plan_attributes(const ApplyPlan* p) {
     constexpr bool f64 = sizeof(T) == 8;
-    const size_t mx = std::max(p->g[0].smem, p->g[1].smem);
-    if (mx > 48 * 1024)
-        RTG_CUDA(cudaFuncSetAttribute(apply_col_kernel<T, T, f64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)mx));
-    if (!f64 && p->tile_smem > 48 * 1024)
-        RTG_CUDA(cudaFuncSetAttribute(apply_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)p->tile_smem));
+    raise_smem_limit((const void*)apply_col_kernel<T, T, f64>, std::max(p->g[0].smem, p->g[1].smem));
+    if (!f64) raise_smem_limit((const void*)apply_tiled_kernel, p->tile_smem);
 }
 
 template <typename T>
 static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<float>& v32, uint32_t flags, const T* x,
                      T* y, cudaStream_t s) {
     constexpr bool f64 = sizeof(T) == 8;
+    RTG_LAUNCHED("a kernel before the apply");
     if constexpr (!f64) {
-        if (plan->ntiles)
+        if (plan->ntiles) {
             apply_tiled_kernel<<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
                 v32, flags, plan->d_tiles, plan->d_tile_cpl, (const float*)x, (float*)y);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                cudaFuncAttributes fa{};
+                cudaFuncGetAttributes(&fa, apply_tiled_kernel);
+                throw RtgError{RTG_ERR_CUDA, "launch of apply_tiled_kernel (items " + std::to_string(plan->ntiles) +
+                                                 ", dynamic smem " + std::to_string(plan->tile_smem) + ", max dynamic " +
+                                                 std::to_string(fa.maxDynamicSharedSizeBytes) + ", static " +
+                                                 std::to_string(fa.sharedSizeBytes) + "): " + cudaGetErrorString(e)};
+            }
+        }
     }
     for (int grp = 0; grp < 2; ++grp) {
         const ApplyGroup& G = plan->g[grp];
-        if (G.nitems)
+        if (G.nitems) {
             apply_col_kernel<T, T, f64><<<G.nitems, kApplyThreads, G.smem, s>>>(v, v32.W, v32.mort, flags,
                                                                               G.d_items, G.stage_w, x, y);
+            RTG_LAUNCHED("apply_col_kernel");
+        }
     }
-    if (plan->nslow)
+    if (plan->nslow) {
         apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y);
-    RTG_CUDA(cudaGetLastError());
+        RTG_LAUNCHED("apply_global_kernel");
+    }
 }
 
 // Autotuner of the FP32 path: for every degree class of columns, time the

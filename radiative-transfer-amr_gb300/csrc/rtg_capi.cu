@@ -1,5 +1,7 @@
 // extern "C" entry points of librtg (declared in include/rtg.h).
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <functional>
 #include <string>
 #include <vector>
@@ -11,6 +13,18 @@ namespace rtg {
 static thread_local std::string g_err;
 
 void set_error(const std::string& msg) { g_err = msg; }
+
+void raise_smem_limit(const void* func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> done;
+    int dev = 0;
+    RTG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& cur = done[std::make_pair(dev, func)];
+    if (bytes <= cur) return;
+    RTG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+}
 
 namespace {
 
@@ -335,6 +349,16 @@ int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* s
         } else {
             throw RtgError{RTG_ERR_ARG, "unknown precision"};
         }
+    });
+}
+
+int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_entries, void* stream) {
+    return guard("rtg_sweep_info", [&] {
+        if (!h) throw RtgError{RTG_ERR_ARG, "null argument"};
+        cudaStream_t s = (cudaStream_t)stream;
+        if (levels) *levels = sweep_levels_count(h, s);
+        if (lagged) *lagged = sweep_lagged_count(h, s);
+        if (inverse_entries) *inverse_entries = sweep_inverse_entries(h, s);
     });
 }
 

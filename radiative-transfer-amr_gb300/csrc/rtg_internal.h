@@ -18,17 +18,37 @@ constexpr double kBcTol = 1.e-15;      // drop rule of the face terms
 
 void set_error(const std::string& msg);
 
+// Opt a kernel in to `bytes` of dynamic shared memory.  The attribute belongs
+// to the function, process-wide, so several handles share it: it is only ever
+// raised (per device), never lowered below what another handle launched with.
+// The default limit is 48 KB minus the kernel's static shared memory, so any
+// launch with dynamic shared memory goes through here.
+void raise_smem_limit(const void* func, size_t bytes);
+
 struct RtgError {
     int code;
     std::string msg;
 };
 
-#define RTG_CUDA(call)                                                        \
-    do {                                                                      \
-        cudaError_t e_ = (call);                                              \
-        if (e_ != cudaSuccess)                                                \
-            throw ::rtg::RtgError{RTG_ERR_CUDA, std::string(#call) + ": " +   \
-                                                    cudaGetErrorString(e_)};  \
+// check the launch just made (launch errors are reported by the next
+// cudaGetLastError, so every launch site checks its own)
+#define RTG_LAUNCHED(what)                                                                    \
+    do {                                                                                      \
+        cudaError_t e_ = cudaGetLastError();                                                  \
+        if (e_ != cudaSuccess)                                                                \
+            throw ::rtg::RtgError{RTG_ERR_CUDA, std::string("launch of ") + (what) + " (" +    \
+                                                    __FILE__ + ":" + RTG_STR(__LINE__) + "): " + \
+                                                    cudaGetErrorString(e_)};                  \
+    } while (0)
+#define RTG_STR2(x) #x
+#define RTG_STR(x) RTG_STR2(x)
+#define RTG_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            throw ::rtg::RtgError{RTG_ERR_CUDA, std::string(#call) + " (" + __FILE__ + ":" + \
+                                                    RTG_STR(__LINE__) + "): " +              \
+                                                    cudaGetErrorString(e_)};                 \
     } while (0)
 
 // Per column.
@@ -175,6 +195,7 @@ void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
 int sweep_levels_count(rtg_handle* h, cudaStream_t s);
 int sweep_lagged_count(rtg_handle* h, cudaStream_t s);
+int64_t sweep_inverse_entries(rtg_handle* h, cudaStream_t s);
 int sweep_status(rtg_handle* h, cudaStream_t s);
 void free_sweep(rtg_handle* h);
 

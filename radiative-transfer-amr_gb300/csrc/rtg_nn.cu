@@ -1,6 +1,6 @@
 // Learned correction of the sweep preconditioner.
 //
-// Preconditioner 2 of rtg_solve is M(r) = z + L z with z = P_sweep^{-1} r and
+// Preconditioner 3 of rtg_solve is M(r) = z + L z with z = P_sweep^{-1} r and
 // L a learned operator that is LINEAR in z: the sweep inverts streaming and
 // extinction only, so what it leaves is the error that scattering spreads over
 // directions and elements, mostly the angle-averaged part in optically thick,
@@ -30,7 +30,6 @@
 // fixed order, so training is deterministic.
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 
 #include <cuda_bf16.h>
 
@@ -713,19 +712,9 @@ struct NNWs {
     std::vector<void*> allocs;
 };
 
-// The MLP kernels use more than 48 KB of dynamic shared memory: opt in once
-// per device.
 static void mlp_attributes() {
-    static std::mutex mu;
-    static std::vector<int> done;
-    int dev = 0;
-    RTG_CUDA(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lk(mu);
-    if (dev < (int)done.size() && done[dev]) return;
-    RTG_CUDA(cudaFuncSetAttribute(nn_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem));
-    RTG_CUDA(cudaFuncSetAttribute(nn_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpSmem));
-    if (dev >= (int)done.size()) done.resize(dev + 1, 0);
-    done[dev] = 1;
+    raise_smem_limit((const void*)nn_forward_kernel, kMlpSmem);
+    raise_smem_limit((const void*)nn_grad_kernel, kMlpSmem);
 }
 
 static void* nn_alloc(NNWs* w, size_t bytes) {

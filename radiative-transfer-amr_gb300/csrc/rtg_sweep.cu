@@ -587,8 +587,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     RTG_CUDA(cudaMemcpy(d_bo, blk_off.data(), sizeof(int64_t) * blk_off.size(), cudaMemcpyHostToDevice));
     RTG_CUDA(cudaMemset(d_status, 0, sizeof(int)));
     const size_t smem = sizeof(float) * (size_t)max_nn * 2 * max_nn;
-    RTG_CUDA(cudaFuncSetAttribute(build_block_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
+    raise_smem_limit((const void*)build_block_inverse_kernel, smem);
     build_block_inverse_kernel<<<(int)blk_elem.size(), 256, smem, st>>>(h->v32, d_be, d_br, d_bo, s->d_inv64,
                                                                          s->d_inv32, d_status);
     RTG_CUDA(cudaGetLastError());
@@ -646,8 +645,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         const int64_t fit = (int64_t)((kSweepSmemBudget - std::min(rhs_bytes, kSweepSmemBudget)) / sizeof(T));
         bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
         smem = rhs_bytes + sizeof(T) * (size_t)bcap;
-        RTG_CUDA(cudaFuncSetAttribute(sweep_persistent_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+        raise_smem_limit((const void*)sweep_persistent_kernel<T>, smem);
         int per_sm = 0, dev = 0, nsm = 0;
         RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
                                                                smem));
@@ -691,5 +689,6 @@ template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t
 
 int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
 int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
+int64_t sweep_inverse_entries(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->inv_entries; }
 
 }  // namespace rtg

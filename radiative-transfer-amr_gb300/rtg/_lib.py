@@ -94,6 +94,7 @@ SIGNATURES = {
                                     C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.c_void_p]),
     "rtg_dots_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
                                    C.c_void_p, C.c_void_p]),
+    "rtg_sweep_info": (C.c_int, [C.c_void_p, i32p, i32p, i64p, C.c_void_p]),
     "rtg_apply_tuning": (C.c_int, [C.c_void_p, i32p, C.c_int, i32p, C.c_void_p]),
     "rtg_sweep_trace": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, i32p, C.c_void_p]),
     "rtg_nn_rows": (C.c_int, [C.c_void_p, i64p]),

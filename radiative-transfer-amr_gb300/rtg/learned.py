@@ -5,7 +5,7 @@ include/rtg.h); this module drives them.  Torch tensors only carry device
 buffers: every feature, moment, forward, loss, gradient and Adam update runs
 in the library's own CUDA kernels.
 
-Preconditioner 2 is M r = z + L z, z = P_sweep^{-1} r, with L linear in z: per
+Preconditioner 3 is M r = z + L z, z = P_sweep^{-1} r, with L linear in z: per
 row (element, spatial node) o = C m(z), C a 3 x 8 coefficient matrix that a
 network computes from 16 local physics features, m(z) eight angular and
 neighbour moments of z, and (L z) = o0 + o1 cos th + o2 sin th.
@@ -155,7 +155,7 @@ def system_rhs(ctx, f_dev, g_dev):
 
 
 def collect_pairs(ctx, f_dev, g_dev, n_pairs=12, cycle=2, rtol=1e-12, restart=30, kind="arnoldi",
-                  normalize=True):
+                  normalize=True, max_it=1500):
     """Residual -> error pairs that the method's own sweep-GMRES generates.
 
     kind "arnoldi": the Arnoldi vectors v_j of sweep-preconditioned GMRES on
@@ -163,7 +163,8 @@ def collect_pairs(ctx, f_dev, g_dev, n_pairs=12, cycle=2, rtol=1e-12, restart=30
     to), with e_j = A_II^{-1} v_j from a converged sweep-GMRES solve each.
     kind "iterates": the residuals r_j = A_II e_j of the iterates u_j of short
     GMRES cycles, e_j = u* - u_j.
-    Returns a list of (F, M, S) row tensors, one entry per pair."""
+    Vectors whose error solve does not converge within max_it iterations are
+    skipped.  Returns a list of (F, M, S) row tensors, one entry per pair."""
     torch = _torch()
     mask = ctx.interior_mask()
     pairs = []
@@ -181,14 +182,14 @@ def collect_pairs(ctx, f_dev, g_dev, n_pairs=12, cycle=2, rtol=1e-12, restart=30
             V.append(w / nw)
         zero = torch.zeros_like(g_dev)
         for v in V:
-            e, inf = ctx.solve(v, zero, method=0, precond=1, rtol=rtol, restart=restart, max_it=4000)
+            e, inf = ctx.solve(v, zero, method=0, precond=1, rtol=rtol, restart=restart, max_it=max_it)
             if not inf["converged"]:
-                raise RuntimeError("solve for a training pair did not converge: {}".format(inf))
+                continue   # no exact error for this vector (stagnating solve): no pair
             pairs.append((v, torch.where(mask, e, torch.zeros_like(e))))
     elif kind == "iterates":
-        u_star, inf = ctx.solve(f_dev, g_dev, method=0, precond=1, rtol=rtol, restart=restart, max_it=4000)
+        u_star, inf = ctx.solve(f_dev, g_dev, method=0, precond=1, rtol=rtol, restart=restart, max_it=max_it)
         if not inf["converged"]:
-            raise RuntimeError("reference solve did not converge: {}".format(inf))
+            return []   # no converged solution to measure errors against
         u = None
         for _ in range(n_pairs):
             u, _ = ctx.solve(f_dev, g_dev, method=0, precond=1, rtol=1e-300, restart=cycle, max_it=cycle, x0=u)
