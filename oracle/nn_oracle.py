@@ -26,8 +26,10 @@ Definitions (shared with the CUDA kernels):
     phi(C, ij) = sum_K (dth_K / 2) sum_a w_a z / (2 pi),
     em(e) = sum_ij (wx wy / 4) m0,  cm(C) = sum_ij (wx wy / 4) phi,
     nm(C) = mean of cm over the distinct face-neighbour columns (0 if none);
-* network: h1 = relu(F W1 + b1), h2 = relu(h1 W2 + b2), C = h2 W3 + b3
-  (16 -> 128 -> 128 -> 24), weights rounded to BF16; C[3][8] per row;
+* network: h1 = relu(F W1 + b1), h2 = relu(h1 W2 + b2),
+  C = g (h2 W3 + b3) with the gate g = s / (1 + s), s = F1 (e^F0 - 1) (the
+  node's sigma h), 16 -> 128 -> 128 -> 24, weights rounded to BF16; C[3][8]
+  per row;
 * correction: o = C m, (L z)_beta = o0 + o1 cos th_a + o2 sin th_a at unknowns;
 * training statistics per row for a target error e, t = (e - z)/s with
   s = sqrt(sum z^2 / N), b_a = (1, cos th_a, sin th_a), unknown rows only:
@@ -231,13 +233,18 @@ class RowLayout:
         return S
 
 
+def gate(F):
+    s = np.maximum(F[:, 1] * np.expm1(F[:, 0]), 0.)
+    return s / (1. + s)
+
+
 def forward(p, F):
     d = unpack(p)
     a1 = F @ d["W1"] + d["b1"]
     h1 = np.maximum(a1, 0.)
     a2 = h1 @ d["W2"] + d["b2"]
     h2 = np.maximum(a2, 0.)
-    o = h2 @ d["W3"] + d["b3"]
+    o = gate(F)[:, None] * (h2 @ d["W3"] + d["b3"])
     return o, (h1, h2)
 
 
@@ -255,7 +262,7 @@ def loss_grad(p, F, M, S):
     Go = np.einsum("rab,rb->ra", G, o)
     loss = float((o * Go).sum() - 2. * (q * o).sum() + S[:, 9].sum())
     do = 2. * (Go - q)
-    dcoef = np.einsum("rk,rl->rkl", do, M).reshape(len(F), N_OUT)
+    dcoef = gate(F)[:, None] * np.einsum("rk,rl->rkl", do, M).reshape(len(F), N_OUT)
     g = {}
     g["W3"] = h2.T @ dcoef
     g["b3"] = dcoef.sum(0)

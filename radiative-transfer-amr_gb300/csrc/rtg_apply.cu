@@ -271,7 +271,7 @@ struct TileItem {
     int cpl_begin, cpl_end;   // entries of the item's couplings
     int tsz;                  // floats of T (padded to 4)
     int wcap;                 // floats of the W region
-    int ttot, ctot;           // work items of the two flux phases
+    int ttot, ctot;           // work items of the two flux phases (ctot: boundary nodes x rows)
 };
 
 // One coupling of a tiled item: where its neighbour line is, its mortars,
@@ -284,12 +284,37 @@ struct TileCpl {
     float dc;
 };
 constexpr int kMaxItemCpl = 96;
+constexpr int kMaxItemCells = 128;
+
+// f-th node on the boundary of an nx x ny node grid, going around (j = 0 row,
+// i = nx-1 column, j = ny-1 row, i = 0 column), each node once
+__device__ __forceinline__ void boundary_node(int f, int nx, int ny, int& i, int& j) {
+    if (nx == 1 || ny == 1) {   // a single row or column: every node is on the boundary
+        i = nx == 1 ? 0 : f;
+        j = nx == 1 ? f : 0;
+        return;
+    }
+    if (f < nx) { i = f; j = 0; return; }
+    f -= nx;
+    if (f < ny - 1) { i = nx - 1; j = f + 1; return; }
+    f -= ny - 1;
+    if (f < nx - 1) { i = nx - 2 - f; j = ny - 1; return; }
+    f -= nx - 1;
+    i = 0;
+    j = ny - 2 - f;
+}
+
+__host__ __device__ __forceinline__ int boundary_nodes(int nx, int ny) {
+    return (nx == 1 || ny == 1) ? nx * ny : 2 * (nx + ny) - 4;
+}
 
 __global__ void __launch_bounds__(kApplyThreads)
 apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__ items,
                    const TileCpl* __restrict__ cpl_ent, const float* __restrict__ x, float* __restrict__ y) {
     extern __shared__ float4 smt4[];
     __shared__ TileCpl sc[kMaxItemCpl];
+    __shared__ int4 s_el[kMaxItemCells];      // per item cell: first entry, end entry, local row, nth
+    __shared__ int s_po[kMaxItemCells + 1];   // prefix of boundary nodes x nth
     float* smt = reinterpret_cast<float*>(smt4);
     const TileItem it = items[blockIdx.x];
     const int ci = it.col;
@@ -319,6 +344,17 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
             off += nij * E.nth;
         }
         cbeg[ncell] = off;
+        int eb = 0, po = 0;
+        const int nb = boundary_nodes(C.nx, C.ny);
+        for (int k = it.cell_begin; k < it.cell_end; ++k) {
+            const ElemDev E = v.elems[C.elem_begin + k];
+            const int nc = E.cpl_end - E.cpl_begin;
+            s_el[k - it.cell_begin] = make_int4(eb, eb + nc, E.row - it.row0, E.nth);
+            s_po[k - it.cell_begin] = po;
+            eb += nc;
+            po += nb * E.nth;
+        }
+        s_po[it.cell_end - it.cell_begin] = po;
     }
     const int nent = it.cpl_end - it.cpl_begin;
     for (int q = threadIdx.x; q < nent; q += blockDim.x) sc[q] = cpl_ent[it.cpl_begin + q];
@@ -392,19 +428,33 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
             }
         }
         __syncthreads();
+        // one thread per (boundary node, row): the element's couplings on the
+        // node's faces in a fixed order, so the sum is deterministic
         {
-            int c = 0;
+            const int nb = boundary_nodes(C.nx, C.ny);
+            int k = 0;
             for (int t = threadIdx.x; t < it.ctot; t += blockDim.x) {
-                while (t >= sc[c].coff + sc[c].n0 * sc[c].nth) ++c;
-                const TileCpl& en = sc[c];
-                const int q = (t - en.coff) / en.nth, r = (t - en.coff) % en.nth;
-                const float* Es = v.mort + en.es;
+                while (t >= s_po[k + 1]) ++k;
+                const int4 el = s_el[k];
+                const int f = (t - s_po[k]) / el.w, r = (t - s_po[k]) % el.w;
+                int i, j;
+                boundary_node(f, C.nx, C.ny, i, j);
                 float acc = 0.f;
-                for (int jj = 0; jj < en.m1; ++jj) acc = fmaf(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], acc);
-                const int F = en.face;
-                const int i = (F == 0) ? C.nx - 1 : (F == 2 ? 0 : q);
-                const int j = (F == 1) ? C.ny - 1 : (F == 3 ? 0 : q);
-                atomicAdd(&Fy[(en.rowloc + r) * nijp + i * C.ny + j], en.dc * acc);
+                for (int c = el.x; c < el.y; ++c) {
+                    const TileCpl& en = sc[c];
+                    const int F = en.face;
+                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                    (F == 3 && j == 0);
+                    if (!on) continue;
+                    const int q = (F % 2 == 0) ? j : i;
+                    const float* Es = v.mort + en.es;
+                    float sacc = 0.f;
+                    for (int jj = 0; jj < en.m1; ++jj)
+                        sacc = fmaf(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+                    acc = fmaf(en.dc, sacc, acc);
+                }
+                (void)nb;
+                Fy[(el.z + r) * nijp + i * C.ny + j] = acc;
             }
         }
         __syncthreads();
@@ -656,7 +706,9 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                 while (k < ncell) {
                     const ElemDev& E = t.elems[C.elem_begin + k];
                     const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
-                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl)) break;
+                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl ||
+                                  k - ti.cell_begin >= kMaxItemCells))
+                        break;
                     M += nth;
                     ncp += nc;
                     ++k;
@@ -690,7 +742,10 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                     }
                 }
                 ti.ttot = tsz;
-                ti.ctot = csz;
+                ti.ctot = 0;
+                for (int q = ti.cell_begin; q < ti.cell_end; ++q)
+                    ti.ctot += boundary_nodes(C.nx, C.ny) * t.elems[C.elem_begin + q].nth;
+                (void)csz;
                 const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
                 // Fy and Ys are read and written as float4: keep every region
                 // a multiple of 4 floats from the 16-byte-aligned base

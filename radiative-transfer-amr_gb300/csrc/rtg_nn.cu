@@ -15,7 +15,10 @@
 //
 // The coefficients C(row) come from a 16-128-128-24 ReLU network of local
 // physics only (optical thickness and albedo at the node and around the
-// column, the cell's direction and extent, degrees, boundary faces), so M is a
+// column, the cell's direction and extent, degrees, boundary faces), times the
+// gate g = s / (1 + s), s = sigma h the node's scattering optical thickness:
+// where a region neither scatters nor is thick the sweep is already close to
+// exact and the correction is switched off whatever the network says.  M is a
 // fixed linear operator per problem: the coefficients are computed once when
 // the network is set, and each application costs a column pass and an element
 // pass over z.  Weights are rounded to BF16 when staged; accumulation is FP32.
@@ -112,8 +115,14 @@ __device__ __forceinline__ void layer_relu(const float* __restrict__ inT, const 
     }
 }
 
-// Forward pass of one tile: features into Ft, then h1T, h2T and the outputs
-// in sO[r][kOut] (thread: row t/4, outputs t%4 + 4u).
+// gate of a row from its features: s = c (e^f0 - 1) = sigma h, g = s / (1 + s)
+__device__ __forceinline__ float row_gate(float f0, float f1) {
+    const float sv = fmaxf(f1 * expm1f(f0), 0.f);
+    return sv / (1.f + sv);
+}
+
+// Forward pass of one tile: features into Ft, then h1T, h2T and the gated
+// outputs in sO[r][kOut] (thread: row t/4, outputs t%4 + 4u).
 __device__ __forceinline__ void forward_tile(const float* __restrict__ F, int64_t r0, int nr, float* sm) {
     float* Ft = sm + sF;
     for (int t = threadIdx.x; t < kTile * kIn; t += blockDim.x) {
@@ -137,8 +146,9 @@ __device__ __forceinline__ void forward_tile(const float* __restrict__ F, int64_
 #pragma unroll
         for (int u = 0; u < kOut / 4; ++u) acc[u] = fmaf(hv, W3[k * kOut + c0 + 4 * u], acc[u]);
     }
+    const float g = row_gate(Ft[r], Ft[kLd + r]);
 #pragma unroll
-    for (int u = 0; u < kOut / 4; ++u) sm[sO + r * kOut + c0 + 4 * u] = acc[u];
+    for (int u = 0; u < kOut / 4; ++u) sm[sO + r * kOut + c0 + 4 * u] = g * acc[u];
     __syncthreads();
 }
 
@@ -218,10 +228,12 @@ nn_grad_kernel(const float* __restrict__ P, const float* __restrict__ F, const f
                 d[1] = 2.f * (g1 - s[7]);
                 d[2] = 2.f * (g2 - s[8]);
             }
+            // dL/d(pre-gate outputs) = g dL/dC
+            const float g = row_gate(Ft[t], Ft[kLd + t]);
 #pragma unroll
             for (int k = 0; k < 3; ++k)
 #pragma unroll
-                for (int l = 0; l < kMom; ++l) dO[t * kLdo + kMom * k + l] = d[k] * m[l];
+                for (int l = 0; l < kMom; ++l) dO[t * kLdo + kMom * k + l] = g * d[k] * m[l];
         }
         __syncthreads();
         // dW3, db3
