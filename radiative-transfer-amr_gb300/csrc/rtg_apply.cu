@@ -129,6 +129,7 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
     extern __shared__ unsigned char smraw[];
     const int4 it = items[blockIdx.x];
     const int ci = it.x;
+    if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
@@ -318,6 +319,7 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
     float* smt = reinterpret_cast<float*>(smt4);
     const TileItem it = items[blockIdx.x];
     const int ci = it.col;
+    if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
@@ -518,6 +520,7 @@ __global__ void __launch_bounds__(kApplyThreads)
 apply_global_kernel(OpView<T> v, const float* __restrict__ mortf, uint32_t flags, const int32_t* __restrict__ cols,
                     const TX* __restrict__ x, TX* __restrict__ y) {
     const int ci = cols[blockIdx.x];
+    if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
     const T small = T(kSmall);

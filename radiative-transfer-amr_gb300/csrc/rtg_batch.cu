@@ -12,6 +12,12 @@
 //
 // method 1 (the batched workload's method): FP64 iterative refinement around
 // FP32 sweep-preconditioned GMRES; method 0: FP64 GMRES.
+//
+// Instances converge at different iterations; a finished instance costs
+// nothing for the rest of the cycle: per-column skip flags (refreshed inside
+// the captured cycle from the per-instance flags) make the operator apply and
+// the sweep leave its columns out, and the vector kernels leave out its
+// chunks.  Its frozen basis columns and correction are never read again.
 #include <chrono>
 #include <cmath>
 #include <vector>
@@ -33,9 +39,10 @@ struct BChunk {
 
 template <typename T>
 __global__ void bdot_kernel(const BChunk* __restrict__ ch, const T* __restrict__ V, int64_t ldv, int k,
-                            const T* __restrict__ w, double* __restrict__ partial) {
+                            const T* __restrict__ w, double* __restrict__ partial, const int32_t* __restrict__ done) {
     __shared__ double red[kBGroup][kBThreads / 32];
     const BChunk c = ch[blockIdx.x];
+    if (done && done[c.inst]) return;
     for (int g0 = 0; g0 < k; g0 += kBGroup) {
         const int gk = min(kBGroup, k - g0);
         double acc[kBGroup];
@@ -86,9 +93,10 @@ __global__ void breduce_kernel(const int32_t* __restrict__ cbeg, const double* _
 // w -= sum_{q<k} h[b][q] V_q on the chunk's instance b
 template <typename T>
 __global__ void baxpy_kernel(const BChunk* __restrict__ ch, T* __restrict__ w, const T* __restrict__ V, int64_t ldv,
-                             int k, const double* __restrict__ h, int ldh) {
+                             int k, const double* __restrict__ h, int ldh, const int32_t* __restrict__ done) {
     __shared__ double hs[64];
     const BChunk c = ch[blockIdx.x];
+    if (done && done[c.inst]) return;
     if (threadIdx.x < k) hs[threadIdx.x] = h[c.inst * ldh + threadIdx.x];
     __syncthreads();
     for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
@@ -102,8 +110,10 @@ __global__ void baxpy_kernel(const BChunk* __restrict__ ch, T* __restrict__ w, c
 template <typename T>
 __global__ void bnormalize_kernel(const BChunk* __restrict__ ch, const int32_t* __restrict__ cbeg,
                                   const T* __restrict__ w, T* __restrict__ out, const double* __restrict__ nsq,
-                                  int ldn, double* __restrict__ hcol, int ldh, int jcol) {
+                                  int ldn, double* __restrict__ hcol, int ldh, int jcol,
+                                  const int32_t* __restrict__ done) {
     const BChunk c = ch[blockIdx.x];
+    if (done && done[c.inst]) return;
     const double nr = sqrt(nsq[c.inst * ldn]);
     if (hcol && threadIdx.x == 0 && cbeg[c.inst] == (int)blockIdx.x) hcol[c.inst * ldh + jcol] = nr;
     const double inv = nr > 0. ? 1. / nr : 0.;
@@ -202,6 +212,24 @@ __global__ void bsolve_kernel(int nb, int m, const double* __restrict__ H, const
     for (int q = k; q < m; ++q) yb[q] = 0.;
 }
 
+// Per-column skip flags from the per-instance state: mode 0 skips finished
+// instances (done), mode 1 skips instances without a correction (kvalid 0).
+__global__ void bskip_kernel(int ncols, const int32_t* __restrict__ col_inst, const int32_t* __restrict__ done,
+                             const int32_t* __restrict__ kvalid, int mode, int32_t* __restrict__ skip) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    const int b = col_inst[c];
+    skip[c] = mode == 0 ? (done[b] != 0) : (kvalid[b] == 0);
+}
+
+// d += z on the chunks of instances that formed a correction this cycle
+__global__ void badd_kernel(const BChunk* __restrict__ ch, const float* __restrict__ z, float* __restrict__ d,
+                            const int32_t* __restrict__ kvalid) {
+    const BChunk c = ch[blockIdx.x];
+    if (kvalid[c.inst] == 0) return;
+    for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) d[i] += z[i];
+}
+
 inline int grid1(int n) { return (n + 127) / 128; }
 
 }  // namespace
@@ -217,6 +245,7 @@ struct BatchWs {
     double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr, *est = nullptr;
     double *tol = nullptr, *tin = nullptr, *scale = nullptr, *vnorm = nullptr;
     int32_t *kvalid = nullptr, *done = nullptr;
+    int32_t *col_inst = nullptr, *col_skip = nullptr;   // per column: instance, skip flag
     cudaGraphExec_t cycle = nullptr;
     std::vector<void*> allocs;
 };
@@ -240,8 +269,8 @@ void free_bws(BatchWs* w) {
 
 // per-instance squared norms into out[b*ldo]
 template <typename T>
-void bnorm2(const BatchWs* w, const T* v, double* out, int ldo, cudaStream_t s) {
-    bdot_kernel<T><<<w->nchunks, kBThreads, 0, s>>>(w->d_ch, v, 0, 1, v, w->partial);
+void bnorm2(const BatchWs* w, const T* v, double* out, int ldo, cudaStream_t s, const int32_t* done = nullptr) {
+    bdot_kernel<T><<<w->nchunks, kBThreads, 0, s>>>(w->d_ch, v, 0, 1, v, w->partial, done);
     breduce_kernel<<<dim3(w->nb, 1), 128, 0, s>>>(w->d_cbeg, w->partial, 1, out, ldo, nullptr, nullptr);
 }
 
@@ -251,37 +280,43 @@ void record_cycle(rtg_handle* h, BatchWs* w, cudaStream_t s) {
     const int m = w->m, nb = w->nb, nc = w->nchunks;
     const int64_t N = w->N;
     const int ldh = m + 2;
-    const OpView<float>& v = h->v32;
+    const int ncols = h->v32.ncols;
+    OpView<float> v = h->v32;       // the operator with the batch's column skip flags
+    v.skip = w->col_skip;
     // w = rhs - A d ; V0 = w / ||w|| ; start
-    launch_apply<float>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, w->d32, w->s32, s);
+    launch_apply<float>(h, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, w->d32, w->s32, s);
     bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->rhs32, w->w32, nullptr, 0, 1., 0.);
     bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->w32, nullptr, 0, -1., 1.);
     bnorm2<float>(w, w->w32, w->nsq, 1, s);
-    bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, w->V32, w->nsq, 1, nullptr, 0, 0);
+    bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, w->V32, w->nsq, 1, nullptr, 0, 0,
+                                                      nullptr);
     bstart_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->nsq, 1, w->g, w->tin, w->kvalid, w->done);
     for (int j = 0; j < m; ++j) {
         float* vj = w->V32 + (int64_t)j * N;
         float* vn = w->V32 + (int64_t)(j + 1) * N;
-        apply_sweep<float>(h, vj, w->z32, s);
+        bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 0, w->col_skip);
+        apply_sweep<float>(h, vj, w->z32, s, nullptr, w->col_skip);
         launch_apply<float>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, w->z32, w->w32, s);
         // CGS2 with per-instance coefficients; ho = h1 + h2
-        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial);
+        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done);
         breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h1, ldh, nullptr, nullptr);
-        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h1, ldh);
-        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial);
+        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h1, ldh, w->done);
+        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done);
         breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h2, ldh, w->h1, w->ho);
-        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h2, ldh);
-        bnorm2<float>(w, w->w32, w->nsq, 1, s);
-        bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, vn, w->nsq, 1, w->ho, ldh, j + 1);
+        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h2, ldh, w->done);
+        bnorm2<float>(w, w->w32, w->nsq, 1, s, w->done);
+        bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, vn, w->nsq, 1, w->ho, ldh, j + 1,
+                                                          w->done);
         barnoldi_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, j, w->ho, ldh, w->H, w->cs, w->sn, w->g, w->tin, w->kvalid,
                                                    w->done, w->est);
     }
-    // d += P^{-1} (V y)
+    // d += P^{-1} (V y), for the instances that formed a correction
     bsolve_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->H, w->g, w->kvalid, w->y);
     bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->s32, nullptr, 0, 0., 0.);
     bcombine_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->V32, N, w->kvalid, w->y, m);
-    apply_sweep<float>(h, w->s32, w->z32, s);
-    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->z32, w->d32, nullptr, 0, 1., 1.);
+    bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 1, w->col_skip);
+    apply_sweep<float>(h, w->s32, w->z32, s, nullptr, w->col_skip);
+    badd_kernel<<<nc, kBThreads, 0, s>>>(w->d_ch, w->z32, w->d32, w->kvalid);
 }
 
 }  // namespace
@@ -359,6 +394,20 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
         w->vnorm = balloc<double>(w, nb);
         w->kvalid = balloc<int32_t>(w, nb);
         w->done = balloc<int32_t>(w, nb);
+        // instance of every column (columns are contiguous in DOF order)
+        const HostTables& t = h->host;
+        std::vector<int32_t> ci(t.cols.size());
+        int b = 0;
+        for (size_t c = 0; c < t.cols.size(); ++c) {
+            while (b + 1 < nb && t.cols[c].dof_off >= inst_off[b + 1]) ++b;
+            if (t.cols[c].dof_off < inst_off[b] || t.cols[c].dof_off + t.cols[c].ndof > inst_off[b + 1])
+                throw RtgError{RTG_ERR_ARG, "an instance boundary splits a column"};
+            ci[c] = b;
+        }
+        w->col_inst = balloc<int32_t>(w, ci.size());
+        w->col_skip = balloc<int32_t>(w, ci.size());
+        RTG_CUDA(cudaMemcpy(w->col_inst, ci.data(), sizeof(int32_t) * ci.size(), cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemset(w->col_skip, 0, sizeof(int32_t) * ci.size()));
     }
     const int nc = w->nchunks;
     // b = mask_I (f - A mask_B g); x = 0

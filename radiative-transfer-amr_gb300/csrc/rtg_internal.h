@@ -116,6 +116,7 @@ struct OpView {
     const CplGeo* cgeo;   // per coupling: neighbour line addressing
     int32_t ncols;
     int32_t nelem;
+    const int32_t* skip = nullptr;   // per column: nonzero = leave the column out (batched solve)
 };
 
 struct HostTables {
@@ -190,7 +191,8 @@ int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s);
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
 template <typename T>
-void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace);
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace,
+                 const int32_t* skip = nullptr);
 void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
 int sweep_levels_count(rtg_handle* h, cudaStream_t s);

@@ -229,6 +229,13 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         const int e = order[idx];
         if (trace && threadIdx.x == 0) trace[kTr * e] = globaltimer_ns();
         const ElemDev E = v.elems[e];
+        if (v.skip && v.skip[E.col]) {
+            // left out (a converged instance of a batch): publish without work;
+            // only elements of the same column set depend on it
+            __syncthreads();
+            if (threadIdx.x == 0) atomicExch(&done[e], epoch);
+            continue;
+        }
         const ColDev C = v.cols[E.col];
         const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
         const int bm = E.flags >> 4;
@@ -630,11 +637,12 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
 // loaded, couplings formed, values stored, fence passed] (globaltimer ns) in
 // trace[8e .. 8e+7].
 template <typename T>
-void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace) {
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
-    const OpView<T>& v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
+    OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
+    v.skip = skip;
     sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_epoch, s->d_next);
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
@@ -684,8 +692,10 @@ int sweep_status(rtg_handle* h, cudaStream_t st) {
 
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t);
-template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t, unsigned long long*);
-template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t, unsigned long long*);
+template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t, unsigned long long*,
+                                  const int32_t*);
+template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t, unsigned long long*,
+                                 const int32_t*);
 
 int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
 int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
