@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
-                    help="short run for ncu: one warm and one measured solve per method, 3 applies")
+                    help="short run for ncu: two solves per method (learned+mixed, mixed, plain), "
+                         "then 3 FP32 and 3 FP64 applies and sweeps")
     ap.add_argument("--rtol", type=float, default=1e-9, help="profile mode: solver tolerance")
     ap.add_argument("--max-it", type=int, default=20000, help="profile mode: iteration cap")
     return ap.parse_args()
@@ -88,18 +89,22 @@ def run_profile(args):
     torch.cuda.synchronize()
     out["sweep_setup_s"] = time.perf_counter() - t0
     print(json.dumps({k: out[k] for k in out}), file=sys.stderr, flush=True)
-    for method in (1, 0):
+    from rtg import learned as LN
+    LN.set_params(ctx, LN.load(LN.DEFAULT_NET)[0])
+    # learned+mixed (the headline method), mixed, plain FP64
+    for name, method, pc in (("learned_mixed", 1, 3), ("mixed", 1, 1), ("plain_fp64", 0, 1)):
         for rep in range(2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=args.rtol, max_it=args.max_it, precond=1)
+            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=args.rtol, max_it=args.max_it, precond=pc,
+                                restart=30, inner_rtol=1e-5)
             torch.cuda.synchronize()
-            out["method%d_rep%d" % (method, rep)] = {"s": time.perf_counter() - t0,
-                                                     "iterations": info["iterations"],
-                                                     "sweeps": info["sweeps"],
-                                                     "res_f": info["res_f"], "rhs_norm": info["rhs_norm"],
-                                                     "converged": info["converged"]}
-            print(json.dumps(out["method%d_rep%d" % (method, rep)]), file=sys.stderr, flush=True)
+            out["%s_rep%d" % (name, rep)] = {"s": time.perf_counter() - t0,
+                                             "iterations": info["iterations"],
+                                             "sweeps": info["sweeps"],
+                                             "res_f": info["res_f"], "rhs_norm": info["rhs_norm"],
+                                             "converged": info["converged"]}
+            print(json.dumps(out["%s_rep%d" % (name, rep)]), file=sys.stderr, flush=True)
     stream = torch.cuda.current_stream()
     for prec in (_lib.RTG_FP32, _lib.RTG_FP64):
         dt = torch.float32 if prec == _lib.RTG_FP32 else torch.float64
@@ -238,6 +243,19 @@ def kernel_time(fn, stream, flush, reps=20):
         torch.cuda.synchronize()
         durs.append(e0.elapsed_time(e1) / 1e3)
     return statistics.median(durs)
+
+
+def profiled_traffic(name):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
+    (line "traffic_bytes_per_launch: N"), or None."""
+    try:
+        with open(os.path.join(REPO, "profiles", name + ".md")) as fh:
+            for line in fh:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 def sweep_bytes(ctx, prec_bytes):
@@ -420,7 +438,9 @@ def run_ours(args):
                 "d2h_bytes_per_step": 8 * N, "rel_l2_err": e2e_err},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": sb / t_sweep / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": sb / t_sweep / 1e9 / peak, "traffic": None,
+                     "frac": sb / t_sweep / 1e9 / peak,
+                     "traffic": profiled_traffic("sweep_persistent_kernel_fp32_cfg2") if args.workload == "cfg2"
+                     else None,
                      "kernel": "sweep_persistent_kernel<float>", "bytes_per_launch": sb, "launch_s": t_sweep,
                      "peak_kind": peak_kind,
                      "note": "latency bound: {} wavefront levels, {:.2f} us per level".format(
