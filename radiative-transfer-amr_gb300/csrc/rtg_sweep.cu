@@ -331,19 +331,9 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
         // ---- couplings c on the face nodes, into rhs[ij * nth + r]
         if (ncs >= 0) {
-            for (int c = 0; c < ncs; ++c) {
-                const int m1 = s_m1[c], nt1 = s_nt1[c];
-                T* dst = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth;
-                const T* src = z + s_base[c];
-                const int str = s_str[c];
-                for (int t = threadIdx.x; t < m1 * nt1; t += blockDim.x) {
-                    const int jj = t / nt1, a = t % nt1;
-                    dst[t] = __ldcg(src + (int64_t)jj * str + a);
-                }
-            }
-            __syncthreads();
-            if (trace && threadIdx.x == 0) trace[kTr * e + 4] = globaltimer_ns();
-            // T[jj][r] = sum_a Et[a][r] zl[jj][a], all couplings at once
+            // T[jj][r] = sum_a Et[a][r] zl[jj][a] for all couplings at once,
+            // reading the upwind face line zl straight from global memory (the
+            // nt1 loads of an item are independent: one round trip)
             {
                 int c = 0, base = 0;
                 for (int t = threadIdx.x;; t += blockDim.x) {
@@ -355,15 +345,22 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                     if (c >= ncs) break;
                     const int m1 = s_m1[c], nt1 = s_nt1[c];
                     const T* Et = cs + s_off[c] + m1 * s_n0[c];
-                    const T* zl = Et + nt1 * nth;
                     T* Tm = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth + m1 * nt1;
                     const int q = t - base, jj = q / nth, r = q % nth;
+                    const T* zl = z + s_base[c] + (int64_t)jj * s_str[c];
+                    T zv[kMaxNodes];
+#pragma unroll
+                    for (int a = 0; a < kMaxNodes; ++a)
+                        if (a < nt1) zv[a] = __ldcg(zl + a);
                     T acc = T(0);
-                    for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
+#pragma unroll
+                    for (int a = 0; a < kMaxNodes; ++a)
+                        if (a < nt1) acc += Et[a * nth + r] * zv[a];
                     Tm[jj * nth + r] = acc;
                 }
             }
             __syncthreads();
+            if (trace && threadIdx.x == 0) trace[kTr * e + 4] = globaltimer_ns();
             for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
                 const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
                 T acc = T(0);
@@ -418,13 +415,12 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             }
             __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
         }
-        if (trace) {
-            __syncthreads();
-            if (threadIdx.x == 0) trace[kTr * e + 6] = globaltimer_ns();
-        }
-        __threadfence();
+        // publish: the barrier orders every thread's stores before thread 0's
+        // GPU-scope fence (cumulative), which orders them before the flag
         __syncthreads();
         if (threadIdx.x == 0) {
+            if (trace) trace[kTr * e + 6] = globaltimer_ns();
+            __threadfence();
             if (trace) trace[kTr * e + 7] = globaltimer_ns();
             atomicExch(&done[e], epoch);
             if (trace) {
