@@ -633,6 +633,10 @@ __global__ void weight_forcing_kernel(OpView<double> v, const double* f, double*
 // outputs, heaviest chunks first, in two launch groups: with the column's W
 // staged too, or (large angular meshes) with W read through L2.
 constexpr int kChunk = 1024;
+// The FP64 apply is FP64-pipe bound and, with large items, all of them fit in
+// one wave, so the heaviest item sets the kernel time: smaller items balance
+// the SMs (the item size is tuned per handle, tune_plan64).
+constexpr int kChunk64 = 256;
 
 struct ApplyGroup {
     int4* d_items = nullptr;
@@ -681,7 +685,7 @@ static size_t tile_smem_bytes(int nth_col, int nij, int wcap, int M, int ncell) 
 // include: per column, whether the plan covers it (null: every column).
 template <typename T>
 static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = nullptr,
-                            const std::vector<char>* include = nullptr) {
+                            const std::vector<char>* include = nullptr, int chunk64 = kChunk64) {
     const HostTables& t = h->host;
     constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
@@ -782,7 +786,8 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         }
         const int grp = (sx + sw <= kSmemBudget) ? 0 : 1;
         need[grp] = std::max(need[grp], grp == 0 ? sx + sw : sx);
-        const int nch = (C.ndof + kChunk - 1) / kChunk;
+        const int chunk = parity ? chunk64 : kChunk;
+        const int nch = (C.ndof + chunk - 1) / chunk;
         const int per = (C.ndof + nch - 1) / nch;
         for (int q = 0; q < nch; ++q) {
             const int b0 = q * per, b1 = std::min(C.ndof, b0 + per);
@@ -987,6 +992,62 @@ static ApplyPlan* tune_plan32(rtg_handle* h, cudaStream_t s) {
     return tuned;
 }
 
+// FP64 apply: the whole apply timed with 128, 256 and 512 outputs per item
+// (best of three after a warm-up); the fastest plan is kept.
+static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
+    const int64_t N = h->host.ndof;
+    double *x = nullptr, *y = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ApplyPlan* best = nullptr;
+    float tbest = 1e30f;
+    auto release = [&] {
+        if (x) cudaFree(x);
+        if (y) cudaFree(y);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    try {
+        RTG_CUDA(cudaMalloc(&x, sizeof(double) * std::max<int64_t>(N, 1)));
+        RTG_CUDA(cudaMalloc(&y, sizeof(double) * std::max<int64_t>(N, 1)));
+        RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s));
+        RTG_CUDA(cudaEventCreate(&e0));
+        RTG_CUDA(cudaEventCreate(&e1));
+        for (int chunk : {128, 256, 512}) {
+            ApplyPlan* p = make_plan<double>(h, nullptr, nullptr, chunk);
+            float tt = 1e30f;
+            try {
+                set_plan_attributes<double>(p);
+                run_plan<double>(p, h->v64, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+                for (int rep = 0; rep < 3; ++rep) {
+                    RTG_CUDA(cudaEventRecord(e0, s));
+                    run_plan<double>(p, h->v64, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+                    RTG_CUDA(cudaEventRecord(e1, s));
+                    RTG_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    tt = std::min(tt, ms);
+                }
+            } catch (...) {
+                free_plan(p);
+                throw;
+            }
+            if (tt < tbest) {
+                free_plan(best);
+                best = p;
+                tbest = tt;
+            } else {
+                free_plan(p);
+            }
+        }
+    } catch (...) {
+        free_plan(best);
+        release();
+        throw;
+    }
+    release();
+    return best;
+}
+
 int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s) {
     if (!h->plan32) {
         h->plan32 = tune_plan32(h, s);
@@ -1018,7 +1079,7 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
     constexpr bool f64 = sizeof(T) == 8;
     ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
     if (!plan) {
-        plan = f64 ? make_plan<T>(h) : tune_plan32(h, s);
+        plan = f64 ? tune_plan64(h, s) : tune_plan32(h, s);
         set_plan_attributes<T>(plan);
     }
     run_plan<T>(plan, v, h->v32, flags, x, y, s);

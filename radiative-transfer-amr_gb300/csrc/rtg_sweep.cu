@@ -331,9 +331,19 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
         // ---- couplings c on the face nodes, into rhs[ij * nth + r]
         if (ncs >= 0) {
-            // T[jj][r] = sum_a Et[a][r] zl[jj][a] for all couplings at once,
-            // reading the upwind face line zl straight from global memory (the
-            // nt1 loads of an item are independent: one round trip)
+            // stage the upwind face lines (coalesced, each value once)
+            for (int c = 0; c < ncs; ++c) {
+                const int m1 = s_m1[c], nt1 = s_nt1[c];
+                T* dst = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth;
+                const T* src = z + s_base[c];
+                const int str = s_str[c];
+                for (int t = threadIdx.x; t < m1 * nt1; t += blockDim.x) {
+                    const int jj = t / nt1, a = t % nt1;
+                    dst[t] = __ldcg(src + (int64_t)jj * str + a);
+                }
+            }
+            __syncthreads();
+            // T[jj][r] = sum_a Et[a][r] zl[jj][a], all couplings at once
             {
                 int c = 0, base = 0;
                 for (int t = threadIdx.x;; t += blockDim.x) {
@@ -345,17 +355,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                     if (c >= ncs) break;
                     const int m1 = s_m1[c], nt1 = s_nt1[c];
                     const T* Et = cs + s_off[c] + m1 * s_n0[c];
+                    const T* zl = Et + nt1 * nth;
                     T* Tm = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth + m1 * nt1;
                     const int q = t - base, jj = q / nth, r = q % nth;
-                    const T* zl = z + s_base[c] + (int64_t)jj * s_str[c];
-                    T zv[kMaxNodes];
-#pragma unroll
-                    for (int a = 0; a < kMaxNodes; ++a)
-                        if (a < nt1) zv[a] = __ldcg(zl + a);
                     T acc = T(0);
-#pragma unroll
-                    for (int a = 0; a < kMaxNodes; ++a)
-                        if (a < nt1) acc += Et[a * nth + r] * zv[a];
+                    for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
                     Tm[jj * nth + r] = acc;
                 }
             }
