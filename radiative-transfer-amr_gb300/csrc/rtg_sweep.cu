@@ -162,12 +162,15 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
 }
 
 // Persistent wavefront sweep: z_e = B_e^{-1} (rin_e - sum_upwind C_ee' z_e').
-// CTAs claim elements in topological order from an atomic counter.  An
-// element waits (bounded) until every upwind element it couples to has
-// published the current epoch in done[]; those elements come earlier in the
-// order, so they were claimed by CTAs that are already running and the wait
-// always ends unless a CTA gave up.  A CTA that gives up sets *status and
-// every other CTA stops waiting as soon as it sees the status.
+// CTAs claim elements in topological order from an atomic counter.  Before
+// the sweep z is filled with a sentinel (a NaN payload that arithmetic never
+// produces); an element reads the upwind face lines it needs straight from z,
+// spinning (bounded) on each value until it no longer holds the sentinel.  A
+// value that has arrived is both the data and the signal, so there is no flag,
+// no release fence and no second round trip per level.  The upwind elements
+// come earlier in the claim order, so they were claimed by CTAs that are
+// already running and every wait ends unless a CTA gave up; a CTA that gives
+// up sets *status and every other CTA stops waiting as soon as it sees it.
 //
 // The critical path of the sweep is the work an element does after its wait,
 // so everything that does not depend on upwind values happens before it: the
@@ -181,6 +184,91 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
 constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
 constexpr int kMaxFaceNodes = 4 * kMaxNodes;
 constexpr int kTr = 8;   // trace entries per element
+
+// The sentinel of the published-value protocol, as raw bits (signalling NaNs
+// with a payload; loads and stores move bits, never FP values).
+template <typename T>
+struct Sentinel;
+template <>
+struct Sentinel<float> {
+    using U = unsigned int;
+    static constexpr U bits = 0x7FBADBADu;
+};
+template <>
+struct Sentinel<double> {
+    using U = unsigned long long;
+    static constexpr U bits = 0x7FF4BADBADBADBADull;
+};
+
+template <typename T>
+__device__ __forceinline__ T from_bits(typename Sentinel<T>::U u) {
+    T v;
+    memcpy(&v, &u, sizeof(T));
+    return v;
+}
+
+// Relaxed GPU-scope accesses: morally strong, so a reader racing with the
+// writer sees either the sentinel or the whole published value.
+__device__ __forceinline__ unsigned int ld_relaxed(const unsigned int* p) {
+    unsigned int u;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(u) : "l"(p) : "memory");
+    return u;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+    unsigned long long u;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(u) : "l"(p) : "memory");
+    return u;
+}
+__device__ __forceinline__ void st_relaxed(float* p, float x) {
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(double* p, double x) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"((unsigned long long)__double_as_longlong(x))
+                 : "memory");
+}
+
+// Load a value of z that an upwind element publishes during this sweep:
+// spin (bounded) while it still holds the sentinel.  Returns false when the
+// wait gave up (timeout, or another CTA's status).
+template <typename T>
+__device__ __forceinline__ bool load_published(const T* p, T& out, int* status) {
+    using U = typename Sentinel<T>::U;
+    const U* q = reinterpret_cast<const U*>(p);
+    U u = ld_relaxed(q);
+    if (u != Sentinel<T>::bits) {
+        out = from_bits<T>(u);
+        return true;
+    }
+    const long long t0 = clock64();
+    for (;;) {
+        __nanosleep(32);
+        u = ld_relaxed(q);
+        if (u != Sentinel<T>::bits) {
+            out = from_bits<T>(u);
+            return true;
+        }
+        if (__ldcv(status) != 0) return false;
+        if (clock64() - t0 > kSpinLimitCycles) {
+            atomicExch(status, RTG_ERR_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+// Writes the sentinel over the values of z the sweep will publish (elements
+// of columns left out keep their values).
+template <typename T>
+__global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z) {
+    using U = typename Sentinel<T>::U;
+    U* q = reinterpret_cast<U*>(z);
+    for (int e = blockIdx.x; e < ne; e += gridDim.x) {
+        const ElemDev E = v.elems[e];
+        if (v.skip && v.skip[E.col]) continue;
+        const ColDev C = v.cols[E.col];
+        const int nloc = C.nx * C.ny * E.nth;
+        for (int t = threadIdx.x; t < nloc; t += blockDim.x) q[E.dof_off + t] = Sentinel<T>::bits;
+    }
+}
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;
@@ -196,8 +284,7 @@ template <typename T>
 __global__ void __launch_bounds__(kSweepThreads)
 sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
                         const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
-                        const T* __restrict__ rin, T* z, unsigned int* __restrict__ done,
-                        const unsigned int* __restrict__ epoch_ptr, unsigned int* __restrict__ next,
+                        const T* __restrict__ rin, T* z, unsigned int* __restrict__ next,
                         int* __restrict__ status,
                         int rhs_cap, int bcap, int ccap, unsigned long long* __restrict__ trace) {
     extern __shared__ unsigned char sraw[];
@@ -217,7 +304,6 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     __shared__ int s_str[kMaxCplStaged];
     __shared__ long long s_base[kMaxCplStaged];
     __shared__ T s_dc[kMaxCplStaged];
-    const unsigned int epoch = __ldcg(epoch_ptr);   // set by sweep_begin_kernel
     for (;;) {
         if (threadIdx.x == 0) {
             s_idx = (int)atomicAdd(next, 1u);
@@ -230,10 +316,9 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         if (trace && threadIdx.x == 0) trace[kTr * e] = globaltimer_ns();
         const ElemDev E = v.elems[e];
         if (v.skip && v.skip[E.col]) {
-            // left out (a converged instance of a batch): publish without work;
-            // only elements of the same column set depend on it
+            // left out (a converged instance of a batch): no work and no
+            // values; only elements left out with it read them
             __syncthreads();
-            if (threadIdx.x == 0) atomicExch(&done[e], epoch);
             continue;
         }
         const ColDev C = v.cols[E.col];
@@ -307,31 +392,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
             zpre[ij * nth + r] = acc;
         }
-        // ---- wait for the upwind elements this one reads
-        for (int k = E.cpl_begin + threadIdx.x; k < E.cpl_end; k += blockDim.x) {
-            if (!active[k]) continue;
-            const int nb = v.cpls[k].nbr;
-            const long long t0 = clock64();
-            while (atomicAdd(&done[nb], 0u) != epoch) {
-                if (atomicAdd((unsigned int*)status, 0u) != 0u) {
-                    s_abort = 1;
-                    break;
-                }
-                if (clock64() - t0 > kSpinLimitCycles) {
-                    atomicExch(status, RTG_ERR_TIMEOUT);
-                    s_abort = 1;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        __syncthreads();
-        if (s_abort) break;
-        __threadfence();
-        if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
         // ---- couplings c on the face nodes, into rhs[ij * nth + r]
+        if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
         if (ncs >= 0) {
-            // stage the upwind face lines (coalesced, each value once)
+            // stage the upwind face lines as they are published (coalesced,
+            // each value once; each thread waits on its own values)
             for (int c = 0; c < ncs; ++c) {
                 const int m1 = s_m1[c], nt1 = s_nt1[c];
                 T* dst = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth;
@@ -339,10 +404,13 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 const int str = s_str[c];
                 for (int t = threadIdx.x; t < m1 * nt1; t += blockDim.x) {
                     const int jj = t / nt1, a = t % nt1;
-                    dst[t] = __ldcg(src + (int64_t)jj * str + a);
+                    T val = T(0);
+                    if (!load_published(src + (int64_t)jj * str + a, val, status)) s_abort = 1;
+                    dst[t] = val;
                 }
             }
             __syncthreads();
+            if (s_abort) break;
             // T[jj][r] = sum_a Et[a][r] zl[jj][a], all couplings at once
             {
                 int c = 0, base = 0;
@@ -399,7 +467,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                     for (int jj = 0; jj < g.m1; ++jj) {
                         const T* zl = z + g.base + (int64_t)jj * g.stride;
                         T sacc = T(0);
-                        for (int a = 0; a < g.nth1; ++a) sacc += Et[a * nth + r] * __ldcg(zl + a);
+                        for (int a = 0; a < g.nth1; ++a) {
+                            T val = T(0);
+                            if (!load_published(zl + a, val, status)) s_abort = 1;
+                            sacc += Et[a * nth + r] * val;
+                        }
                         acc += dc * Es[jj * n0 + qq] * sacc;
                     }
                 }
@@ -407,6 +479,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             }
         }
         __syncthreads();
+        if (s_abort) break;
         if (trace && threadIdx.x == 0) trace[kTr * e + 5] = globaltimer_ns();
         // ---- z = zpre - B c over the face columns of B
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
@@ -417,32 +490,25 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 const int k = s_face[f];
                 acc -= col[k * nn] * rhs[k * nth + r];
             }
-            __stcg(z + E.dof_off + (int64_t)ij * nth + r, acc);
+            st_relaxed(z + E.dof_off + (int64_t)ij * nth + r, acc);
         }
-        // publish: the barrier orders every thread's stores before thread 0's
-        // GPU-scope fence (cumulative), which orders them before the flag
+        // the stored values are the publication (downstream elements wait on
+        // the values themselves); the barrier ends this element's use of the
+        // shared buffers before the next claim
         __syncthreads();
-        if (threadIdx.x == 0) {
-            if (trace) trace[kTr * e + 6] = globaltimer_ns();
-            __threadfence();
-            if (trace) trace[kTr * e + 7] = globaltimer_ns();
-            atomicExch(&done[e], epoch);
-            if (trace) {
-                trace[kTr * e + 2] = globaltimer_ns();
-                trace[kTr * e + 3] = (unsigned long long)blockIdx.x;
-            }
+        if (trace && threadIdx.x == 0) {
+            const unsigned long long tn = globaltimer_ns();
+            trace[kTr * e + 2] = tn;
+            trace[kTr * e + 6] = tn;
+            trace[kTr * e + 7] = tn;
+            trace[kTr * e + 3] = (unsigned long long)blockIdx.x;
         }
     }
 }
 
-// Starts a sweep: advance the epoch (never 0, the flags' initial value) and
-// reset the work counter.  Device-side so that a captured graph can replay it.
-__global__ void sweep_begin_kernel(unsigned int* epoch, unsigned int* next) {
-    unsigned int e = *epoch + 1u;
-    if (e == 0u) e = 1u;
-    *epoch = e;
-    *next = 0u;
-}
+// Starts a sweep: reset the work counter.  Device-side so that a captured
+// graph can replay it.
+__global__ void sweep_begin_kernel(unsigned int* next) { *next = 0u; }
 
 }  // namespace
 
@@ -462,9 +528,7 @@ struct Sweep {
     int bcap64 = 0, bcap32 = 0, grid64 = 0, grid32 = 0;
     int n_lagged = 0;
     std::vector<void*> allocs;
-    unsigned int* d_done = nullptr;      // per element: epoch of the last sweep that finished it
     unsigned int* d_next = nullptr;      // work counter
-    unsigned int* d_epoch = nullptr;     // current epoch
     int* d_status = nullptr;             // RTG_ERR_TIMEOUT if a wait gave up
 };
 
@@ -602,12 +666,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     RTG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     RTG_CUDA(cudaStreamSynchronize(st));
     if (status) throw RtgError{RTG_ERR_NONFINITE, "singular element block in the sweep preconditioner"};
-    s->d_done = sw_alloc<unsigned int>(s, ne);
     s->d_next = sw_alloc<unsigned int>(s, 1);
-    s->d_epoch = sw_alloc<unsigned int>(s, 1);
-    RTG_CUDA(cudaMemset(s->d_epoch, 0, sizeof(unsigned int)));
     s->d_status = sw_alloc<int>(s, 1);
-    RTG_CUDA(cudaMemset(s->d_done, 0, sizeof(unsigned int) * ne));
     RTG_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
     int64_t max_b = 0;
     for (int e = 0; e < ne; ++e) {
@@ -633,9 +693,9 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
 }
 
 // z = P^{-1} r (full-length vectors; inflow-boundary entries of z are zero).
-// With trace, element e records [claim, ready, published, cta, upwind lines
-// loaded, couplings formed, values stored, fence passed] (globaltimer ns) in
-// trace[8e .. 8e+7].
+// With trace, element e records [claim, independent work done, published,
+// cta, upwind lines loaded, couplings formed, published, published]
+// (globaltimer ns) in trace[8e .. 8e+7].
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip) {
     Sweep* s = get_sweep(h, st);
@@ -643,7 +703,11 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
     v.skip = skip;
-    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_epoch, s->d_next);
+    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_next);
+    {
+        const int ne = (int)h->host.elems.size();
+        sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z);
+    }
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
     int& grid = f64 ? s->grid64 : s->grid32;
@@ -662,8 +726,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
     }
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
-        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_done,
-        s->d_epoch, s->d_next, s->d_status, rhs_cap, bcap, (int)s->max_c, trace);
+        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next, s->d_status,
+        rhs_cap, bcap, (int)s->max_c, trace);
     RTG_CUDA(cudaGetLastError());
 }
 
