@@ -255,37 +255,62 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
 }
 
 // ------------------------------------------------------------ tiled path
-// FP32 only (the FP64 path keeps the reference's drop rules).  Work item:
-// whole cells [cell_begin, cell_end) of one column, i.e. the rectangle of
-// angular rows R0 .. R0+M-1 times all nij spatial nodes.  The scattering of the
-// item is the product Y[m][ij] = sum_c W[R0+m][c] X[c][ij] over all Nth angular
-// nodes of the column; it runs from shared memory with 4 x 4 register tiles
-// (16 FMAs per two 16-byte loads).  The epilogue adds extinction, streaming
-// and face terms and writes y in global order.
+// Work item: whole cells [cell_begin, cell_end) of one column, i.e. the
+// rectangle of angular rows R0 .. R0+M-1 times all nij spatial nodes.  The
+// scattering of the item is the product Y[m][ij] = sum_c W[R0+m][c] X[c][ij]
+// over all Nth angular nodes of the column; it runs from shared memory with
+// 4 x 4 register tiles (16 FMAs per eight loaded values).  The epilogue adds
+// extinction, streaming and face terms and writes y in global order.
 // The inflow face fluxes of the item's elements are factorised per coupling
 // (T[jj][r] = sum_a Et[a][r] x_nbr[jj][a], then sum_jj Es[jj][q] T[jj][r]) and
 // accumulated into Fy before the epilogue; T and Fy reuse the W region.
 // Shared memory: Xs[Nth][nijp] | WsT[Nth][Mp] (later T | Fy[Mp][nijp]) |
 // Ys[Mp][nijp] | cell tables.
+//
+// FP64 (kParity) keeps the reference's drop rules without per-term tests on
+// the common path:
+//  * scattering: W's diagonal is left out of the product, and each spatial
+//    node has a class computed on the host with the exact FP64 test: every
+//    nonzero off-diagonal term kept (use Y), none kept (0), or mixed (the
+//    per-term loop with the FP32-prefiltered test); the diagonal joins the
+//    extinction term before its test (rt/preconditioner_matrix.py:450-495);
+//  * faces: a coupling whose dropped terms (|dcoeff Es Et| <= 1e-15) are
+//    exactly the products with a set of Es entries or a set of Et entries
+//    (round-off-sized mortar entries) uses cleaned copies of dcoeff*Es and
+//    Et with those entries zeroed, so the factorised flux sums exactly the
+//    kept terms; any other coupling is summed term by term with the test
+//    (rt/boundary_convection_matrix.py:258-524).
 struct TileItem {
     int col, cell_begin, cell_end, row0;
     int cpl_begin, cpl_end;   // entries of the item's couplings
-    int tsz;                  // floats of T (padded to 4)
-    int wcap;                 // floats of the W region
+    int tsz;                  // values of T (padded to 4)
+    int wcap;                 // values of the W region
     int ttot, ctot;           // work items of the two flux phases (ctot: boundary nodes x rows)
 };
 
 // One coupling of a tiled item: where its neighbour line is, its mortars,
-// and its offsets in the two flux phases.
+// and its offsets in the two flux phases.  FP64: es and et index the cleaned
+// tables (dcoeff*Es and Et); k is the coupling, tested marks a coupling summed
+// term by term.
 struct TileCpl {
     int64_t base;             // neighbour line: x[base + jj*stride + a]
     int rowloc, nth, toff, coff;
     int m1, nt1, n0, face;
     int stride, es, et;
     float dc;
+    int k, tested;
 };
 constexpr int kMaxItemCpl = 96;
 constexpr int kMaxItemCells = 128;
+
+// Host-built tables of the FP64 tiled path.
+template <typename T>
+struct TileParity {
+    const uint8_t* scls = nullptr;   // per spatial node: 0 no, 1 every, 2 some off-diagonal scattering term kept
+    const T* mortc = nullptr;        // cleaned dcoeff*Es and Et per coupling
+    const float* mortf = nullptr;    // FP32 copy of the mortars (tested couplings)
+    const float* Wf = nullptr;       // FP32 copy of W (mixed nodes)
+};
 
 // f-th node on the boundary of an nx x ny node grid, going around (j = 0 row,
 // i = nx-1 column, j = ny-1 row, i = 0 column), each node once
@@ -309,14 +334,39 @@ __host__ __device__ __forceinline__ int boundary_nodes(int nx, int ny) {
     return (nx == 1 || ny == 1) ? nx * ny : 2 * (nx + ny) - 4;
 }
 
+// four consecutive values from 16-byte-aligned shared memory
+__device__ __forceinline__ void load4(const float* p, float o[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+}
+__device__ __forceinline__ void load4(const double* p, double o[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+}
+__device__ __forceinline__ void store4(float* p, const float v[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void store4(double* p, const double v[4]) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+
+template <typename T, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
-apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__ items,
-                   const TileCpl* __restrict__ cpl_ent, const float* __restrict__ x, float* __restrict__ y) {
-    extern __shared__ float4 smt4[];
+apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileItem* __restrict__ items,
+                   const TileCpl* __restrict__ cpl_ent, const T* __restrict__ x, T* __restrict__ y) {
+    extern __shared__ double2 smt4[];
     __shared__ TileCpl sc[kMaxItemCpl];
     __shared__ int4 s_el[kMaxItemCells];      // per item cell: first entry, end entry, local row, nth
     __shared__ int s_po[kMaxItemCells + 1];   // prefix of boundary nodes x nth
-    float* smt = reinterpret_cast<float*>(smt4);
+    T* smt = reinterpret_cast<T*>(smt4);
     const TileItem it = items[blockIdx.x];
     const int ci = it.col;
     if (v.skip && v.skip[ci]) return;
@@ -330,11 +380,11 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
         return m;
     }();
     const int Mp = (M + 3) & ~3;
-    float* Xs = smt;                                  // [Nth][nijp]
-    float* WsT = Xs + (size_t)Nth * nijp;             // [Nth][Mp]
-    float* Ys = WsT + (size_t)it.wcap;                // [Mp][nijp]
-    float* Tb = WsT;                                  // after the product: T
-    float* Fy = WsT + it.tsz;                         //                    Fy[Mp][nijp]
+    T* Xs = smt;                                  // [Nth][nijp]
+    T* WsT = Xs + (size_t)Nth * nijp;             // [Nth][Mp]
+    T* Ys = WsT + (size_t)it.wcap;                // [Mp][nijp]
+    T* Tb = WsT;                                  // after the product: T
+    T* Fy = WsT + it.tsz;                         //                    Fy[Mp][nijp]
     int* cbeg = reinterpret_cast<int*>(Ys + (size_t)Mp * nijp);   // [ncell+1] local DOF start
     int* crow = cbeg + ncell + 1;                                  // [ncell] first row
     if (threadIdx.x == 0) {
@@ -347,21 +397,20 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
         }
         cbeg[ncell] = off;
         int eb = 0, po = 0;
-        const int nb = boundary_nodes(C.nx, C.ny);
         for (int k = it.cell_begin; k < it.cell_end; ++k) {
             const ElemDev E = v.elems[C.elem_begin + k];
             const int nc = E.cpl_end - E.cpl_begin;
             s_el[k - it.cell_begin] = make_int4(eb, eb + nc, E.row - it.row0, E.nth);
             s_po[k - it.cell_begin] = po;
             eb += nc;
-            po += nb * E.nth;
+            po += boundary_nodes(C.nx, C.ny) * E.nth;
         }
         s_po[it.cell_end - it.cell_begin] = po;
     }
     const int nent = it.cpl_end - it.cpl_begin;
     for (int q = threadIdx.x; q < nent; q += blockDim.x) sc[q] = cpl_ent[it.cpl_begin + q];
     __syncthreads();
-    const float* xc = x + C.dof_off;
+    const T* xc = x + C.dof_off;
     // stage x transposed: Xs[row][ij]; pad columns are zero (d grows per
     // thread, so the cell index k only moves forward)
     {
@@ -375,12 +424,14 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
     }
     if (nijp != nij)
         for (int t = threadIdx.x; t < Nth * (nijp - nij); t += blockDim.x)
-            Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = 0.f;
+            Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = T(0);
+    const T* Wg = v.W + v.W_off[C.sig];
     if (fl.scat) {
-        const float* Wg = v.W + v.W_off[C.sig];
         for (int t = threadIdx.x; t < Nth * Mp; t += blockDim.x) {
             const int c = t / Mp, m = t % Mp;
-            WsT[t] = m < M ? __ldg(Wg + (int64_t)(it.row0 + m) * Nth + c) : 0.f;
+            // FP64: the diagonal joins the extinction term in the epilogue
+            const bool use = m < M && !(kParity && c == it.row0 + m);
+            WsT[t] = use ? __ldg(Wg + (int64_t)(it.row0 + m) * Nth + c) : T(0);
         }
     }
     __syncthreads();
@@ -388,32 +439,29 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
         const int tm = Mp / 4, tn = nijp / 4;
         for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
             const int m0 = 4 * (tile / tn), j0 = 4 * (tile % tn);
-            float acc[4][4];
+            T acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+                for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
 #pragma unroll 4
             for (int c = 0; c < Nth; ++c) {
-                const float4 w = *reinterpret_cast<const float4*>(WsT + c * Mp + m0);
-                const float4 xv = *reinterpret_cast<const float4*>(Xs + c * nijp + j0);
-                const float wv[4] = {w.x, w.y, w.z, w.w};
-                const float xa[4] = {xv.x, xv.y, xv.z, xv.w};
+                T wv[4], xa[4];
+                load4(WsT + c * Mp + m0, wv);
+                load4(Xs + c * nijp + j0, xa);
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(wv[i], xa[j], acc[i][j]);
+                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
             }
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-                *reinterpret_cast<float4*>(Ys + (m0 + i) * nijp + j0) =
-                    make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+            for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
         }
     }
     __syncthreads();
     // inflow face fluxes of the item's elements into Fy (the W region is free)
     if (fl.bc) {
-        for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = 0.f;
+        for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = T(0);
         // T[jj][r] of every coupling, flattened over (coupling, jj, r); t
         // grows per thread, so the coupling index only moves forward
         {
@@ -421,11 +469,12 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
             for (int t = threadIdx.x; t < it.ttot; t += blockDim.x) {
                 while (t >= sc[c].toff + sc[c].m1 * sc[c].nth) ++c;
                 const TileCpl& en = sc[c];
+                if (kParity && en.tested) continue;   // summed term by term below
                 const int q = t - en.toff, jj = q / en.nth, r = q % en.nth;
-                const float* Et = v.mort + en.et;
-                const float* xl = x + en.base + (int64_t)jj * en.stride;
-                float acc = 0.f;
-                for (int a = 0; a < en.nt1; ++a) acc = fmaf(Et[a * en.nth + r], xl[a], acc);
+                const T* Et = (kParity ? par.mortc : v.mort) + en.et;
+                const T* xl = x + en.base + (int64_t)jj * en.stride;
+                T acc = T(0);
+                for (int a = 0; a < en.nt1; ++a) acc = fma(Et[a * en.nth + r], xl[a], acc);
                 Tb[t] = acc;
             }
         }
@@ -433,7 +482,6 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
         // one thread per (boundary node, row): the element's couplings on the
         // node's faces in a fixed order, so the sum is deterministic
         {
-            const int nb = boundary_nodes(C.nx, C.ny);
             int k = 0;
             for (int t = threadIdx.x; t < it.ctot; t += blockDim.x) {
                 while (t >= s_po[k + 1]) ++k;
@@ -441,7 +489,7 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
                 const int f = (t - s_po[k]) / el.w, r = (t - s_po[k]) % el.w;
                 int i, j;
                 boundary_node(f, C.nx, C.ny, i, j);
-                float acc = 0.f;
+                T acc = T(0);
                 for (int c = el.x; c < el.y; ++c) {
                     const TileCpl& en = sc[c];
                     const int F = en.face;
@@ -449,22 +497,54 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
                                     (F == 3 && j == 0);
                     if (!on) continue;
                     const int q = (F % 2 == 0) ? j : i;
-                    const float* Es = v.mort + en.es;
-                    float sacc = 0.f;
-                    for (int jj = 0; jj < en.m1; ++jj)
-                        sacc = fmaf(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
-                    acc = fmaf(en.dc, sacc, acc);
+                    if constexpr (kParity) {
+                        if (en.tested) {
+                            // keep dcoeff*Es*Et iff |.| > 1e-15, tested in FP32 with
+                            // an FP64 fallback within 1e-6 of the threshold
+                            const CplDev cp = v.cpls[en.k];
+                            const T* Es = v.mort + cp.es;
+                            const T* Et = v.mort + cp.et;
+                            const T dc = v.cplc[en.k];
+                            const float hi = 1.e-15f * (1.f + 1.e-6f), lo = 1.e-15f * (1.f - 1.e-6f);
+                            for (int jj = 0; jj < en.m1; ++jj) {
+                                const T des = dc * Es[jj * en.n0 + q];
+                                const float fdes = fabsf((float)des);
+                                const T* xl = x + en.base + (int64_t)jj * en.stride;
+                                T s = T(0);
+                                for (int a = 0; a < en.nt1; ++a) {
+                                    const T et = Et[a * en.nth + r];
+                                    const float pf = fdes * fabsf(par.mortf[cp.et + a * en.nth + r]);
+                                    bool keep = pf > hi;
+                                    if (!keep && pf >= lo) keep = tabs(des * et) > T(kBcTol);
+                                    s = fma(keep ? et : T(0), xl[a], s);
+                                }
+                                acc += des * s;
+                            }
+                        } else {
+                            const T* Es = par.mortc + en.es;
+                            T sacc = T(0);
+                            for (int jj = 0; jj < en.m1; ++jj)
+                                sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+                            acc += sacc;
+                        }
+                    } else {
+                        const T* Es = v.mort + en.es;
+                        T sacc = T(0);
+                        for (int jj = 0; jj < en.m1; ++jj)
+                            sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+                        acc = fma(T(en.dc), sacc, acc);
+                    }
                 }
-                (void)nb;
                 Fy[(el.z + r) * nijp + i * C.ny + j] = acc;
             }
         }
         __syncthreads();
     }
-    const float dxdy8 = v.colc[ci];
-    const float* Gx = v.G + gofs(C.nx);
-    const float* Gy = v.G + gofs(C.ny);
-    float* yc = y + C.dof_off;
+    const T small = T(kSmall);
+    const T dxdy8 = v.colc[ci];
+    const T* Gx = v.G + gofs(C.nx);
+    const T* Gy = v.G + gofs(C.ny);
+    T* yc = y + C.dof_off;
     const int d0 = cbeg[it.cell_begin], d1 = cbeg[it.cell_end];
     int k = it.cell_begin;
     for (int d = d0 + threadIdx.x; d < d1; d += blockDim.x) {
@@ -475,27 +555,57 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
         const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
         const ElemDev E = v.elems[e];
         if (fl.mask_rows && bdry_node(E.flags >> 4, i, j, C.nx, C.ny)) {
-            yc[d] = 0.f;
+            yc[d] = T(0);
             continue;
         }
         const int R = crow[k] + r;
-        const float* A = v.ang + E.ang;
-        const float xself = Xs[R * nijp + ij];
+        const T* A = v.ang + E.ang;
+        const T xself = Xs[R * nijp + ij];
         const int node = C.node_off + ij;
-        const float mterm = v.econst[4 * e] * A[r] * v.kw[node];
-        float acc = 0.f;
-        if (fl.scat) acc = -dxdy8 * v.sw[node] * Ys[(R - it.row0) * nijp + ij];
-        if (fl.mass) acc += mterm * xself;
+        const T mterm = v.econst[4 * e] * A[r] * v.kw[node];
+        T acc = T(0);
+        if constexpr (kParity) {
+            if (fl.scat) {
+                const T swv = v.sw[node];
+                const T cw = dxdy8 * swv;
+                const int cls = par.scls[node];
+                T s = T(0);
+                if (cls == 1) {
+                    s = Ys[(R - it.row0) * nijp + ij];
+                } else if (cls == 2) {
+                    // some terms kept, some dropped: test each one
+                    const bool skip_cross = !(tabs(swv) > small);
+                    const int c0 = skip_cross ? crow[k] : 0;
+                    const int c1 = skip_cross ? crow[k] + nth : Nth;
+                    const float cwf = fabsf((float)cw);
+                    const float hi = 1.e-14f * (1.f + 1.e-6f), lo = 1.e-14f * (1.f - 1.e-6f);
+                    const float* Wf = par.Wf + v.W_off[C.sig];
+                    for (int c = c0; c < c1; ++c) {
+                        const T wv = Wg[(int64_t)R * Nth + c];
+                        const float pf = cwf * fabsf(Wf[(int64_t)R * Nth + c]);
+                        bool keep = pf > hi;
+                        if (!keep && pf >= lo) keep = tabs(cw * wv) > small;
+                        s = fma(keep && c != R ? wv : T(0), Xs[c * nijp + ij], s);
+                    }
+                }
+                const T vd = (fl.merged ? mterm : T(0)) - cw * Wg[(int64_t)R * Nth + R];
+                acc = -cw * s + (tabs(vd) > small ? vd : T(0)) * xself;
+            }
+            if (fl.mass && !fl.merged) acc += mterm * xself;
+        } else {
+            if (fl.scat) acc = -dxdy8 * v.sw[node] * Ys[(R - it.row0) * nijp + ij];
+            if (fl.mass) acc += mterm * xself;
+        }
         if (fl.ic) {
-            const float* xr = Xs + R * nijp;
-            float t1 = 0.f, t2 = 0.f;
-            const float* gy = Gy + j * C.ny;
+            const T* xr = Xs + R * nijp;
+            T t1 = T(0), t2 = T(0);
+            const T* gy = Gy + j * C.ny;
             for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
-            const float* gx = Gx + i * C.nx;
+            const T* gx = Gx + i * C.nx;
             for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * xr[ii * C.ny + j];
-            const float ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
-                             v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
-            acc += fl.ic_sign * ic;
+            const T ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
+                         v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
+            acc += T(fl.ic_sign) * ic;
         }
         if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
             acc += Fy[(R - it.row0) * nijp + ij];
@@ -505,9 +615,10 @@ apply_tiled_kernel(OpView<float> v, uint32_t flags, const TileItem* __restrict__
                 const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
                                 (F == 3 && j == 0);
                 if (!on) continue;
-                const float dc = (F % 2 == 0) ? v.econst[4 * e + 2] : v.econst[4 * e + 1];
-                const float w = (F % 2 == 0) ? v.lglw[C.ny * kMaxNodes + j] : v.lglw[C.nx * kMaxNodes + i];
-                acc += dc * w * A[r] * A[(3 + F) * nth + r] * xself;
+                const T dc = (F % 2 == 0) ? v.econst[4 * e + 2] : v.econst[4 * e + 1];
+                const T w = (F % 2 == 0) ? v.lglw[C.ny * kMaxNodes + j] : v.lglw[C.nx * kMaxNodes + i];
+                const T val = dc * w * A[r] * A[(3 + F) * nth + r];
+                if (!kParity || tabs(val) > T(kBcTol)) acc += val * xself;
             }
         }
         yc[d] = acc;
@@ -658,34 +769,189 @@ struct TuneRecord {
     int ns[kNumTuneCaps];
 };
 
+// Tables of the FP64 tiled path (drop rules resolved on the host): the
+// scattering class of every spatial node and the cleaned mortar products of
+// every coupling.
+struct ParityTables {
+    uint8_t* d_scls = nullptr;
+    double* d_mortc = nullptr;
+    std::vector<int> esc, etc;     // per coupling: offsets of dcoeff*Es and Et in the cleaned table
+    std::vector<char> tested;      // per coupling: summed term by term
+    int64_t nodes[3] = {0, 0, 0};  // nodes per scattering class
+    int64_t ntested = 0;
+};
+
 struct ApplyPlan {
     ApplyGroup g[2];            // 0: input and W staged; 1: input staged, W read through L2
     int32_t* d_slow = nullptr;
     int nslow = 0;
-    TileItem* d_tiles = nullptr;   // FP32: tiled items
+    TileItem* d_tiles = nullptr;   // tiled items
     TileCpl* d_tile_cpl = nullptr; // their coupling entries
     int ntiles = 0;
     size_t tile_smem = 0;
+    const ParityTables* par = nullptr;   // FP64 tiled path
+    bool own_par = false;
     std::vector<TuneRecord> tuning;
     std::vector<void*> allocs;
 };
+
+static void free_parity(const ParityTables* pt) {
+    if (!pt) return;
+    cudaFree(pt->d_scls);
+    cudaFree(pt->d_mortc);
+    delete pt;
+}
+
+// Resolves the FP64 drop rules of the tiled path on the host, with the same
+// FP64 products and comparisons the per-term path makes.
+//  * node class: |fl(cw w)| grows with |w|, so the smallest and largest
+//    nonzero off-diagonal |W| entries decide whether every, no or some
+//    scattering term of the node is kept (cross-cell terms only where
+//    |wx wy sigma| > 1e-14, rt/preconditioner_matrix.py:450-495);
+//  * coupling: the terms dropped by |dcoeff Es Et| <= 1e-15 must be exactly
+//    the products with a set of Es entries or a set of Et entries; then those
+//    entries are zeroed in copies of dcoeff*Es and Et
+//    (rt/boundary_convection_matrix.py:258-524).
+static ParityTables* build_parity(const rtg_handle* h) {
+    const HostTables& t = h->host;
+    ParityTables* pt = new ParityTables();
+    std::vector<uint8_t> scls((size_t)std::max(t.nnodes, 1), 0);
+    for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
+        const ColDev& C = t.cols[ci];
+        const int Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
+        const double* W = t.W.data() + t.W_off[C.sig];
+        double wmin = 0., wmax = 0.;   // nonzero off-diagonal |W|, whole column
+        std::vector<double> cmax(ncell, 0.);   // largest own-cell off-diagonal |W| per cell
+        std::vector<int> rcell(Nth, 0);
+        for (int k = 0; k < ncell; ++k) {
+            const ElemDev& E = t.elems[C.elem_begin + k];
+            for (int r = 0; r < E.nth; ++r) rcell[E.row + r] = k;
+        }
+        for (int R = 0; R < Nth; ++R)
+            for (int c = 0; c < Nth; ++c) {
+                const double a = std::fabs(W[(int64_t)R * Nth + c]);
+                if (c == R || a == 0.) continue;
+                wmin = (wmin == 0.) ? a : std::min(wmin, a);
+                wmax = std::max(wmax, a);
+                if (rcell[R] == rcell[c]) cmax[rcell[R]] = std::max(cmax[rcell[R]], a);
+            }
+        const double dxdy8 = t.colc[ci];
+        for (int ij = 0; ij < C.nx * C.ny; ++ij) {
+            const double swv = t.sw[C.node_off + ij];
+            const double cw = dxdy8 * swv;
+            uint8_t cls;
+            if (!(std::fabs(swv) > kSmall)) {
+                // cross-cell terms left out: the per-term loop when any own-cell term is kept
+                bool any = false;
+                for (int k = 0; k < ncell; ++k) any |= std::fabs(cw * cmax[k]) > kSmall;
+                cls = any ? 2 : 0;
+            } else if (wmax == 0.) {
+                cls = 0;
+            } else if (std::fabs(cw * wmin) > kSmall) {
+                cls = 1;
+            } else if (!(std::fabs(cw * wmax) > kSmall)) {
+                cls = 0;
+            } else {
+                cls = 2;
+            }
+            scls[C.node_off + ij] = cls;
+            ++pt->nodes[cls];
+        }
+    }
+    const int ncpl = (int)t.cpls.size();
+    std::vector<double> mortc;
+    pt->esc.assign(ncpl, 0);
+    pt->etc.assign(ncpl, 0);
+    pt->tested.assign(ncpl, 0);
+    std::map<std::pair<int, std::vector<char>>, int> et_seen;   // (Et offset, zeroed entries) -> offset
+    for (int e = 0; e < (int)t.elems.size(); ++e) {
+        const ElemDev& E = t.elems[e];
+        const ColDev& C = t.cols[E.col];
+        for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+            const CplDev& cp = t.cpls[k];
+            const CplGeo& g = t.cgeo[k];
+            const int n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+            const int nes = g.m1 * n0, net = g.nth1 * E.nth;
+            const double dc = t.cplc[k];
+            std::vector<double> des(nes);
+            for (int q = 0; q < nes; ++q) des[q] = dc * t.mort[cp.es + q];
+            const double* et = t.mort.data() + cp.et;
+            // an entry is removable when every product it takes part in is dropped
+            std::vector<char> esz(nes, 0), etz(net, 0);
+            std::vector<char> es_any(nes, 0), et_any(net, 0), es_kept(nes, 0), et_kept(net, 0);
+            for (int q = 0; q < nes; ++q) {
+                if (des[q] == 0.) continue;
+                for (int b = 0; b < net; ++b) {
+                    if (et[b] == 0.) continue;
+                    const bool kept = std::fabs(des[q] * et[b]) > kBcTol;
+                    es_any[q] = et_any[b] = 1;
+                    if (kept) es_kept[q] = et_kept[b] = 1;
+                }
+            }
+            for (int q = 0; q < nes; ++q) esz[q] = es_any[q] && !es_kept[q];
+            for (int b = 0; b < net; ++b) etz[b] = et_any[b] && !et_kept[b];
+            bool separable = true;
+            for (int q = 0; q < nes && separable; ++q) {
+                if (des[q] == 0.) continue;
+                for (int b = 0; b < net; ++b) {
+                    if (et[b] == 0.) continue;
+                    const bool dropped = !(std::fabs(des[q] * et[b]) > kBcTol);
+                    if (dropped != (esz[q] || etz[b])) {
+                        separable = false;
+                        break;
+                    }
+                }
+            }
+            if (!separable) {
+                pt->tested[k] = 1;
+                ++pt->ntested;
+                continue;
+            }
+            pt->esc[k] = (int)mortc.size();
+            for (int q = 0; q < nes; ++q) mortc.push_back(esz[q] ? 0. : des[q]);
+            auto key = std::make_pair((int)cp.et, etz);
+            auto f = et_seen.find(key);
+            if (f != et_seen.end()) {
+                pt->etc[k] = f->second;
+            } else {
+                pt->etc[k] = (int)mortc.size();
+                for (int b = 0; b < net; ++b) mortc.push_back(etz[b] ? 0. : et[b]);
+                et_seen.emplace(std::move(key), pt->etc[k]);
+            }
+        }
+    }
+    if (mortc.size() > (size_t)INT32_MAX) throw RtgError{RTG_ERR_ARG, "cleaned mortar table too large"};
+    try {
+        RTG_CUDA(cudaMalloc(&pt->d_scls, scls.size()));
+        RTG_CUDA(cudaMemcpy(pt->d_scls, scls.data(), scls.size(), cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMalloc(&pt->d_mortc, sizeof(double) * std::max<size_t>(mortc.size(), 1)));
+        if (!mortc.empty())
+            RTG_CUDA(cudaMemcpy(pt->d_mortc, mortc.data(), sizeof(double) * mortc.size(), cudaMemcpyHostToDevice));
+    } catch (...) {
+        free_parity(pt);
+        throw;
+    }
+    return pt;
+}
 
 // Tiled items of the FP32 path: consecutive cells of a column, at most
 // kTileRows angular rows and kTileOut outputs per item, when the column's
 // input, the item's W rows and its products fit in shared memory.
 
 
-static size_t tile_smem_bytes(int nth_col, int nij, int wcap, int M, int ncell) {
+static size_t tile_smem_bytes(size_t vsize, int nth_col, int nij, int wcap, int M, int ncell) {
     const int nijp = (nij + 3) & ~3, Mp = (M + 3) & ~3;
-    return sizeof(float) * ((size_t)nth_col * nijp + (size_t)wcap + (size_t)Mp * nijp) + sizeof(int) * (2 * ncell + 2) +
-           16;
+    return vsize * ((size_t)nth_col * nijp + (size_t)wcap + (size_t)Mp * nijp) + sizeof(int) * (2 * ncell + 2) + 16;
 }
 
-// cap: per column, the largest number of angular rows of a tiled item (FP32);
-// include: per column, whether the plan covers it (null: every column).
+// cap: per column, the largest number of angular rows of a tiled item;
+// include: per column, whether the plan covers it (null: every column);
+// par: the FP64 tiled path's tables (null: FP64 columns use the per-output
+// kernels).
 template <typename T>
 static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = nullptr,
-                            const std::vector<char>* include = nullptr, int chunk64 = kChunk64) {
+                            const std::vector<char>* include = nullptr, int chunk64 = kChunk64,
+                            const ParityTables* par = nullptr) {
     const HostTables& t = h->host;
     constexpr bool parity = sizeof(T) == 8;
     ApplyPlan* p = new ApplyPlan();
@@ -700,7 +966,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         const int ncell = C.elem_end - C.elem_begin;
         const int nij = C.nx * C.ny;
         const int rows_cap = cap ? (*cap)[ci] : kTileRows;
-        if (!parity && ncell <= kMaxCellsStaged) {
+        if ((!parity || par) && ncell <= kMaxCellsStaged) {
             // split the column into items of whole cells
             std::vector<TileItem> its;
             bool fits = true;
@@ -740,9 +1006,11 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                         tc.face = cp.face;
                         tc.n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
                         tc.stride = g.stride;
-                        tc.es = cp.es;
-                        tc.et = cp.et;
+                        tc.es = parity ? par->esc[kk] : cp.es;
+                        tc.et = parity ? par->etc[kk] : cp.et;
                         tc.dc = (float)t.cplc[kk];
+                        tc.k = kk;
+                        tc.tested = parity ? par->tested[kk] : 0;
                         en.push_back(tc);
                         tsz += g.m1 * E.nth;
                         csz += tc.n0 * E.nth;
@@ -754,13 +1022,13 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                     ti.ctot += boundary_nodes(C.nx, C.ny) * t.elems[C.elem_begin + q].nth;
                 (void)csz;
                 const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
-                // Fy and Ys are read and written as float4: keep every region
-                // a multiple of 4 floats from the 16-byte-aligned base
+                // Fy and Ys are read and written four values at a time: keep
+                // every region a multiple of 4 values from the aligned base
                 ti.tsz = (tsz + 3) & ~3;
                 ti.wcap = std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
                 if ((ti.wcap & 3) || (ti.tsz & 3) || (nijp & 3))
                     throw RtgError{RTG_ERR_ARG, "tiled apply: unaligned shared-memory region"};
-                const size_t b = tile_smem_bytes(C.nth_col, nij, ti.wcap, M, ncell);
+                const size_t b = tile_smem_bytes(sizeof(T), C.nth_col, nij, ti.wcap, M, ncell);
                 if (b > kSmemBudget) fits = false;
                 bytes.push_back(b);
                 ents.push_back(std::move(en));
@@ -826,6 +1094,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         tv.push_back(ti);
     }
     p->ntiles = (int)tv.size();
+    p->par = parity ? par : nullptr;
     p->d_tiles = (TileItem*)up(tv.data(), sizeof(TileItem) * tv.size());
     p->d_tile_cpl = (TileCpl*)up(ent.data(), sizeof(TileCpl) * ent.size());
     return p;
@@ -834,6 +1103,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
 static void free_plan(ApplyPlan* p) {
     if (!p) return;
     for (void* d : p->allocs) cudaFree(d);
+    if (p->own_par) free_parity(p->par);
     delete p;
 }
 
@@ -841,7 +1111,7 @@ template <typename T>
 static void set_plan_attributes(const ApplyPlan* p) {
     constexpr bool f64 = sizeof(T) == 8;
     raise_smem_limit((const void*)apply_col_kernel<T, T, f64>, std::max(p->g[0].smem, p->g[1].smem));
-    if (!f64) raise_smem_limit((const void*)apply_tiled_kernel, p->tile_smem);
+    if (p->ntiles) raise_smem_limit((const void*)apply_tiled_kernel<T, f64>, p->tile_smem);
 }
 
 template <typename T>
@@ -849,14 +1119,21 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
                      T* y, cudaStream_t s) {
     constexpr bool f64 = sizeof(T) == 8;
     RTG_LAUNCHED("a kernel before the apply");
-    if constexpr (!f64) {
+    {
         if (plan->ntiles) {
-            apply_tiled_kernel<<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
-                v32, flags, plan->d_tiles, plan->d_tile_cpl, (const float*)x, (float*)y);
+            TileParity<T> tp{};
+            if constexpr (f64) {
+                tp.scls = plan->par->d_scls;
+                tp.mortc = plan->par->d_mortc;
+                tp.mortf = v32.mort;
+                tp.Wf = v32.W;
+            }
+            apply_tiled_kernel<T, f64><<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
+                v, tp, flags, plan->d_tiles, plan->d_tile_cpl, x, y);
             const cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 cudaFuncAttributes fa{};
-                cudaFuncGetAttributes(&fa, apply_tiled_kernel);
+                cudaFuncGetAttributes(&fa, apply_tiled_kernel<T, f64>);
                 throw RtgError{RTG_ERR_CUDA, "launch of apply_tiled_kernel (items " + std::to_string(plan->ntiles) +
                                                  ", dynamic smem " + std::to_string(plan->tile_smem) + ", max dynamic " +
                                                  std::to_string(fa.maxDynamicSharedSizeBytes) + ", static " +
@@ -992,14 +1269,18 @@ static ApplyPlan* tune_plan32(rtg_handle* h, cudaStream_t s) {
     return tuned;
 }
 
-// FP64 apply: the whole apply timed with 128, 256 and 512 outputs per item
-// (best of three after a warm-up); the fastest plan is kept.
+// FP64 apply: columns that fit in shared memory run the tiled kernel with the
+// drop rules resolved on the host (build_parity); the whole apply is timed
+// with 16, 32 and 64 angular rows per tiled item (best of three after a
+// warm-up) and the fastest plan is kept.
 static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
     const int64_t N = h->host.ndof;
+    const int nc = (int)h->host.cols.size();
     double *x = nullptr, *y = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ApplyPlan* best = nullptr;
     float tbest = 1e30f;
+    ParityTables* par = build_parity(h);
     auto release = [&] {
         if (x) cudaFree(x);
         if (y) cudaFree(y);
@@ -1012,8 +1293,9 @@ static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
         RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s));
         RTG_CUDA(cudaEventCreate(&e0));
         RTG_CUDA(cudaEventCreate(&e1));
-        for (int chunk : {128, 256, 512}) {
-            ApplyPlan* p = make_plan<double>(h, nullptr, nullptr, chunk);
+        for (int rows : {16, 32, 64}) {
+            std::vector<int> cap(nc, rows);
+            ApplyPlan* p = make_plan<double>(h, &cap, nullptr, kChunk64, par);
             float tt = 1e30f;
             try {
                 set_plan_attributes<double>(p);
@@ -1041,10 +1323,12 @@ static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
         }
     } catch (...) {
         free_plan(best);
+        free_parity(par);
         release();
         throw;
     }
     release();
+    best->own_par = true;
     return best;
 }
 
