@@ -211,12 +211,13 @@ int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stre
  * and FP64); builds the sweep if needed.  Any output may be NULL. */
 int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_entries, void* stream);
 /* One sweep as rtg_precondition, recording for every element e
- * trace[8e .. 8e+7] = {claimed, upwind inputs ready, published, CTA, upwind
- * lines loaded, couplings formed, values stored, fence passed} (device array
- * of 8*nelem uint64, times in GPU global-timer nanoseconds) and, when
- * level (host, nelem int32) is not NULL, each element's wavefront level.  A
- * profiling aid: the sweep's cost is its level count times the per-level
- * latency these timestamps resolve. */
+ * trace[8e .. 8e+7] = {claimed, independent work done, published (GPU
+ * global-timer nanoseconds), CTA, then SM clock cycles spent waiting for the
+ * upwind face lines, forming T = Et z_upwind, forming the face couplings, and
+ * applying the face columns of the block inverse with the stores} (device
+ * array of 8*nelem uint64) and, when level (host, nelem int32) is not NULL,
+ * each element's wavefront level.  A profiling aid: the sweep's cost is its
+ * level count times the per-level latency these records resolve. */
 int rtg_sweep_trace(rtg_handle* h, int prec, const void* r, void* z, uint64_t* trace, int32_t* level,
                     void* stream);
 /* out_beta = (dx dy dth / 8) wx_i wy_j wth_a * fvals_beta (device doubles). */

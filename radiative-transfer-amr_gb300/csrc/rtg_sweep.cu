@@ -15,7 +15,12 @@
 // neighbour" graph over all angular cells at once; where the graph has a
 // cycle (cells that lie in no single quadrant couple on every face) the
 // couplings that close it are dropped from P.  One persistent launch applies
-// P^{-1}: CTAs take elements in level order and wait on per-element flags.
+// P^{-1}: CTAs take elements in level order and wait on the upwind values
+// themselves (z is filled with a sentinel first).  An element whose upwind
+// map G_e = -B_e C_e (built once, FP64 with an FP32 copy) fits in shared
+// memory computes z_e = B_e rin_e + G_e z_upwind in one phase after its
+// inputs arrive; the others form the face couplings in factorised form
+// (T = Et z, c = Es T) and apply the face columns of B_e.
 // Applying P^{-1} is exact for the transport part of an acyclic mesh; the
 // cross-cell scattering is left to the Krylov iteration.
 #include <algorithm>
@@ -200,11 +205,12 @@ struct Sentinel<double> {
     static constexpr U bits = 0x7FF4BADBADBADBADull;
 };
 
+__device__ __forceinline__ float from_bits_f(unsigned int u) { return __uint_as_float(u); }
+__device__ __forceinline__ double from_bits_f(unsigned long long u) { return __longlong_as_double((long long)u); }
+
 template <typename T>
 __device__ __forceinline__ T from_bits(typename Sentinel<T>::U u) {
-    T v;
-    memcpy(&v, &u, sizeof(T));
-    return v;
+    return from_bits_f(u);
 }
 
 // Relaxed GPU-scope accesses: morally strong, so a reader racing with the
@@ -270,6 +276,19 @@ __global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z) {
     }
 }
 
+// Asynchronous global -> shared copies (cp.async): every copy of a staging
+// loop is in flight at once and no register holds the data.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+template <int kBytes>
+__device__ __forceinline__ void cp_async_small(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(kBytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -280,18 +299,37 @@ __device__ __forceinline__ bool on_face(int F, int i, int j, int nx, int ny) {
     return (F == 0 && i == nx - 1) || (F == 1 && j == ny - 1) || (F == 2 && i == 0) || (F == 3 && j == 0);
 }
 
+// Upwind maps of the elements that take the one-phase path: for element e
+// with nup upwind values (the facing node lines of its active couplings, in
+// coupling order, then jj, then a), G_e = -B_e C_e maps them to the element's
+// values: z_e = B_e rin_e + G_e z_upwind.  G is stored [u][l] (l = ij*nth + r),
+// each element's block starting on a 16-byte boundary.  Shared memory of
+// the path (after rhs and zpre): upwind values [nup, padded to 16 bytes] |
+// G_e [nup*nloc, padded] | B_e [nth*nn*nn].
 template <typename T>
-__global__ void __launch_bounds__(kSweepThreads)
+struct UpwindMap {
+    const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
+    const int32_t* nup = nullptr;    // per element: upwind values
+    const int64_t* goff = nullptr;   // per element: first entry of G_e
+    const int64_t* uoff = nullptr;   // per element: first entry of its upwind index list
+    const int64_t* up = nullptr;     // upwind value offsets into z
+    const T* G = nullptr;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kSweepThreads, 4)
 sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
                         const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ next,
-                        int* __restrict__ status,
+                        int* __restrict__ status, UpwindMap<T> um,
                         int rhs_cap, int bcap, int ccap, unsigned long long* __restrict__ trace) {
-    extern __shared__ unsigned char sraw[];
+    extern __shared__ __align__(16) unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);      // rin, then the couplings c (face nodes)
     T* zpre = rhs + rhs_cap;                  // B rin
     T* Bs = zpre + rhs_cap;
     T* cs = Bs + bcap;   // staged couplings: per active coupling Es | Et | upwind face line | T
+    // one-phase path: the upwind values and G_e take the place of Bs and cs
+    constexpr uint8_t kOkBit = sizeof(T) == 8 ? 2 : 1;
     __shared__ int s_idx;
     __shared__ int s_abort;
     __shared__ int s_nc;
@@ -327,6 +365,74 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         // ---- independent of the sweep: block inverse, residual, mortars
         const T* B = inv + inv_elem_off[e];
         const int bsize = nth * nn * nn;
+        if (um.ok && (um.ok[e] & kOkBit)) {
+            // ---- one-phase path: zpre = B rin and G_e staged before the wait,
+            // then z = zpre + G_e z_upwind once the upwind values arrive
+            constexpr int kVec = 16 / sizeof(T);   // values per 16-byte copy
+            const int nup = um.nup[e];
+            const int nupp = (nup + kVec - 1) / kVec * kVec;
+            const int gsz = nup * nloc, gszp = (gsz + kVec - 1) / kVec * kVec;
+            T* zl = Bs;
+            T* Gs = Bs + nupp;
+            T* Bg = Gs + gszp;
+            const T* Gg = um.G + um.goff[e];
+            const int64_t* up = um.up + um.uoff[e];
+            for (int t = threadIdx.x; t < gszp / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
+            for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bg + t, B + t);
+            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+                const int ij = l / nth;
+                rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
+            }
+            int64_t my_up = threadIdx.x < nup ? __ldg(up + threadIdx.x) : 0;
+            cp_async_wait_all();
+            __syncthreads();
+            for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
+                const int r = t / nn, ij = t % nn;
+                const T* col = Bg + r * nn * nn + ij;
+                T acc = T(0);
+#pragma unroll 4
+                for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
+                zpre[ij * nth + r] = acc;
+            }
+            long long ck0 = 0, ck1 = 0;
+            if (trace && threadIdx.x == 0) {
+                trace[kTr * e + 1] = globaltimer_ns();
+                ck0 = clock64();
+            }
+            for (int u = threadIdx.x; u < nup; u += blockDim.x) {
+                const int64_t o = u == threadIdx.x ? my_up : __ldg(up + u);
+                T val = T(0);
+                if (!load_published(z + o, val, status)) s_abort = 1;
+                zl[u] = val;
+            }
+            __syncthreads();
+            if (s_abort) break;
+            if (trace && threadIdx.x == 0) ck1 = clock64();
+            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+                T a0 = zpre[l], a1 = T(0), a2 = T(0), a3 = T(0);
+                const T* g = Gs + l;
+                int u = 0;
+                for (; u + 4 <= nup; u += 4) {
+                    a0 += g[(u + 0) * nloc] * zl[u + 0];
+                    a1 += g[(u + 1) * nloc] * zl[u + 1];
+                    a2 += g[(u + 2) * nloc] * zl[u + 2];
+                    a3 += g[(u + 3) * nloc] * zl[u + 3];
+                }
+                for (; u < nup; ++u) a0 += g[u * nloc] * zl[u];
+                st_relaxed(z + E.dof_off + l, (a0 + a1) + (a2 + a3));
+            }
+            __syncthreads();
+            if (trace && threadIdx.x == 0) {
+                const long long ck4 = clock64();
+                trace[kTr * e + 2] = globaltimer_ns();
+                trace[kTr * e + 3] = (unsigned long long)blockIdx.x;
+                trace[kTr * e + 4] = (unsigned long long)(ck1 - ck0);
+                trace[kTr * e + 5] = 0;
+                trace[kTr * e + 6] = 0;
+                trace[kTr * e + 7] = (unsigned long long)(ck4 - ck1);
+            }
+            continue;
+        }
         const bool staged = bsize <= bcap;
         if (staged)
             for (int t = threadIdx.x; t < bsize; t += blockDim.x) Bs[t] = __ldg(B + t);
@@ -393,7 +499,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             zpre[ij * nth + r] = acc;
         }
         // ---- couplings c on the face nodes, into rhs[ij * nth + r]
-        if (trace && threadIdx.x == 0) trace[kTr * e + 1] = globaltimer_ns();
+        long long ck0 = 0, ck1 = 0, ck2 = 0, ck3 = 0;   // phase clocks (thread 0, traced sweeps)
+        if (trace && threadIdx.x == 0) {
+            trace[kTr * e + 1] = globaltimer_ns();
+            ck0 = clock64();
+        }
         if (ncs >= 0) {
             // stage the upwind face lines as they are published (coalesced,
             // each value once; each thread waits on its own values)
@@ -411,6 +521,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             }
             __syncthreads();
             if (s_abort) break;
+            if (trace && threadIdx.x == 0) ck1 = clock64();
             // T[jj][r] = sum_a Et[a][r] zl[jj][a], all couplings at once
             {
                 int c = 0, base = 0;
@@ -432,7 +543,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 }
             }
             __syncthreads();
-            if (trace && threadIdx.x == 0) trace[kTr * e + 4] = globaltimer_ns();
+            if (trace && threadIdx.x == 0) ck2 = clock64();
             for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
                 const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
                 T acc = T(0);
@@ -480,7 +591,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         }
         __syncthreads();
         if (s_abort) break;
-        if (trace && threadIdx.x == 0) trace[kTr * e + 5] = globaltimer_ns();
+        if (trace && threadIdx.x == 0) ck3 = clock64();
         // ---- z = zpre - B c over the face columns of B
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
@@ -497,12 +608,60 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         // shared buffers before the next claim
         __syncthreads();
         if (trace && threadIdx.x == 0) {
-            const unsigned long long tn = globaltimer_ns();
-            trace[kTr * e + 2] = tn;
-            trace[kTr * e + 6] = tn;
-            trace[kTr * e + 7] = tn;
+            const long long ck4 = clock64();
+            trace[kTr * e + 2] = globaltimer_ns();
             trace[kTr * e + 3] = (unsigned long long)blockIdx.x;
+            // SM clock cycles of the phases after the independent work
+            // (staged path; on the other path the first two stay 0)
+            trace[kTr * e + 4] = (unsigned long long)(ck1 ? ck1 - ck0 : 0);
+            trace[kTr * e + 5] = (unsigned long long)(ck2 ? ck2 - ck1 : 0);
+            trace[kTr * e + 6] = (unsigned long long)(ck3 - (ck2 ? ck2 : ck0));
+            trace[kTr * e + 7] = (unsigned long long)(ck4 - ck3);
         }
+    }
+}
+
+// Builds the upwind maps G_e = -B_e C_e of the one-phase elements in FP64
+// (and their FP32 copies): entry (u, l) with u = (coupling k, jj, a) and
+// l = (ij, r) is -dcoeff_k Et_k[a][r] sum_q B_r[ij][f_q] Es_k[jj][q] over the
+// nodes f_q of coupling k's face that are not inflow-boundary nodes.  One CTA
+// per element.
+__global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restrict__ active,
+                                        const double* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
+                                        const int32_t* __restrict__ elems, const int32_t* __restrict__ nup_e,
+                                        const int64_t* __restrict__ goff, double* __restrict__ G64,
+                                        float* __restrict__ G32) {
+    const int e = elems[blockIdx.x];
+    const ElemDev E = v.elems[e];
+    const ColDev C = v.cols[E.col];
+    const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth, bm = E.flags >> 4;
+    const int nup = nup_e[e];
+    const double* B = inv + inv_elem_off[e];
+    for (int t = threadIdx.x; t < nup * nloc; t += blockDim.x) {
+        const int u = t / nloc, l = t % nloc, ij = l / nth, r = l % nth;
+        int uu = u, k = E.cpl_begin;
+        for (; k < E.cpl_end; ++k) {
+            if (!active[k]) continue;
+            const int sz = v.cgeo[k].m1 * v.cgeo[k].nth1;
+            if (uu < sz) break;
+            uu -= sz;
+        }
+        const CplGeo g = v.cgeo[k];
+        const CplDev cp = v.cpls[k];
+        const int jj = uu / g.nth1, a = uu % g.nth1;
+        const int F = cp.face;
+        const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+        const double et = v.mort[cp.et + a * nth + r];
+        double acc = 0.;
+        for (int q = 0; q < n0; ++q) {
+            const int i = (F == 0) ? C.nx - 1 : (F == 2) ? 0 : q;
+            const int j = (F == 1) ? C.ny - 1 : (F == 3) ? 0 : q;
+            if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+            acc += B[(int64_t)r * nn * nn + (int64_t)(i * C.ny + j) * nn + ij] * v.mort[cp.es + jj * n0 + q];
+        }
+        const double val = -v.cplc[k] * et * acc;
+        G64[goff[e] + t] = val;
+        G32[goff[e] + t] = (float)val;
     }
 }
 
@@ -530,6 +689,15 @@ struct Sweep {
     std::vector<void*> allocs;
     unsigned int* d_next = nullptr;      // work counter
     int* d_status = nullptr;             // RTG_ERR_TIMEOUT if a wait gave up
+    // one-phase elements (upwind maps)
+    uint8_t* d_gok = nullptr;
+    int32_t* d_gnup = nullptr;
+    int64_t *d_goff = nullptr, *d_uoff = nullptr, *d_up = nullptr;
+    double* d_G64 = nullptr;
+    float* d_G32 = nullptr;
+    int64_t gmax32 = 0, gmax64 = 0;     // largest staged region (values) per precision
+    int64_t g_entries = 0;
+    int n_onephase32 = 0, n_onephase64 = 0;
 };
 
 namespace {
@@ -689,13 +857,74 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         max_c = std::max(max_c, c);
     }
     s->max_c = max_c;
+    // ---- upwind maps of the elements whose map fits in shared memory
+    {
+        const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
+        std::vector<uint8_t> gok(ne, 0);
+        std::vector<int32_t> gnup(ne, 0), gel;
+        std::vector<int64_t> goff(ne, 0), uoff(ne, 0), up;
+        int64_t gtot = 0;
+        for (int e = 0; e < ne; ++e) {
+            const ElemDev& E = t.elems[e];
+            const ColDev& C = t.cols[E.col];
+            const int nloc = C.nx * C.ny * E.nth;
+            int64_t nup = 0;
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k)
+                if (active[k]) nup += (int64_t)t.cgeo[k].m1 * t.cgeo[k].nth1;
+            // upwind values and G_e padded to 16 bytes (4 floats), then B_e
+            const int64_t bsize = (int64_t)E.nth * C.nx * C.ny * C.nx * C.ny;
+            auto pad = [](int64_t n, int64_t q) { return (n + q - 1) / q * q; };
+            const int64_t region32 = pad(nup, 4) + pad(nup * nloc, 4) + bsize;
+            const int64_t region64 = pad(nup, 2) + pad(nup * nloc, 2) + bsize;
+            uint8_t ok = 0;
+            if (region32 * 4 + 2 * rhs_cap * 4 <= (int64_t)kSweepSmemBudget) ok |= 1;
+            if (region64 * 8 + 2 * rhs_cap * 8 <= (int64_t)kSweepSmemBudget) ok |= 2;
+            if (!ok) continue;
+            gok[e] = ok;
+            gnup[e] = (int32_t)nup;
+            goff[e] = gtot;
+            uoff[e] = (int64_t)up.size();
+            gtot += pad(nup * nloc, 4);
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                if (!active[k]) continue;
+                const CplGeo& g = t.cgeo[k];
+                for (int jj = 0; jj < g.m1; ++jj)
+                    for (int a = 0; a < g.nth1; ++a) up.push_back(g.base + (int64_t)jj * g.stride + a);
+            }
+            if (ok & 1) s->gmax32 = std::max(s->gmax32, region32), ++s->n_onephase32;
+            if (ok & 2) s->gmax64 = std::max(s->gmax64, region64), ++s->n_onephase64;
+            gel.push_back(e);
+        }
+        s->g_entries = gtot;
+        s->d_gok = sw_alloc<uint8_t>(s, ne);
+        s->d_gnup = sw_alloc<int32_t>(s, ne);
+        s->d_goff = sw_alloc<int64_t>(s, ne);
+        s->d_uoff = sw_alloc<int64_t>(s, ne);
+        s->d_up = sw_alloc<int64_t>(s, up.size());
+        s->d_G64 = sw_alloc<double>(s, gtot);
+        s->d_G32 = sw_alloc<float>(s, gtot);
+        int32_t* d_gel = sw_alloc<int32_t>(s, gel.size());
+        RTG_CUDA(cudaMemcpy(s->d_gok, gok.data(), ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_gnup, gnup.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_goff, goff.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_uoff, uoff.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
+        if (!up.empty())
+            RTG_CUDA(cudaMemcpy(s->d_up, up.data(), sizeof(int64_t) * up.size(), cudaMemcpyHostToDevice));
+        if (!gel.empty()) {
+            RTG_CUDA(cudaMemcpy(d_gel, gel.data(), sizeof(int32_t) * gel.size(), cudaMemcpyHostToDevice));
+            build_upwind_map_kernel<<<(int)gel.size(), 256, 0, st>>>(h->v64, s->d_active, s->d_inv64, s->d_inv_off,
+                                                                    d_gel, s->d_gnup, s->d_goff, s->d_G64, s->d_G32);
+            RTG_CUDA(cudaGetLastError());
+        }
+    }
     return s;
 }
 
 // z = P^{-1} r (full-length vectors; inflow-boundary entries of z are zero).
-// With trace, element e records [claim, independent work done, published,
-// cta, upwind lines loaded, couplings formed, published, published]
-// (globaltimer ns) in trace[8e .. 8e+7].
+// With trace, element e records in trace[8e .. 8e+7]: claimed, independent
+// work done, published (globaltimer ns), its CTA, then SM clock cycles of
+// the phases after that: waiting for the upwind lines, forming T, forming the
+// couplings, the face columns of B and the stores.
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip) {
     Sweep* s = get_sweep(h, st);
@@ -711,12 +940,14 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
     int& grid = f64 ? s->grid64 : s->grid32;
-    const int rhs_cap = std::max(s->max_nloc, 1);
+    const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
     if (grid == 0) {
         const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
         const int64_t fit = (int64_t)((kSweepSmemBudget - std::min(rhs_bytes, kSweepSmemBudget)) / sizeof(T));
         bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
-        smem = rhs_bytes + sizeof(T) * (size_t)bcap;
+        // the one-phase elements use the region of Bs and cs for their maps
+        const int64_t gmax = f64 ? s->gmax64 : s->gmax32;
+        smem = sizeof(T) * (size_t)(2 * rhs_cap + std::max<int64_t>((int64_t)bcap + s->max_c, gmax));
         raise_smem_limit((const void*)sweep_persistent_kernel<T>, smem);
         int per_sm = 0, dev = 0, nsm = 0;
         RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
@@ -725,9 +956,16 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
     }
+    UpwindMap<T> um;
+    um.ok = s->d_gok;
+    um.nup = s->d_gnup;
+    um.goff = s->d_goff;
+    um.uoff = s->d_uoff;
+    um.up = s->d_up;
+    um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
         v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next, s->d_status,
-        rhs_cap, bcap, (int)s->max_c, trace);
+        um, rhs_cap, bcap, (int)s->max_c, trace);
     RTG_CUDA(cudaGetLastError());
 }
 
