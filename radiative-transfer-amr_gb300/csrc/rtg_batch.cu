@@ -20,6 +20,7 @@
 // chunks.  Its frozen basis columns and correction are never read again.
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "rtg_internal.h"
@@ -45,20 +46,22 @@ __global__ void bdot_kernel(const BChunk* __restrict__ ch, const T* __restrict__
     if (done && done[c.inst]) return;
     for (int g0 = 0; g0 < k; g0 += kBGroup) {
         const int gk = min(kBGroup, k - g0);
-        double acc[kBGroup];
+        // per element and per warp in the vectors' precision (FP32 stays on
+        // the FP32 pipe), double from the per-warp sums on
+        T acc[kBGroup];
 #pragma unroll
-        for (int q = 0; q < kBGroup; ++q) acc[q] = 0.;
+        for (int q = 0; q < kBGroup; ++q) acc[q] = T(0);
         for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
-            const double wi = (double)w[i];
+            const T wi = w[i];
 #pragma unroll
             for (int q = 0; q < kBGroup; ++q)
-                if (q < gk) acc[q] += (double)V[(int64_t)(g0 + q) * ldv + i] * wi;
+                if (q < gk) acc[q] = fma(V[(int64_t)(g0 + q) * ldv + i], wi, acc[q]);
         }
 #pragma unroll
         for (int q = 0; q < kBGroup; ++q) {
-            double s = acc[q];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
+            T sw = acc[q];
+            for (int o = 16; o > 0; o >>= 1) sw += __shfl_down_sync(0xffffffffu, sw, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = (double)sw;
         }
         __syncthreads();
         if (threadIdx.x < gk) {
@@ -94,15 +97,15 @@ __global__ void breduce_kernel(const int32_t* __restrict__ cbeg, const double* _
 template <typename T>
 __global__ void baxpy_kernel(const BChunk* __restrict__ ch, T* __restrict__ w, const T* __restrict__ V, int64_t ldv,
                              int k, const double* __restrict__ h, int ldh, const int32_t* __restrict__ done) {
-    __shared__ double hs[64];
+    __shared__ T hs[64];
     const BChunk c = ch[blockIdx.x];
     if (done && done[c.inst]) return;
-    if (threadIdx.x < k) hs[threadIdx.x] = h[c.inst * ldh + threadIdx.x];
+    if (threadIdx.x < k) hs[threadIdx.x] = (T)h[c.inst * ldh + threadIdx.x];
     __syncthreads();
     for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
-        double s = (double)w[i];
-        for (int q = 0; q < k; ++q) s -= hs[q] * (double)V[(int64_t)q * ldv + i];
-        w[i] = (T)s;
+        T sv = w[i];
+        for (int q = 0; q < k; ++q) sv = fma(-hs[q], V[(int64_t)q * ldv + i], sv);
+        w[i] = sv;
     }
 }
 
@@ -116,25 +119,26 @@ __global__ void bnormalize_kernel(const BChunk* __restrict__ ch, const int32_t* 
     if (done && done[c.inst]) return;
     const double nr = sqrt(nsq[c.inst * ldn]);
     if (hcol && threadIdx.x == 0 && cbeg[c.inst] == (int)blockIdx.x) hcol[c.inst * ldh + jcol] = nr;
-    const double inv = nr > 0. ? 1. / nr : 0.;
-    for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) out[i] = (T)((double)w[i] * inv);
+    const T inv = (T)(nr > 0. ? 1. / nr : 0.);
+    for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) out[i] = w[i] * inv;
 }
 
 // x += scale[b] * sum_{q < kb[b]} y[b][q] V_q
 template <typename TV, typename TX>
 __global__ void bcombine_kernel(const BChunk* __restrict__ ch, TX* __restrict__ x, const TV* __restrict__ V,
                                 int64_t ldv, const int32_t* __restrict__ kb, const double* __restrict__ y, int ldy) {
-    __shared__ double ys[64];
+    using A = typename std::conditional<sizeof(TV) == 4 && sizeof(TX) == 4, float, double>::type;
+    __shared__ A ys[64];
     __shared__ int s_k;
     const BChunk c = ch[blockIdx.x];
     if (threadIdx.x == 0) s_k = kb[c.inst];
-    if (threadIdx.x < 64) ys[threadIdx.x] = y[c.inst * ldy + min((int)threadIdx.x, ldy - 1)];
+    if (threadIdx.x < 64) ys[threadIdx.x] = (A)y[c.inst * ldy + min((int)threadIdx.x, ldy - 1)];
     __syncthreads();
     const int k = s_k;
     for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x) {
-        double s = 0.;
-        for (int q = 0; q < k; ++q) s += ys[q] * (double)V[(int64_t)q * ldv + i];
-        x[i] = (TX)((double)x[i] + s);
+        A sv = A(0);
+        for (int q = 0; q < k; ++q) sv = fma(ys[q], (A)V[(int64_t)q * ldv + i], sv);
+        x[i] = (TX)((A)x[i] + sv);
     }
 }
 
@@ -143,10 +147,12 @@ __global__ void bcombine_kernel(const BChunk* __restrict__ ch, TX* __restrict__ 
 template <typename TX, typename TY>
 __global__ void bscale_kernel(const BChunk* __restrict__ ch, const TX* __restrict__ x, TY* __restrict__ y,
                               const double* __restrict__ a, int lda, double ascal, double beta) {
+    using A = typename std::conditional<sizeof(TX) == 4 && sizeof(TY) == 4, float, double>::type;
     const BChunk c = ch[blockIdx.x];
     const double s = a ? a[c.inst * lda] : ascal;
+    const A sa = (A)s, ba = (A)beta;
     for (int64_t i = c.begin + threadIdx.x; i < c.end; i += blockDim.x)
-        y[i] = (TY)((s == 0. ? 0. : s * (double)x[i]) + (beta == 0. ? 0. : beta * (double)y[i]));
+        y[i] = (TY)((s == 0. ? A(0) : sa * (A)x[i]) + (beta == 0. ? A(0) : ba * (A)y[i]));
 }
 
 // Start of a restart cycle, one thread per instance: beta = ||r||, g = (beta, 0...).

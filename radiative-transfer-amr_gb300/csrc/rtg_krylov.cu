@@ -18,6 +18,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 #include <vector>
 
 #include "rtg_internal.h"
@@ -30,69 +31,81 @@ constexpr int kRedBlocks = 296;   // 2 x 148-ish; partial sums per reduction
 constexpr int kRedThreads = 256;
 constexpr int kDotGroup = 8;      // vectors per pass in multi_dot
 
+// Arithmetic of the vector kernels: a vector's own precision per element and
+// per warp (FP32 vectors stay on the FP32 pipe: GB300's FP64 rate is 1/64 of
+// it), double from the per-warp sums on.
+template <typename T>
+using Acc = T;
+
+// out[q] = <V_q, w> for q < k.  Each block writes its partial sums; the last
+// block to finish (atomic ticket) adds them in block order, so the result does
+// not depend on the schedule, writes out (and out_sum = out + add when add is
+// given) and resets the ticket.
 template <typename T>
 __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, const T* __restrict__ w,
-                                 int64_t n, double* __restrict__ partial) {
+                                 int64_t n, double* __restrict__ partial, unsigned int* __restrict__ ticket,
+                                 double* __restrict__ out, const double* __restrict__ add,
+                                 double* __restrict__ out_sum) {
     __shared__ double red[kDotGroup][kRedThreads / 32];
+    __shared__ int s_last;
     for (int g0 = 0; g0 < k; g0 += kDotGroup) {
         const int gk = min(kDotGroup, k - g0);
-        double acc[kDotGroup];
+        Acc<T> acc[kDotGroup];
 #pragma unroll
-        for (int q = 0; q < kDotGroup; ++q) acc[q] = 0.;
+        for (int q = 0; q < kDotGroup; ++q) acc[q] = Acc<T>(0);
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
              i += (int64_t)gridDim.x * blockDim.x) {
-            const double wi = (double)w[i];
+            const Acc<T> wi = w[i];
 #pragma unroll
             for (int q = 0; q < kDotGroup; ++q)
-                if (q < gk) acc[q] += (double)V[(int64_t)(g0 + q) * ldv + i] * wi;
+                if (q < gk) acc[q] = fma(Acc<T>(V[(int64_t)(g0 + q) * ldv + i]), wi, acc[q]);
         }
 #pragma unroll
         for (int q = 0; q < kDotGroup; ++q) {
-            double s = acc[q];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = s;
+            Acc<T> sw = acc[q];
+            for (int o = 16; o > 0; o >>= 1) sw += __shfl_down_sync(0xffffffffu, sw, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = (double)sw;
         }
         __syncthreads();
         if (threadIdx.x < gk) {
-            double s = 0.;
-            for (int wq = 0; wq < kRedThreads / 32; ++wq) s += red[threadIdx.x][wq];
-            partial[(int64_t)blockIdx.x * k + g0 + threadIdx.x] = s;
+            double sb = 0.;
+            for (int wq = 0; wq < kRedThreads / 32; ++wq) sb += red[threadIdx.x][wq];
+            partial[(int64_t)blockIdx.x * k + g0 + threadIdx.x] = sb;
         }
         __syncthreads();
     }
-}
-
-// out[q] = sum_b partial[b][q]; with add, also out_sum[q] = out[q] + add[q]
-__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nb, int k,
-                                       double* __restrict__ out, const double* __restrict__ add,
-                                       double* __restrict__ out_sum) {
-    const int q = blockIdx.x;
-    double s = 0.;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[(int64_t)b * k + q];
-    __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __threadfence();   // every writer's partials before the ticket
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.;
-        for (int wq = 0; wq < (int)(blockDim.x + 31) / 32; ++wq) t += red[wq];
-        out[q] = t;
-        if (add) out_sum[q] = t + add[q];
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // one warp per output: lanes add every 32nd block, then a fixed shuffle tree
+    const int lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < k; q += blockDim.x >> 5) {
+        double sq = 0.;
+        for (int b = lane; b < (int)gridDim.x; b += 32) sq += __ldcg(partial + (int64_t)b * k + q);
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
+        if (lane == 0) {
+            out[q] = sq;
+            if (add) out_sum[q] = sq + add[q];
+        }
     }
+    if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // w -= sum_q h[q] V_q
 template <typename T>
 __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
                                   const double* __restrict__ h, int64_t n) {
-    __shared__ double hs[64];
-    if (threadIdx.x < k) hs[threadIdx.x] = h[threadIdx.x];
+    __shared__ Acc<T> hs[64];
+    if (threadIdx.x < k) hs[threadIdx.x] = (Acc<T>)h[threadIdx.x];
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double s = (double)w[i];
-        for (int q = 0; q < k; ++q) s -= hs[q] * (double)V[(int64_t)q * ldv + i];
-        w[i] = (T)s;
+        Acc<T> sv = w[i];
+        for (int q = 0; q < k; ++q) sv = fma(-hs[q], Acc<T>(V[(int64_t)q * ldv + i]), sv);
+        w[i] = (T)sv;
     }
 }
 
@@ -102,34 +115,38 @@ __global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, c
                                  double* hcol, int k, int64_t n) {
     const double nr = sqrt(nrm2sq[0]);
     if (blockIdx.x == 0 && threadIdx.x == 0) hcol[k] = nr;
-    const double inv = nr > 0. ? 1. / nr : 0.;
+    const Acc<T> inv = (Acc<T>)(nr > 0. ? 1. / nr : 0.);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = (T)((double)w[i] * inv);
+        out[i] = (T)(Acc<T>(w[i]) * inv);
 }
 
-// y = a*x + b*y over full vectors of possibly different types; a zero
-// coefficient drops its term without reading it (the buffer may hold anything,
-// NaN included)
+// y = a*x + b*y over full vectors of possibly different types (FP32 when both
+// are FP32, else FP64); a zero coefficient drops its term without reading it
+// (the buffer may hold anything, NaN included)
 template <typename TX, typename TY>
 __global__ void axpby_kernel(double a, const TX* __restrict__ x, double b, TY* __restrict__ y, int64_t n) {
+    using A = typename std::conditional<sizeof(TX) == 4 && sizeof(TY) == 4, float, double>::type;
+    const A aa = (A)a, bb = (A)b;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
-        y[i] = (TY)((a == 0. ? 0. : a * (double)x[i]) + (b == 0. ? 0. : b * (double)y[i]));
+        y[i] = (TY)((a == 0. ? A(0) : aa * (A)x[i]) + (b == 0. ? A(0) : bb * (A)y[i]));
 }
 
-// x += sum_q c[q] V_q (c on device)
+// x += scale * sum_q c[q] V_q (c on device; FP32 when both vectors are FP32)
 template <typename TV, typename TX>
 __global__ void combine_kernel(TX* __restrict__ x, const TV* __restrict__ V, int64_t ldv, int k,
                                const double* __restrict__ c, double scale, int64_t n) {
-    __shared__ double cs[64];
-    if (threadIdx.x < k) cs[threadIdx.x] = c[threadIdx.x];
+    using A = typename std::conditional<sizeof(TV) == 4 && sizeof(TX) == 4, float, double>::type;
+    __shared__ A cs[64];
+    if (threadIdx.x < k) cs[threadIdx.x] = (A)c[threadIdx.x];
     __syncthreads();
+    const A sc = (A)scale;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double s = 0.;
-        for (int q = 0; q < k; ++q) s += cs[q] * (double)V[(int64_t)q * ldv + i];
-        x[i] = (TX)((double)x[i] + scale * s);
+        A sv = A(0);
+        for (int q = 0; q < k; ++q) sv = fma(cs[q], (A)V[(int64_t)q * ldv + i], sv);
+        x[i] = (TX)((A)x[i] + sc * sv);
     }
 }
 
@@ -154,6 +171,7 @@ struct Workspace {
     double* Z64 = nullptr;      // m x N flexible basis (preconditioners 2 and 3)
     float* Z32 = nullptr;
     double* partial = nullptr;  // kRedBlocks x (m+1)
+    unsigned int* ticket = nullptr;   // last-block ticket of multi_dot_kernel (0 between launches)
     double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
     std::vector<void*> allocs;
@@ -194,6 +212,8 @@ Workspace* get_ws(rtg_handle* h, int m) {
     ws->t32 = dalloc<float>(ws, N);
     ws->s32 = dalloc<float>(ws, N);
     ws->partial = dalloc<double>(ws, (int64_t)kRedBlocks * (m + 2));
+    ws->ticket = dalloc<unsigned int>(ws, 1);
+    RTG_CUDA(cudaMemset(ws->ticket, 0, sizeof(unsigned int)));
     ws->hdev = dalloc<double>(ws, 4 * (m + 2));
     RTG_CUDA(cudaMallocHost(&ws->hhost, sizeof(double) * 4 * (m + 2)));
     return ws;
@@ -202,8 +222,8 @@ Workspace* get_ws(rtg_handle* h, int m) {
 template <typename T>
 void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, double* out,
           const double* add, double* out_sum, cudaStream_t s) {
-    multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial);
-    reduce_partials_kernel<<<k, 256, 0, s>>>(ws->partial, kRedBlocks, k, out, add, out_sum);
+    multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
+                                                          out_sum);
 }
 
 template <typename T>
