@@ -164,6 +164,10 @@ typedef struct rtg_solve_info {
 /* library / quadrature ------------------------------------------------------ */
 int         rtg_abi_version(void);
 const char* rtg_last_error(void);
+/* Kernels the library has launched since it was loaded (host-side count of
+ * launch statements, all handles and streams; captured graphs count when
+ * recorded, not when replayed). */
+int64_t rtg_launch_count(void);
 /* kind 0: Legendre-Gauss-Lobatto (x, y), 1: Legendre-Gauss (th); ascending on
  * [-1, 1]; n in [1, 16]. */
 int rtg_quad_nodes(int kind, int n, double* nodes, double* weights);

@@ -1129,7 +1129,7 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
                 tp.Wf = v32.W;
             }
             apply_tiled_kernel<T, f64><<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
-                v, tp, flags, plan->d_tiles, plan->d_tile_cpl, x, y);
+                v, tp, flags, plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
             const cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 cudaFuncAttributes fa{};
@@ -1145,12 +1145,12 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
         const ApplyGroup& G = plan->g[grp];
         if (G.nitems) {
             apply_col_kernel<T, T, f64><<<G.nitems, kApplyThreads, G.smem, s>>>(v, v32.W, v32.mort, flags,
-                                                                              G.d_items, G.stage_w, x, y);
+                                                                              G.d_items, G.stage_w, x, y), count_launch();
             RTG_LAUNCHED("apply_col_kernel");
         }
     }
     if (plan->nslow) {
-        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y);
+        apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y), count_launch();
         RTG_LAUNCHED("apply_global_kernel");
     }
 }
@@ -1375,17 +1375,17 @@ template void launch_apply<float>(const rtg_handle*, const OpView<float>&, uint3
                                   float*, cudaStream_t);
 
 void launch_interior_mask(const rtg_handle* h, uint8_t* mask, cudaStream_t s) {
-    interior_mask_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, mask);
+    interior_mask_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, mask), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
 void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* out, cudaStream_t s) {
-    mask_vector_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, part, x, out);
+    mask_vector_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, part, x, out), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
 void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s) {
-    weight_forcing_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, f, out);
+    weight_forcing_kernel<<<h->v64.nelem, 128, 0, s>>>(h->v64, f, out), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 

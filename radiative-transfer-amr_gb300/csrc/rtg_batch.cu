@@ -276,8 +276,8 @@ void free_bws(BatchWs* w) {
 // per-instance squared norms into out[b*ldo]
 template <typename T>
 void bnorm2(const BatchWs* w, const T* v, double* out, int ldo, cudaStream_t s, const int32_t* done = nullptr) {
-    bdot_kernel<T><<<w->nchunks, kBThreads, 0, s>>>(w->d_ch, v, 0, 1, v, w->partial, done);
-    breduce_kernel<<<dim3(w->nb, 1), 128, 0, s>>>(w->d_cbeg, w->partial, 1, out, ldo, nullptr, nullptr);
+    bdot_kernel<T><<<w->nchunks, kBThreads, 0, s>>>(w->d_ch, v, 0, 1, v, w->partial, done), count_launch();
+    breduce_kernel<<<dim3(w->nb, 1), 128, 0, s>>>(w->d_cbeg, w->partial, 1, out, ldo, nullptr, nullptr), count_launch();
 }
 
 // One restart cycle of batched FP32 GMRES for A d = rhs32, sweep right
@@ -291,38 +291,38 @@ void record_cycle(rtg_handle* h, BatchWs* w, cudaStream_t s) {
     v.skip = w->col_skip;
     // w = rhs - A d ; V0 = w / ||w|| ; start
     launch_apply<float>(h, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, w->d32, w->s32, s);
-    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->rhs32, w->w32, nullptr, 0, 1., 0.);
-    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->w32, nullptr, 0, -1., 1.);
+    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->rhs32, w->w32, nullptr, 0, 1., 0.), count_launch();
+    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->w32, nullptr, 0, -1., 1.), count_launch();
     bnorm2<float>(w, w->w32, w->nsq, 1, s);
     bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, w->V32, w->nsq, 1, nullptr, 0, 0,
-                                                      nullptr);
-    bstart_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->nsq, 1, w->g, w->tin, w->kvalid, w->done);
+                                                      nullptr), count_launch();
+    bstart_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->nsq, 1, w->g, w->tin, w->kvalid, w->done), count_launch();
     for (int j = 0; j < m; ++j) {
         float* vj = w->V32 + (int64_t)j * N;
         float* vn = w->V32 + (int64_t)(j + 1) * N;
-        bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 0, w->col_skip);
+        bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 0, w->col_skip), count_launch();
         apply_sweep<float>(h, vj, w->z32, s, nullptr, w->col_skip);
         launch_apply<float>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, w->z32, w->w32, s);
         // CGS2 with per-instance coefficients; ho = h1 + h2
-        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done);
-        breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h1, ldh, nullptr, nullptr);
-        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h1, ldh, w->done);
-        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done);
-        breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h2, ldh, w->h1, w->ho);
-        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h2, ldh, w->done);
+        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done), count_launch();
+        breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h1, ldh, nullptr, nullptr), count_launch();
+        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h1, ldh, w->done), count_launch();
+        bdot_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->V32, N, j + 1, w->w32, w->partial, w->done), count_launch();
+        breduce_kernel<<<dim3(nb, j + 1), 128, 0, s>>>(w->d_cbeg, w->partial, j + 1, w->h2, ldh, w->h1, w->ho), count_launch();
+        baxpy_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->w32, w->V32, N, j + 1, w->h2, ldh, w->done), count_launch();
         bnorm2<float>(w, w->w32, w->nsq, 1, s, w->done);
         bnormalize_kernel<float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d_cbeg, w->w32, vn, w->nsq, 1, w->ho, ldh, j + 1,
-                                                          w->done);
+                                                          w->done), count_launch();
         barnoldi_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, j, w->ho, ldh, w->H, w->cs, w->sn, w->g, w->tin, w->kvalid,
-                                                   w->done, w->est);
+                                                   w->done, w->est), count_launch();
     }
     // d += P^{-1} (V y), for the instances that formed a correction
-    bsolve_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->H, w->g, w->kvalid, w->y);
-    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->s32, nullptr, 0, 0., 0.);
-    bcombine_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->V32, N, w->kvalid, w->y, m);
-    bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 1, w->col_skip);
+    bsolve_kernel<<<grid1(nb), 128, 0, s>>>(nb, m, w->H, w->g, w->kvalid, w->y), count_launch();
+    bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->s32, nullptr, 0, 0., 0.), count_launch();
+    bcombine_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->s32, w->V32, N, w->kvalid, w->y, m), count_launch();
+    bskip_kernel<<<grid1(ncols), 128, 0, s>>>(ncols, w->col_inst, w->done, w->kvalid, 1, w->col_skip), count_launch();
     apply_sweep<float>(h, w->s32, w->z32, s, nullptr, w->col_skip);
-    badd_kernel<<<nc, kBThreads, 0, s>>>(w->d_ch, w->z32, w->d32, w->kvalid);
+    badd_kernel<<<nc, kBThreads, 0, s>>>(w->d_ch, w->z32, w->d32, w->kvalid), count_launch();
 }
 
 }  // namespace
@@ -420,8 +420,8 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
     launch_mask_vector(h, 1, g, w->gb, s);
     launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, w->gb, w->t, s);
     launch_mask_vector(h, 0, f, w->b, s);
-    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->t, w->b, nullptr, 0, -1., 1.);
-    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->t, w->x, nullptr, 0, 0., 0.);
+    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->t, w->b, nullptr, 0, -1., 1.), count_launch();
+    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->t, w->x, nullptr, 0, 0., 0.), count_launch();
     std::vector<double> bn(nb), rn(nb), tol(nb), tin(nb), scale(nb), inv(nb);
     bnorm2<double>(w, w->b, w->vnorm, 1, s);
     RTG_CUDA(cudaMemcpyAsync(bn.data(), w->vnorm, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
@@ -436,7 +436,7 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
         // r = b - A x (FP64), per-instance norms
         launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, w->x, w->r, s);
         ++fp64_applies;
-        bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->b, w->r, nullptr, 0, 1., -1.);
+        bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->b, w->r, nullptr, 0, 1., -1.), count_launch();
         bnorm2<double>(w, w->r, w->vnorm, 1, s);
         RTG_CUDA(cudaMemcpyAsync(rn.data(), w->vnorm, sizeof(double) * nb, cudaMemcpyDeviceToHost, s));
         RTG_CUDA(cudaStreamSynchronize(s));
@@ -455,8 +455,8 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
         // inner FP32 solve of A d = r / ||r|| per instance
         RTG_CUDA(cudaMemcpyAsync(w->scale, inv.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, s));
         RTG_CUDA(cudaMemcpyAsync(w->tin, tin.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, s));
-        bscale_kernel<double, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->r, w->rhs32, w->scale, 1, 0., 0.);
-        bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d32, w->d32, nullptr, 0, 0., 0.);
+        bscale_kernel<double, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->r, w->rhs32, w->scale, 1, 0., 0.), count_launch();
+        bscale_kernel<float, float><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d32, w->d32, nullptr, 0, 0., 0.), count_launch();
         if (!w->cycle) {
             // build the FP32 apply plan and sweep launch shape before capture
             launch_apply<float>(h, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, w->d32, w->s32, s);
@@ -488,12 +488,12 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
         }
         // x += ||r|| d
         RTG_CUDA(cudaMemcpyAsync(w->scale, scale.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, s));
-        bscale_kernel<float, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d32, w->x, w->scale, 1, 0., 1.);
+        bscale_kernel<float, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->d32, w->x, w->scale, 1, 0., 1.), count_launch();
     }
     if (sweep_status(h, s) != RTG_OK)
         throw RtgError{RTG_ERR_TIMEOUT, "a sweep wait gave up; the solution is not valid"};
     // u = x on the unknowns, g on the inflow-boundary DOFs
-    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->x, w->gb, nullptr, 0, 1., 1.);
+    bscale_kernel<double, double><<<nc, kBThreads, 0, s>>>(w->d_ch, w->x, w->gb, nullptr, 0, 1., 1.), count_launch();
     RTG_CUDA(cudaMemcpyAsync(u, w->gb, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
     RTG_CUDA(cudaStreamSynchronize(s));
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

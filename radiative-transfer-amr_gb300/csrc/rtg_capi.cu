@@ -14,6 +14,11 @@ static thread_local std::string g_err;
 
 void set_error(const std::string& msg) { g_err = msg; }
 
+std::atomic<long long>& launch_counter() {
+    static std::atomic<long long> n{0};
+    return n;
+}
+
 void raise_smem_limit(const void* func, size_t bytes) {
     static std::mutex mu;
     static std::map<std::pair<int, const void*>, size_t> done;
@@ -82,6 +87,8 @@ using namespace rtg;
 extern "C" {
 
 int rtg_abi_version(void) { return RTG_ABI_VERSION; }
+
+int64_t rtg_launch_count(void) { return (int64_t)rtg::launch_counter().load(); }
 
 const char* rtg_last_error(void) { return g_err.c_str(); }
 
@@ -405,7 +412,7 @@ int rtg_split_vector(rtg_handle* h, const double* x, double* x_int, void* stream
     return guard("rtg_split_vector", [&] {
         if (!h || !x || !x_int) throw RtgError{RTG_ERR_ARG, "null argument"};
         const int64_t n = h->host.ndof_interior;
-        gather_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(x, h->d_interior_index, x_int, n);
+        gather_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(x, h->d_interior_index, x_int, n), count_launch();
         RTG_CUDA(cudaGetLastError());
     });
 }
@@ -416,7 +423,7 @@ int rtg_merge_vectors(rtg_handle* h, const double* x_int, const double* g, doubl
         cudaStream_t s = (cudaStream_t)stream;
         launch_mask_vector(h, 1, g, x, s);
         const int64_t n = h->host.ndof_interior;
-        scatter_kernel<<<grid_for(n), 256, 0, s>>>(x_int, h->d_interior_index, x, n);
+        scatter_kernel<<<grid_for(n), 256, 0, s>>>(x_int, h->d_interior_index, x, n), count_launch();
         RTG_CUDA(cudaGetLastError());
     });
 }

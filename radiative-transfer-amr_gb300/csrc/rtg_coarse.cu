@@ -226,20 +226,20 @@ void invert_dense(const std::vector<double>& A, int n, double* inv64, float* inv
         RTG_CUDA(cudaMalloc(&fcol, sizeof(double) * n));
         RTG_CUDA(cudaMemcpy2DAsync(M, sizeof(double) * 2 * n, A.data(), sizeof(double) * n, sizeof(double) * n, n,
                                    cudaMemcpyHostToDevice, s));
-        gj_identity_kernel<<<vgrid((int64_t)n * n), 256, 0, s>>>(M, n);
+        gj_identity_kernel<<<vgrid((int64_t)n * n), 256, 0, s>>>(M, n), count_launch();
         int* dpiv = (int*)small;
         double* dpval = small + 1;
         int* dstatus = (int*)(small + 2);
         RTG_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
         for (int k = 0; k < n; ++k) {
-            gj_pivot_kernel<<<1, 1024, 0, s>>>(M, n, k, dpiv, dpval, dstatus);
-            gj_column_kernel<<<std::max(1, std::min((n + 255) / 256, 256)), 256, 0, s>>>(M, n, k, dpiv, fcol);
+            gj_pivot_kernel<<<1, 1024, 0, s>>>(M, n, k, dpiv, dpval, dstatus), count_launch();
+            gj_column_kernel<<<std::max(1, std::min((n + 255) / 256, 256)), 256, 0, s>>>(M, n, k, dpiv, fcol), count_launch();
             gj_swap_scale_kernel<<<std::max(1, std::min((2 * n + 255) / 256, 1024)), 256, 0, s>>>(M, n, k, dpiv,
-                                                                                                   dpval);
+                                                                                                   dpval), count_launch();
             dim3 g(std::max(1, std::min((2 * n - k + 255) / 256, 8)), n);
-            gj_eliminate_kernel<<<g, 256, 0, s>>>(M, n, k, fcol);
+            gj_eliminate_kernel<<<g, 256, 0, s>>>(M, n, k, fcol), count_launch();
         }
-        gj_extract_kernel<<<vgrid((int64_t)n * n), 256, 0, s>>>(M, n, inv64, inv32);
+        gj_extract_kernel<<<vgrid((int64_t)n * n), 256, 0, s>>>(M, n, inv64, inv32), count_launch();
         int status = 0;
         RTG_CUDA(cudaMemcpyAsync(&status, dstatus, sizeof(int), cudaMemcpyDeviceToHost, s));
         RTG_CUDA(cudaStreamSynchronize(s));
@@ -402,14 +402,14 @@ void apply_coarse(rtg_handle* h, const T* v, T* z, cudaStream_t s) {
     const int64_t N = h->host.ndof;
     T* r = sizeof(T) == 8 ? (T*)c->r64 : (T*)c->r32;
     launch_apply<T>(h, ov, RTG_SYSTEM | RTG_MASK_ROWS, z, r, s);
-    residual_kernel<T><<<vgrid(N), 256, 0, s>>>(v, r, N);
-    restrict_kernel<T><<<ov.ncols, 128, 0, s>>>(ov, r, c->bc);
+    residual_kernel<T><<<vgrid(N), 256, 0, s>>>(v, r, N), count_launch();
+    restrict_kernel<T><<<ov.ncols, 128, 0, s>>>(ov, r, c->bc), count_launch();
     if (sizeof(T) == 8) {
-        gemv_kernel<double><<<egrid(c->n), 256, 0, s>>>(c->inv64, c->bc, c->n, c->cc64);
-        prolong_kernel<T, double><<<egrid(ov.nelem), 256, 0, s>>>(ov, c->cc64, z);
+        gemv_kernel<double><<<egrid(c->n), 256, 0, s>>>(c->inv64, c->bc, c->n, c->cc64), count_launch();
+        prolong_kernel<T, double><<<egrid(ov.nelem), 256, 0, s>>>(ov, c->cc64, z), count_launch();
     } else {
-        gemv_kernel<float><<<egrid(c->n), 256, 0, s>>>(c->inv32, c->bc, c->n, c->cc32);
-        prolong_kernel<T, float><<<egrid(ov.nelem), 256, 0, s>>>(ov, c->cc32, z);
+        gemv_kernel<float><<<egrid(c->n), 256, 0, s>>>(c->inv32, c->bc, c->n, c->cc32), count_launch();
+        prolong_kernel<T, float><<<egrid(ov.nelem), 256, 0, s>>>(ov, c->cc32, z), count_launch();
     }
     RTG_CUDA(cudaGetLastError());
 }

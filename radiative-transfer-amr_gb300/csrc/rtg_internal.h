@@ -2,6 +2,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -24,6 +25,11 @@ void set_error(const std::string& msg);
 // The default limit is 48 KB minus the kernel's static shared memory, so any
 // launch with dynamic shared memory goes through here.
 void raise_smem_limit(const void* func, size_t bytes);
+
+// Kernels launched by the library since it was loaded: every launch statement
+// ends with count_launch() (comma operator, so it stays one statement).
+std::atomic<long long>& launch_counter();
+inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
 
 struct RtgError {
     int code;

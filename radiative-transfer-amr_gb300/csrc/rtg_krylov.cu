@@ -223,7 +223,7 @@ template <typename T>
 void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, double* out,
           const double* add, double* out_sum, cudaStream_t s) {
     multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
-                                                          out_sum);
+                                                          out_sum), count_launch();
 }
 
 template <typename T>
@@ -244,7 +244,7 @@ double norm2(rtg_handle* h, Workspace* ws, const double* v, cudaStream_t s) {
 double residual64(rtg_handle* h, Workspace* ws, const double* b, const double* x, double* r,
                   cudaStream_t s) {
     launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, x, r, s);
-    axpby_kernel<double, double><<<grid_for(ws->N), 256, 0, s>>>(1., b, -1., r, ws->N);
+    axpby_kernel<double, double><<<grid_for(ws->N), 256, 0, s>>>(1., b, -1., r, ws->N), count_launch();
     return norm2(h, ws, r, s);
 }
 
@@ -286,23 +286,23 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
     GmresResult res;
     const OpView<T>& v = view<T>(h);
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
-    axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., rhs, 0., xT, N);
+    axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., rhs, 0., xT, N), count_launch();
     // r = rhs - A x = rhs (x = 0)
     int total = 0;
     bool first = true;
     while (total < max_it) {
         // r = rhs - A x  into V_0 (unnormalised), beta = ||r||
         if (first) {
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, 0., wbuf, N);
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, 0., wbuf, N), count_launch();
         } else {
             launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, xT, wbuf, s);
             ++*applies;
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, -1., wbuf, N);
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, -1., wbuf, N), count_launch();
         }
         first = false;
         dots<T>(ws, wbuf, 0, 1, wbuf, N, ws->hdev + 3 * (m + 2), nullptr, nullptr, s);
         normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ws->hdev + 3 * (m + 2),
-                                                         ws->hdev + 2 * (m + 2), 0, N);
+                                                         ws->hdev + 2 * (m + 2), 0, N), count_launch();
         RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev + 2 * (m + 2), sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
         RTG_CUDA(cudaStreamSynchronize(s));
@@ -349,11 +349,11 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             double* nr = ws->hdev + 3 * (m + 2);
             // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
             dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s);
-            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N);
+            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
             dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
-            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N);
+            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
             dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
-            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N);
+            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N), count_launch();
             RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
                                      cudaMemcpyDeviceToHost, s));
             RTG_CUDA(cudaStreamSynchronize(s));
@@ -394,16 +394,16 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         if (flex) {
             // x += Z y
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N);
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N), count_launch();
         } else if (mode == 1) {
             // x += P^{-1} (V y)
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., tbuf, 0., tbuf, N);
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(tbuf, V, N, j, ws->hdev, 1., N);
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., tbuf, 0., tbuf, N), count_launch();
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(tbuf, V, N, j, ws->hdev, 1., N), count_launch();
             apply_sweep<T>(h, tbuf, zbuf, s);
             ++pc.sweeps;
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., zbuf, 1., xT, N);
+            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., zbuf, 1., xT, N), count_launch();
         } else {
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N);
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N), count_launch();
         }
         res.iters = total;
         if (res.converged) break;
@@ -440,12 +440,12 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, ws->gb, ws->t, s);
     inf.fp64_applies++;
     launch_mask_vector(h, 0, f, ws->b, s);
-    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(-1., ws->t, 1., ws->b, N);
+    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(-1., ws->t, 1., ws->b, N), count_launch();
     // x0 = u_I (nonzero guess) or 0; the reference starts from f_I (rt/solve.py:104)
     if (o->nonzero_guess)
         launch_mask_vector(h, 0, u, ws->x, s);
     else
-        axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(0., ws->b, 0., ws->x, N);
+        axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(0., ws->b, 0., ws->x, N), count_launch();
 
     inf.rhs_norm = norm2(h, ws, ws->b, s);
     const double tol = std::max(o->rtol * inf.rhs_norm, o->atol);
@@ -469,7 +469,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
             GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
                                            o->max_it - used, &hv, &applies64, pc, ws->z64, ws->t64, s);
             used += std::max(gr.iters, 1);
-            axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N);
+            axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N), count_launch();
             const double prev = res;
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
             inf.fp64_applies++;
@@ -487,14 +487,14 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
         const double inner_rtol = o->inner_rtol > 0. ? o->inner_rtol : 1e-6;
         while (res > tol && used < o->max_it && outer < max_outer) {
             // r32 = r / ||r||
-            axpby_kernel<double, float><<<grid_for(N), 256, 0, s>>>(1. / res, ws->r, 0., ws->w32, N);
+            axpby_kernel<double, float><<<grid_for(N), 256, 0, s>>>(1. / res, ws->r, 0., ws->w32, N), count_launch();
             // one FP32 solve per refinement step, capped at 20 restart cycles
             const int inner_cap = std::min(o->max_it - used, 20 * m);
             GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, ws->s32, ws->V32, m,
                                           std::max(inner_rtol, tol / res), inner_cap,
                                           nullptr, &applies32, pc, ws->z32, ws->t32, s);
             used += std::max(gr.iters, 1);
-            axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N);
+            axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N), count_launch();
             const double prev = res;
             res = residual64(h, ws, ws->b, ws->x, ws->r, s);
             inf.fp64_applies++;
@@ -519,7 +519,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.res_f = res;
     inf.converged = res <= tol ? 1 : 0;
     // u = x on the unknowns, g on the inflow-boundary DOFs (rt/solve.py:163)
-    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->x, 1., ws->gb, N);
+    axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->x, 1., ws->gb, N), count_launch();
     RTG_CUDA(cudaMemcpyAsync(u, ws->gb, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
     RTG_CUDA(cudaStreamSynchronize(s));
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -788,9 +788,9 @@ int64_t nn_rows(rtg_handle* h) { return get_nn(h)->rows; }
 void nn_features(rtg_handle* h, float* feat, cudaStream_t s) {
     NNWs* w = get_nn(h);
     const OpView<float>& v = h->v32;
-    nn_colphys_kernel<float><<<elem_grid(v.ncols), 256, 0, s>>>(v, w->ctau, w->calb);
+    nn_colphys_kernel<float><<<elem_grid(v.ncols), 256, 0, s>>>(v, w->ctau, w->calb), count_launch();
     nn_physfeat_kernel<float><<<elem_grid(v.nelem), 256, 0, s>>>(v, w->ctau, w->calb, w->nbr8, w->raw, w->nfree,
-                                                                w->row_off, feat ? feat : w->feat);
+                                                                w->row_off, feat ? feat : w->feat), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
@@ -799,7 +799,7 @@ void nn_forward(const float* params, const float* feat, int64_t rows, float* coe
     mlp_attributes();
     const int64_t ntiles = (rows + kTile - 1) / kTile;
     const int grid = (int)std::min<int64_t>(ntiles, 152);
-    nn_forward_kernel<<<grid, kMlpThreads, kMlpSmem, s>>>(params, feat, rows, coef);
+    nn_forward_kernel<<<grid, kMlpThreads, kMlpSmem, s>>>(params, feat, rows, coef), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
@@ -827,7 +827,7 @@ template <typename T>
 static void colstats(rtg_handle* h, NNWs* w, const T* z, cudaStream_t s) {
     const OpView<T>& v = nview<T>(h);
     const size_t smem = sizeof(float) * std::max(1, h->host.max_cells_col);
-    nn_colstats_kernel<T><<<v.ncols, 128, smem, s>>>(v, z, w->phi, w->em, w->cm, w->colsq);
+    nn_colstats_kernel<T><<<v.ncols, 128, smem, s>>>(v, z, w->phi, w->em, w->cm, w->colsq), count_launch();
 }
 
 template <typename T>
@@ -835,9 +835,9 @@ void nn_moments(rtg_handle* h, const T* z, float* mom, float* scale, cudaStream_
     NNWs* w = get_nn(h);
     const OpView<T>& v = nview<T>(h);
     colstats<T>(h, w, z, s);
-    nn_scale_kernel<<<1, 1024, 0, s>>>(w->colsq, v.ncols, (double)h->host.ndof, scale);
+    nn_scale_kernel<<<1, 1024, 0, s>>>(w->colsq, v.ncols, (double)h->host.ndof, scale), count_launch();
     nn_moments_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, z, w->phi, w->em, w->cm, w->nbr8, w->row_off, scale,
-                                                           mom);
+                                                           mom), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
@@ -846,7 +846,7 @@ void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s) {
     NNWs* w = get_nn(h);
     const OpView<T>& v = nview<T>(h);
     colstats<T>(h, w, z, s);
-    nn_correct_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, coef, w->phi, w->em, w->cm, w->nbr8, w->row_off, z);
+    nn_correct_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, coef, w->phi, w->em, w->cm, w->nbr8, w->row_off, z), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
@@ -854,7 +854,7 @@ template <typename T>
 void nn_stats(rtg_handle* h, const T* z, const T* err, const float* scale, float weight, float* S, cudaStream_t s) {
     NNWs* w = get_nn(h);
     const OpView<T>& v = nview<T>(h);
-    nn_stats_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, z, err, w->row_off, scale, weight, S);
+    nn_stats_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, z, err, w->row_off, scale, weight, S), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
@@ -867,15 +867,15 @@ void nn_loss_grad(const float* params, const float* feat, const float* mom, cons
     const int grid = (int)std::min<int64_t>(ntiles, kGradCtas);
     double* lossw = reinterpret_cast<double*>(work + (int64_t)kGradCtas * kNP);
     nn_grad_kernel<<<grid, kMlpThreads, kMlpSmem, s>>>(params, feat, mom, stats, std::max<int64_t>(rows, 0), work,
-                                                       lossw);
-    nn_reduce_grad_kernel<<<(kNP + 255) / 256, 256, 0, s>>>(work, grid, lossw, grad, loss);
+                                                       lossw), count_launch();
+    nn_reduce_grad_kernel<<<(kNP + 255) / 256, 256, 0, s>>>(work, grid, lossw, grad, loss), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 
 void nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float b1, float b2,
              float eps, float wd, cudaStream_t s) {
     const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    nn_adam_kernel<<<(kNP + 255) / 256, 256, 0, s>>>(params, grad, m, v, kNP, lr, b1, b2, eps, wd, c1, c2);
+    nn_adam_kernel<<<(kNP + 255) / 256, 256, 0, s>>>(params, grad, m, v, kNP, lr, b1, b2, eps, wd, c1, c2), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 

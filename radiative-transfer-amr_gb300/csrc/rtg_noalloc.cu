@@ -118,8 +118,8 @@ extern "C" int rtg_dots_noalloc(int k, const double* V, int64_t ldv, const doubl
         if (k > 1 && ldv < n) throw RtgError{RTG_ERR_ARG, "ldv smaller than n"};
         double* partial = partial_for_current_device();
         cudaStream_t s = (cudaStream_t)stream;
-        noalloc_dot_kernel<<<kNaBlocks, kNaThreads, 0, s>>>(V, ldv, k, w, n, partial);
-        noalloc_reduce_kernel<<<k, 256, 0, s>>>(partial, kNaBlocks, k, out);
+        noalloc_dot_kernel<<<kNaBlocks, kNaThreads, 0, s>>>(V, ldv, k, w, n, partial), count_launch();
+        noalloc_reduce_kernel<<<k, 256, 0, s>>>(partial, kNaBlocks, k, out), count_launch();
         RTG_CUDA(cudaGetLastError());
         return RTG_OK;
     } catch (const RtgError& e) {

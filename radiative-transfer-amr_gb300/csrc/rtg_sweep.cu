@@ -828,7 +828,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     const size_t smem = sizeof(float) * (size_t)max_nn * 2 * max_nn;
     raise_smem_limit((const void*)build_block_inverse_kernel, smem);
     build_block_inverse_kernel<<<(int)blk_elem.size(), 256, smem, st>>>(h->v32, d_be, d_br, d_bo, s->d_inv64,
-                                                                         s->d_inv32, d_status);
+                                                                         s->d_inv32, d_status), count_launch();
     RTG_CUDA(cudaGetLastError());
     int status = 0;
     RTG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -913,7 +913,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         if (!gel.empty()) {
             RTG_CUDA(cudaMemcpy(d_gel, gel.data(), sizeof(int32_t) * gel.size(), cudaMemcpyHostToDevice));
             build_upwind_map_kernel<<<(int)gel.size(), 256, 0, st>>>(h->v64, s->d_active, s->d_inv64, s->d_inv_off,
-                                                                    d_gel, s->d_gnup, s->d_goff, s->d_G64, s->d_G32);
+                                                                    d_gel, s->d_gnup, s->d_goff, s->d_G64, s->d_G32), count_launch();
             RTG_CUDA(cudaGetLastError());
         }
     }
@@ -932,10 +932,10 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
     v.skip = skip;
-    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_next);
+    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_next), count_launch();
     {
         const int ne = (int)h->host.elems.size();
-        sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z);
+        sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z), count_launch();
     }
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
@@ -965,7 +965,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
     sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
         v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next, s->d_status,
-        um, rhs_cap, bcap, (int)s->max_c, trace);
+        um, rhs_cap, bcap, (int)s->max_c, trace), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
 

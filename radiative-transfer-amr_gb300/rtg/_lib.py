@@ -77,6 +77,7 @@ class SolveInfo(C.Structure):
 SIGNATURES = {
     "rtg_abi_version": (C.c_int, []),
     "rtg_last_error": (C.c_char_p, []),
+    "rtg_launch_count": (C.c_int64, []),
     "rtg_quad_nodes": (C.c_int, [C.c_int, C.c_int, f64p, f64p]),
     "rtg_create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(Coeffs), C.c_int, C.POINTER(C.c_void_p)]),
     "rtg_destroy": (None, [C.c_void_p]),
