@@ -408,18 +408,37 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             __syncthreads();
             if (s_abort) break;
             if (trace && threadIdx.x == 0) ck1 = clock64();
-            for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-                T a0 = zpre[l], a1 = T(0), a2 = T(0), a3 = T(0);
-                const T* g = Gs + l;
-                int u = 0;
-                for (; u + 4 <= nup; u += 4) {
-                    a0 += g[(u + 0) * nloc] * zl[u + 0];
-                    a1 += g[(u + 1) * nloc] * zl[u + 1];
-                    a2 += g[(u + 2) * nloc] * zl[u + 2];
-                    a3 += g[(u + 3) * nloc] * zl[u + 3];
+            // FP64 (bound by the FP64 pipe): two threads per output when the
+            // CTA has them, the second half of the upwind values through rhs
+            // (free once zpre is formed).  FP32 is latency bound and keeps one
+            // thread per output (the extra barrier costs more than it saves).
+            const bool split = sizeof(T) == 8 && 2 * nloc <= (int)blockDim.x;
+            const int uh = split ? (nup + 1) / 2 : nup;
+            T part = T(0);
+            const int t = threadIdx.x;
+            const int l = split ? t % nloc : t;
+            const int half = split ? t / nloc : 0;
+            if (!split || t < 2 * nloc) {
+                for (int l2 = l; l2 < nloc; l2 += blockDim.x) {
+                    const int u0 = half ? uh : 0, u1 = half ? nup : uh;
+                    T a0 = half ? T(0) : zpre[l2], a1 = T(0), a2 = T(0), a3 = T(0);
+                    const T* g = Gs + l2;
+                    int u = u0;
+                    for (; u + 4 <= u1; u += 4) {
+                        a0 += g[(u + 0) * nloc] * zl[u + 0];
+                        a1 += g[(u + 1) * nloc] * zl[u + 1];
+                        a2 += g[(u + 2) * nloc] * zl[u + 2];
+                        a3 += g[(u + 3) * nloc] * zl[u + 3];
+                    }
+                    for (; u < u1; ++u) a0 += g[u * nloc] * zl[u];
+                    part = (a0 + a1) + (a2 + a3);
+                    if (half) rhs[l2] = part;
+                    else if (!split) st_relaxed(z + E.dof_off + l2, part);
                 }
-                for (; u < nup; ++u) a0 += g[u * nloc] * zl[u];
-                st_relaxed(z + E.dof_off + l, (a0 + a1) + (a2 + a3));
+            }
+            if (split) {
+                __syncthreads();
+                if (t < nloc) st_relaxed(z + E.dof_off + t, part + rhs[t]);
             }
             __syncthreads();
             if (trace && threadIdx.x == 0) {
