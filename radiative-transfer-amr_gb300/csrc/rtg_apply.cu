@@ -309,7 +309,10 @@ struct TileParity {
     const uint8_t* scls = nullptr;   // per spatial node: 0 no, 1 every, 2 some off-diagonal scattering term kept
     const T* mortc = nullptr;        // cleaned dcoeff*Es and Et per coupling
     const float* mortf = nullptr;    // FP32 copy of the mortars (tested couplings)
-    const float* Wf = nullptr;       // FP32 copy of W (mixed nodes)
+    const float* Wf = nullptr;       // FP32 copy of W (mixed nodes without a mask)
+    const uint64_t* colfull = nullptr;   // per column: bit ij set when node ij is of class 1 (ij < 64)
+    const int64_t* kbase = nullptr;      // per spatial node of class 2: first keep mask, or -1
+    const uint64_t* kmask = nullptr;     // per (class-2 node, row R): bit c set when term (R, c) is kept
 };
 
 // f-th node on the boundary of an nx x ny node grid, going around (j = 0 row,
@@ -437,8 +440,11 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileIte
     __syncthreads();
     if (fl.scat) {
         const int tm = Mp / 4, tn = nijp / 4;
+        // FP64: only nodes of class 1 read the product
+        const uint64_t fullm = kParity ? (nij <= 64 ? par.colfull[ci] : ~0ull) : ~0ull;
         for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
             const int m0 = 4 * (tile / tn), j0 = 4 * (tile % tn);
+            if (kParity && j0 < 64 && !((fullm >> j0) & 0xFull)) continue;
             T acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
@@ -572,6 +578,15 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileIte
                 T s = T(0);
                 if (cls == 1) {
                     s = Ys[(R - it.row0) * nijp + ij];
+                } else if (cls == 2 && par.kbase[node] >= 0) {
+                    // some terms kept, some dropped: the host's keep mask of row R
+                    uint64_t mk = par.kmask[par.kbase[node] + R];
+                    const T* wr = Wg + (int64_t)R * Nth;
+                    while (mk) {
+                        const int c = __ffsll((long long)mk) - 1;
+                        mk &= mk - 1;
+                        s = fma(wr[c], Xs[c * nijp + ij], s);
+                    }
                 } else if (cls == 2) {
                     // some terms kept, some dropped: test each one
                     const bool skip_cross = !(tabs(swv) > small);
@@ -775,6 +790,9 @@ struct TuneRecord {
 struct ParityTables {
     uint8_t* d_scls = nullptr;
     double* d_mortc = nullptr;
+    uint64_t* d_colfull = nullptr;
+    int64_t* d_kbase = nullptr;
+    uint64_t* d_kmask = nullptr;
     std::vector<int> esc, etc;     // per coupling: offsets of dcoeff*Es and Et in the cleaned table
     std::vector<char> tested;      // per coupling: summed term by term
     int64_t nodes[3] = {0, 0, 0};  // nodes per scattering class
@@ -799,6 +817,9 @@ static void free_parity(const ParityTables* pt) {
     if (!pt) return;
     cudaFree(pt->d_scls);
     cudaFree(pt->d_mortc);
+    cudaFree(pt->d_colfull);
+    cudaFree(pt->d_kbase);
+    cudaFree(pt->d_kmask);
     delete pt;
 }
 
@@ -816,6 +837,8 @@ static ParityTables* build_parity(const rtg_handle* h) {
     const HostTables& t = h->host;
     ParityTables* pt = new ParityTables();
     std::vector<uint8_t> scls((size_t)std::max(t.nnodes, 1), 0);
+    std::vector<uint64_t> colfull(t.cols.size(), 0), kmask;
+    std::vector<int64_t> kbase((size_t)std::max(t.nnodes, 1), -1);
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
         const ColDev& C = t.cols[ci];
         const int Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
@@ -856,6 +879,20 @@ static ParityTables* build_parity(const rtg_handle* h) {
             }
             scls[C.node_off + ij] = cls;
             ++pt->nodes[cls];
+            if (cls == 1 && ij < 64) colfull[ci] |= 1ull << ij;
+            if (cls == 2 && Nth <= 64) {
+                // the exact FP64 test of every term of every row of the node
+                const bool cross = std::fabs(swv) > kSmall;
+                kbase[C.node_off + ij] = (int64_t)kmask.size();
+                for (int R = 0; R < Nth; ++R) {
+                    uint64_t mk = 0;
+                    for (int c = 0; c < Nth; ++c) {
+                        if (c == R || (!cross && rcell[c] != rcell[R])) continue;
+                        if (std::fabs(cw * W[(int64_t)R * Nth + c]) > kSmall) mk |= 1ull << c;
+                    }
+                    kmask.push_back(mk);
+                }
+            }
         }
     }
     const int ncpl = (int)t.cpls.size();
@@ -924,6 +961,15 @@ static ParityTables* build_parity(const rtg_handle* h) {
     try {
         RTG_CUDA(cudaMalloc(&pt->d_scls, scls.size()));
         RTG_CUDA(cudaMemcpy(pt->d_scls, scls.data(), scls.size(), cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMalloc(&pt->d_colfull, sizeof(uint64_t) * std::max<size_t>(colfull.size(), 1)));
+        if (!colfull.empty())
+            RTG_CUDA(cudaMemcpy(pt->d_colfull, colfull.data(), sizeof(uint64_t) * colfull.size(),
+                                cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMalloc(&pt->d_kbase, sizeof(int64_t) * kbase.size()));
+        RTG_CUDA(cudaMemcpy(pt->d_kbase, kbase.data(), sizeof(int64_t) * kbase.size(), cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMalloc(&pt->d_kmask, sizeof(uint64_t) * std::max<size_t>(kmask.size(), 1)));
+        if (!kmask.empty())
+            RTG_CUDA(cudaMemcpy(pt->d_kmask, kmask.data(), sizeof(uint64_t) * kmask.size(), cudaMemcpyHostToDevice));
         RTG_CUDA(cudaMalloc(&pt->d_mortc, sizeof(double) * std::max<size_t>(mortc.size(), 1)));
         if (!mortc.empty())
             RTG_CUDA(cudaMemcpy(pt->d_mortc, mortc.data(), sizeof(double) * mortc.size(), cudaMemcpyHostToDevice));
@@ -1127,6 +1173,9 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
                 tp.mortc = plan->par->d_mortc;
                 tp.mortf = v32.mort;
                 tp.Wf = v32.W;
+                tp.colfull = plan->par->d_colfull;
+                tp.kbase = plan->par->d_kbase;
+                tp.kmask = plan->par->d_kmask;
             }
             apply_tiled_kernel<T, f64><<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
                 v, tp, flags, plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
