@@ -369,6 +369,15 @@ int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_ent
     });
 }
 
+int rtg_sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind_entries,
+                   void* stream) {
+    return guard("rtg_sweep_maps", [&] {
+        if (!h) throw RtgError{RTG_ERR_ARG, "null argument"};
+        if (prec != RTG_FP32 && prec != RTG_FP64) throw RtgError{RTG_ERR_ARG, "unknown precision"};
+        sweep_maps(h, prec, onephase, map_entries, upwind_entries, (cudaStream_t)stream);
+    });
+}
+
 int rtg_sweep_trace(rtg_handle* h, int prec, const void* r, void* z, uint64_t* trace, int32_t* level,
                     void* stream) {
     return guard("rtg_sweep_trace", [&] {

@@ -200,6 +200,7 @@ template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace,
                  const int32_t* skip = nullptr);
 void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
+void sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
 int sweep_levels_count(rtg_handle* h, cudaStream_t s);
 int sweep_lagged_count(rtg_handle* h, cudaStream_t s);

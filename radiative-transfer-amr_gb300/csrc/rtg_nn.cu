@@ -492,64 +492,70 @@ __global__ void nn_physfeat_kernel(OpView<T> v, const float* __restrict__ ctau, 
 
 // ------------------------------------------------------------- z moments
 // Per column: angular mean phi at each node, the element means em, the column
-// mean cm of phi, and sum z^2 over the column.
+// mean cm of phi and, when colsq is given, sum z^2 over the column.  One thread
+// per (cell, node) forms the node's angular sums; the sums over cells (phi) and
+// over nodes (em, cm, colsq) run in a fixed order, so the result does not
+// depend on the schedule.  Shared memory: s0w[ncell][nij] (w-weighted sums),
+// swt[ncell] (angular weight sums), and, with colsq, sqs[ncell][nij].
 template <typename T>
 __global__ void nn_colstats_kernel(OpView<T> v, const T* __restrict__ z, float* __restrict__ phi,
                                    float* __restrict__ em, float* __restrict__ cm, double* __restrict__ colsq) {
-    extern __shared__ float ems[];
-    __shared__ double red[32];
-    __shared__ float redf[32];
+    extern __shared__ float sm[];
     const ColDev C = v.cols[blockIdx.x];
     const int nij = C.nx * C.ny, ncell = C.elem_end - C.elem_begin;
-    for (int k = threadIdx.x; k < ncell; k += blockDim.x) ems[k] = 0.f;
-    __syncthreads();
+    float* s0w = sm;                           // [ncell][nij]
+    float* swt = s0w + ncell * nij;            // [ncell]
+    float* phs = swt + ncell;                  // [nij]
+    float* sqs = phs + nij;                    // [ncell][nij] (colsq only)
     const T* wx = v.lglw + C.nx * kMaxNodes;
     const T* wy = v.lglw + C.ny * kMaxNodes;
-    double sq = 0.;
-    float cacc = 0.f;
-    for (int ij = threadIdx.x; ij < nij; ij += blockDim.x) {
-        const int i = ij / C.ny, j = ij % C.ny;
-        const float wij = (float)(wx[i] * wy[j]) * 0.25f;
-        float ph = 0.f;
-        for (int k = 0; k < ncell; ++k) {
-            const ElemDev E = v.elems[C.elem_begin + k];
-            const T* A = v.ang + E.ang;
-            const T* ze = z + E.dof_off + (int64_t)ij * E.nth;
-            float s0 = 0.f, sw = 0.f;
-            for (int a = 0; a < E.nth; ++a) {
-                const float zv = (float)ze[a];
-                const float w = (float)A[a];
-                s0 = fmaf(w, zv, s0);
-                sw += w;
-                sq += (double)zv * zv;
-            }
-            ph = fmaf((float)E.dth * 0.5f, s0, ph);
-            atomicAdd(&ems[k], wij * s0 / sw);
+    for (int t = threadIdx.x; t < ncell * nij; t += blockDim.x) {
+        const int k = t / nij, ij = t % nij;
+        const ElemDev E = v.elems[C.elem_begin + k];
+        const T* A = v.ang + E.ang;
+        const T* ze = z + E.dof_off + (int64_t)ij * E.nth;
+        float s0 = 0.f, sw = 0.f, sq = 0.f;
+        for (int a = 0; a < E.nth; ++a) {
+            const float zv = (float)ze[a];
+            const float w = (float)A[a];
+            s0 = fmaf(w, zv, s0);
+            sw += w;
+            sq = fmaf(zv, zv, sq);
         }
+        s0w[t] = s0;
+        if (ij == 0) swt[k] = sw;
+        if (colsq) sqs[t] = sq;
+    }
+    __syncthreads();
+    // phi per node: cells in order
+    for (int ij = threadIdx.x; ij < nij; ij += blockDim.x) {
+        float ph = 0.f;
+        for (int k = 0; k < ncell; ++k) ph = fmaf((float)v.elems[C.elem_begin + k].dth * 0.5f, s0w[k * nij + ij], ph);
         ph /= kTwoPi;
         phi[C.node_off + ij] = ph;
-        cacc = fmaf(wij, ph, cacc);
+        phs[ij] = ph;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        sq += __shfl_down_sync(0xffffffffu, sq, o);
-        cacc += __shfl_down_sync(0xffffffffu, cacc, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        red[threadIdx.x >> 5] = sq;
-        redf[threadIdx.x >> 5] = cacc;
+    // element means: nodes in order
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+        float acc = 0.f;
+        for (int ij = 0; ij < nij; ++ij) {
+            const float wij = (float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f;
+            acc = fmaf(wij, s0w[k * nij + ij], acc);
+        }
+        em[C.elem_begin + k] = acc / swt[k];
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.;
         float c = 0.f;
-        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) {
-            s += red[w];
-            c += redf[w];
-        }
-        colsq[blockIdx.x] = s;
+        for (int ij = 0; ij < nij; ++ij) c = fmaf((float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f, phs[ij], c);
         cm[blockIdx.x] = c;
     }
-    for (int k = threadIdx.x; k < ncell; k += blockDim.x) em[C.elem_begin + k] = ems[k];
+    if (colsq && threadIdx.x < 32) {
+        double sq = 0.;
+        for (int t = threadIdx.x; t < ncell * nij; t += 32) sq += (double)sqs[t];
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
+        if (threadIdx.x == 0) colsq[blockIdx.x] = sq;
+    }
 }
 
 __global__ void nn_scale_kernel(const double* __restrict__ colsq, int ncols, double n, float* __restrict__ scale) {
@@ -824,17 +830,22 @@ void nn_set_params(rtg_handle* h, const float* params, cudaStream_t s) {
 bool nn_has_params(rtg_handle* h) { return h->nn && h->nn->has_params; }
 
 template <typename T>
-static void colstats(rtg_handle* h, NNWs* w, const T* z, cudaStream_t s) {
+static void colstats(rtg_handle* h, NNWs* w, const T* z, bool with_sq, cudaStream_t s) {
     const OpView<T>& v = nview<T>(h);
-    const size_t smem = sizeof(float) * std::max(1, h->host.max_cells_col);
-    nn_colstats_kernel<T><<<v.ncols, 128, smem, s>>>(v, z, w->phi, w->em, w->cm, w->colsq), count_launch();
+    int max_nij = 1;
+    for (const ColDev& C : h->host.cols) max_nij = std::max(max_nij, C.nx * C.ny);
+    const size_t cells = (size_t)std::max(1, h->host.max_cells_col);
+    const size_t smem = sizeof(float) * (cells * max_nij * (with_sq ? 2 : 1) + cells + max_nij);
+    raise_smem_limit((const void*)nn_colstats_kernel<T>, smem);
+    nn_colstats_kernel<T><<<v.ncols, 128, smem, s>>>(v, z, w->phi, w->em, w->cm, with_sq ? w->colsq : nullptr),
+        count_launch();
 }
 
 template <typename T>
 void nn_moments(rtg_handle* h, const T* z, float* mom, float* scale, cudaStream_t s) {
     NNWs* w = get_nn(h);
     const OpView<T>& v = nview<T>(h);
-    colstats<T>(h, w, z, s);
+    colstats<T>(h, w, z, true, s);
     nn_scale_kernel<<<1, 1024, 0, s>>>(w->colsq, v.ncols, (double)h->host.ndof, scale), count_launch();
     nn_moments_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, z, w->phi, w->em, w->cm, w->nbr8, w->row_off, scale,
                                                            mom), count_launch();
@@ -845,7 +856,7 @@ template <typename T>
 void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s) {
     NNWs* w = get_nn(h);
     const OpView<T>& v = nview<T>(h);
-    colstats<T>(h, w, z, s);
+    colstats<T>(h, w, z, false, s);
     nn_correct_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, coef, w->phi, w->em, w->cm, w->nbr8, w->row_off, z), count_launch();
     RTG_CUDA(cudaGetLastError());
 }

@@ -717,6 +717,7 @@ struct Sweep {
     int64_t gmax32 = 0, gmax64 = 0;     // largest staged region (values) per precision
     int64_t g_entries = 0;
     int n_onephase32 = 0, n_onephase64 = 0;
+    int64_t g_read[2] = {0, 0}, up_read[2] = {0, 0};   // per sweep (FP32, FP64): map entries and upwind indices read
 };
 
 namespace {
@@ -912,6 +913,11 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             }
             if (ok & 1) s->gmax32 = std::max(s->gmax32, region32), ++s->n_onephase32;
             if (ok & 2) s->gmax64 = std::max(s->gmax64, region64), ++s->n_onephase64;
+            for (int p = 0; p < 2; ++p)
+                if (ok & (1 << p)) {
+                    s->g_read[p] += pad(nup * nloc, p ? 2 : 4);
+                    s->up_read[p] += nup;
+                }
             gel.push_back(e);
         }
         s->g_entries = gtot;
@@ -991,6 +997,16 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
     apply_sweep<T>(h, r, z, st, nullptr);
+}
+
+// one-phase elements of a precision, and the map entries and upwind indices
+// one sweep in that precision reads
+void sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind, cudaStream_t st) {
+    Sweep* s = get_sweep(h, st);
+    const int p = prec == RTG_FP64 ? 1 : 0;
+    if (onephase) *onephase = p ? s->n_onephase64 : s->n_onephase32;
+    if (map_entries) *map_entries = s->g_read[p];
+    if (upwind) *upwind = s->up_read[p];
 }
 
 // level of each element in the sweep order (host array of nelem)
