@@ -113,7 +113,7 @@ def test_to_scipy_small():
 
 def test_sweep_preconditioner_properties(case):
     """P^{-1} r: finite, zero at inflow-boundary DOFs, repeatable across calls
-    (per-element epoch flags), FP32 within 1e-4 of FP64, linear."""
+    (the sentinel fill before every sweep), FP32 within 1e-4 of FP64, linear."""
     import torch
     from rtg import _lib
     name, g, mesh, prob = case
