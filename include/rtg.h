@@ -296,8 +296,33 @@ int rtg_nn_loss_grad(const float* params, const float* feat, const float* mom, c
 /* one Adam step (bias-corrected, decoupled weight decay wd) on all parameters */
 int rtg_nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1,
                 float beta2, float eps, float wd, void* stream);
-/* z = M r = (I + L) P^{-1} r with the handle's network (the preconditioner of precond 2) */
+/* z = M r = (I + L) P^{-1} r with the handle's network (the preconditioner of precond 3) */
 int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stream);
+
+/* error indicators and hp steering of the AMR loop -------------------------
+ * Replace the reference's Error_Indicator methods (src/amr/Error_Indicator).
+ * u: device FP64 solution, full length N in the global DOF order.  Outputs
+ * are device FP64 arrays; errors are returned squared (the reference stores
+ * their square roots).  The first call builds the indicator tables (angular
+ * neighbours, face pairs with their interpolation matrices) on the handle. */
+/* angular jump (error/error_angular_jump.py:14-98): per element
+ * cell_err2[e] = 1/4 sum_ij wx_i wy_j (jl^2 + ju^2)/2, with jl, ju the jumps of
+ * u at theta pull-back -1 and +1 against the lower and upper angular neighbour
+ * cells of the column; col_err2[ncols] (may be NULL): sums over each column's
+ * cells in order. */
+int rtg_error_angular_jump(rtg_handle* h, const double* u, double* cell_err2, double* col_err2, void* stream);
+/* spatial jump (error/error_spatial_jump.py:17-247): col_err2[ncols] = the
+ * squared jumps of the column's face traces against every facing neighbour
+ * cell, projected on the finer face interval's LGL rule (the larger node
+ * count) times the smaller angular cell's LG rule and integrated, summed and
+ * divided by perimeter * 2 pi. */
+int rtg_error_spatial_jump(rtg_handle* h, const double* u, double* col_err2, void* stream);
+/* hp-steering estimates (col_hp_steer.py:14-64, cell_hp_steer.py:15-48):
+ * col_lp[ncols] from the Legendre coefficients of the angle-integrated
+ * solution, cell_lp[nelem] from those of the space-integrated solution (either
+ * may be NULL).  The reference refines a column in p when col_lp - 0.5 >=
+ * (nx + ny)/2 and a cell when cell_lp - 0.5 >= nth, else in h. */
+int rtg_hp_steer(rtg_handle* h, const double* u, double* col_lp, double* cell_lp, void* stream);
 
 /* allocation-free inner products --------------------------------------------
  * No counterpart in the reference: this is the two-stage reduction rtg_solve

@@ -276,6 +276,10 @@ void build_tables(const rtg_mesh_desc* m, const rtg_coeffs* c, HostTables& t) {
         throw RtgError{RTG_ERR_ARG, "null array in coefficient description"};
     const int nc = m->ncols, ne = m->nelem;
     if (m->col_elem_start[0] != 0 || m->col_elem_start[nc] != ne) fail("col_elem_start does not cover the elements");
+    t.col_pos.assign(m->col_pos, m->col_pos + 4 * (size_t)nc);
+    t.cell_pos.assign(m->cell_pos, m->cell_pos + 2 * (size_t)ne);
+    t.cell_lv.assign(m->cell_lv, m->cell_lv + ne);
+    t.cell_idx.assign(m->cell_idx, m->cell_idx + ne);
 
     // quadrature tables: LGL weights and G[n][p][i] = l'_p(x_i) w_i
     t.lglw.assign((size_t)(kMaxNodes + 1) * kMaxNodes, 0.);

@@ -188,6 +188,7 @@ void rtg_destroy(rtg_handle* h) {
     free_batch(h);
     free_coarse(h);
     free_nn(h);
+    free_amr(h);
     free_workspace(h);
     free_sweep(h);
     free_apply_plans(h);
@@ -356,6 +357,27 @@ int rtg_nn_precondition(rtg_handle* h, int prec, const void* r, void* z, void* s
         } else {
             throw RtgError{RTG_ERR_ARG, "unknown precision"};
         }
+    });
+}
+
+int rtg_error_angular_jump(rtg_handle* h, const double* u, double* cell_err2, double* col_err2, void* stream) {
+    return guard("rtg_error_angular_jump", [&] {
+        if (!h || !u || !cell_err2) throw RtgError{RTG_ERR_ARG, "null argument"};
+        error_angular_jump(h, u, cell_err2, col_err2, (cudaStream_t)stream);
+    });
+}
+
+int rtg_error_spatial_jump(rtg_handle* h, const double* u, double* col_err2, void* stream) {
+    return guard("rtg_error_spatial_jump", [&] {
+        if (!h || !u || !col_err2) throw RtgError{RTG_ERR_ARG, "null argument"};
+        error_spatial_jump(h, u, col_err2, (cudaStream_t)stream);
+    });
+}
+
+int rtg_hp_steer(rtg_handle* h, const double* u, double* col_lp, double* cell_lp, void* stream) {
+    return guard("rtg_hp_steer", [&] {
+        if (!h || !u) throw RtgError{RTG_ERR_ARG, "null argument"};
+        hp_steer(h, u, col_lp, cell_lp, (cudaStream_t)stream);
     });
 }
 

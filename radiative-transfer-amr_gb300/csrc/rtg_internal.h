@@ -136,6 +136,9 @@ struct HostTables {
     std::vector<int32_t> col_nbr8;   // [ncols][8] distinct neighbour columns, -1 padded
     std::vector<int32_t> col_nbr_raw;  // [ncols][4 faces][2] neighbour columns as given, -1 none
     std::vector<int32_t> col_free;   // [ncols] faces without a neighbour
+    std::vector<double> col_pos;     // [ncols][4] x0, y0, x1, y1
+    std::vector<double> cell_pos;    // [nelem][2] th0, th1
+    std::vector<int32_t> cell_lv, cell_idx;   // [nelem] angular level and index
     int64_t ndof = 0, ndof_interior = 0;
     int32_t nnodes = 0;              // spatial nodes over all columns
     int32_t max_col_ndof = 0, max_nth_col = 0, max_cells_col = 0;
@@ -152,6 +155,7 @@ struct ApplyPlan;  // column partition of the apply kernels (rtg_apply.cu)
 struct BatchWs;    // batched-solve workspace (rtg_batch.cu)
 struct NNWs;       // learned correction of the sweep (rtg_nn.cu)
 struct Coarse;     // coarse-space correction of the two-level preconditioner (rtg_coarse.cu)
+struct AmrTables;  // error indicators and hp steering (rtg_amr.cu)
 
 }  // namespace rtg
 
@@ -171,6 +175,7 @@ struct rtg_handle {
     rtg::BatchWs* bws = nullptr;
     rtg::NNWs* nn = nullptr;
     rtg::Coarse* coarse = nullptr;
+    rtg::AmrTables* amr = nullptr;
 };
 
 namespace rtg {
@@ -233,6 +238,13 @@ void apply_learned(rtg_handle* h, T* z, cudaStream_t s);
 // Two-level preconditioner (rtg_coarse.cu): column diffusion correction
 void build_coarse(rtg_handle* h, cudaStream_t s);
 void free_coarse(rtg_handle* h);
+
+// Error indicators and hp steering (rtg_amr.cu)
+void free_amr(rtg_handle* h);
+void error_angular_jump(rtg_handle* h, const double* u, double* cell_err2, double* col_err2, cudaStream_t s);
+void error_spatial_jump(rtg_handle* h, const double* u, double* col_err2, cudaStream_t s);
+void hp_steer(rtg_handle* h, const double* u, double* col_lp, double* cell_lp, cudaStream_t s);
+int64_t error_jump_pairs(rtg_handle* h);
 int coarse_size(rtg_handle* h);
 void coarse_operator(rtg_handle* h, double* out);
 template <typename T>

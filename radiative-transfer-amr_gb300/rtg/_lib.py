@@ -97,6 +97,9 @@ SIGNATURES = {
                                    C.c_void_p, C.c_void_p]),
     "rtg_sweep_info": (C.c_int, [C.c_void_p, i32p, i32p, i64p, C.c_void_p]),
     "rtg_apply_tuning": (C.c_int, [C.c_void_p, i32p, C.c_int, i32p, C.c_void_p]),
+    "rtg_error_angular_jump": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_error_spatial_jump": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtg_hp_steer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_sweep_maps": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_void_p]),
     "rtg_sweep_trace": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, i32p, C.c_void_p]),
     "rtg_nn_rows": (C.c_int, [C.c_void_p, i64p]),

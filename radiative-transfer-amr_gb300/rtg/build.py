@@ -17,7 +17,7 @@ INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "librtg.so")
 SOURCES = ["rtg_build.cpp", "rtg_apply.cu", "rtg_krylov.cu", "rtg_sweep.cu", "rtg_batch.cu",
-           "rtg_nn.cu", "rtg_coarse.cu", "rtg_capi.cu", "rtg_noalloc.cu"]
+           "rtg_nn.cu", "rtg_coarse.cu", "rtg_amr.cu", "rtg_capi.cu", "rtg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
