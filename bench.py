@@ -245,6 +245,59 @@ def kernel_time(fn, stream, flush, reps=20):
     return statistics.median(durs)
 
 
+def amr_indicators(ctx, mesh, u_host, stream, flush, with_cpu):
+    """The AMR step after the solve on the solution: the librtg indicator
+    kernels (CUDA events, L2 flushed), the whole rtg.ErrorIndicator methods
+    (host flags included, wall clock), and the CPU restatement's time (oracle
+    port, one core) on the same mesh and vector."""
+    import torch
+    from rtg import ErrorIndicator, Projection, _lib
+    N = ctx.N
+    lay = ctx.layout
+    ud = ctx.to_device(u_host)
+    ce = torch.empty(lay.nelem, dtype=torch.float64, device=ctx.device)
+    cc = torch.empty(lay.ncols, dtype=torch.float64, device=ctx.device)
+    cl = torch.empty(lay.ncols, dtype=torch.float64, device=ctx.device)
+    el = torch.empty(lay.nelem, dtype=torch.float64, device=ctx.device)
+    lib, h, sp = ctx.lib, ctx.h, C.c_void_p(stream.cuda_stream)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    t0 = time.perf_counter()
+    _lib.check(lib.rtg_error_spatial_jump(h, p(ud), p(cc), sp))   # first call builds the pair tables
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    t_ang = kernel_time(lambda: _lib.check(lib.rtg_error_angular_jump(h, p(ud), p(ce), p(cc), sp)), stream, flush)
+    t_spt = kernel_time(lambda: _lib.check(lib.rtg_error_spatial_jump(h, p(ud), p(cc), sp)), stream, flush)
+    t_hp = kernel_time(lambda: _lib.check(lib.rtg_hp_steer(h, p(ud), p(cl), p(el), sp)), stream, flush)
+    proj = Projection(mesh)
+    proj.from_vector(u_host)
+    walls = {}
+    for kind in ("angular", "spatial"):
+        ts = []
+        for _ in range(4):
+            ind = ErrorIndicator(proj, "all", "hp", (0.5, 0.5), ctx=ctx)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            (ind.error_angular_jump if kind == "angular" else ind.error_spatial_jump)()
+            ts.append(time.perf_counter() - t0)
+        walls[kind] = statistics.median(ts[1:])
+    out = {"workload": "indicators on the solution of the same problem", "ndof": N,
+           "setup_s": setup,
+           "angular_jump_us": 1e6 * t_ang, "spatial_jump_us": 1e6 * t_spt, "hp_steer_us": 1e6 * t_hp,
+           "error_angular_jump_method_s": walls["angular"], "error_spatial_jump_method_s": walls["spatial"],
+           "dof_per_s_spatial_jump": N / t_spt}
+    if with_cpu:
+        from oracle import amr_oracle as AO
+        t0 = time.perf_counter()
+        AO.indicator(mesh, u_host, "ang", "all", "hp", (0.5, 0.5))
+        t1 = time.perf_counter()
+        AO.indicator(mesh, u_host, "spt", "all", "hp", (0.5, 0.5))
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "angular_s": t1 - t0, "spatial_s": t2 - t1,
+                               "sample": "whole mesh: oracle restatement (numpy) of error_angular_jump and "
+                                         "error_spatial_jump with the flags and hp steering they trigger"}
+    return out
+
+
 def profiled_traffic(name):
     """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
     (line "traffic_bytes_per_launch: N"), or None."""
@@ -460,6 +513,7 @@ def run_ours(args):
                            "dof_applies_per_s": N / t_apply},
         "clocks": clk.summary(),
     }
+    out["amr_indicators"] = amr_indicators(ctx, mesh, u_ref_h, stream, flush, not args.no_cpu)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(mesh, spec, rtols["plain_fp64"], u_ref_h, w)
     return out

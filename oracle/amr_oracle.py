@@ -149,12 +149,12 @@ def col_lp(mesh, u, ck, V=None):
     jj = np.arange(ny)
     Ly = np.array([eval_legendre(j, yb) for j in jj])           # [ny(j), ny(q)]
     a_x = (2. * nx - 1.) * (2. * jj + 1.) / 4. * (Lx @ W @ Ly.T)
-    ax2 = float(np.sum(a_x ** 2 * (2. / (2. * jj + 1.))))
+    ax2 = np.float64(np.sum(a_x ** 2 * (2. / (2. * jj + 1.))))   # numpy scalars: x/0 -> inf as in the reference
     ii = np.arange(nx)
     Lxi = np.array([eval_legendre(i, xb) for i in ii])
     Lyn = eval_legendre(ny - 1, yb)
     a_y = (2. * ii + 1.) * (2. * ny - 1.) / 4. * (Lxi @ W @ Lyn)
-    ay2 = float(np.sum(a_y ** 2 * (2. / (2. * ii + 1.))))
+    ay2 = np.float64(np.sum(a_y ** 2 * (2. / (2. * ii + 1.))))
     with np.errstate(divide="ignore", invalid="ignore"):
         t0 = np.log((2. * nx - 1.) / (2 * ax2)) / (2. * np.log(nx - 1.))
         t1 = np.log((2. * ny - 1.) / (2 * ay2)) / (2. * np.log(ny - 1.))
@@ -173,7 +173,7 @@ def cell_lp(mesh, u, ck, kk, V=None):
     nth = col.cells[kk].ndofs[0]
     tb, wt = O.lg_nodes(nth)
     uh = (x1 - x0) * (y1 - y0) / 4. * np.sum(wx.reshape(nx, 1, 1) * wy.reshape(1, ny, 1) * V[(ck, kk)], axis=(0, 1))
-    a = (2. * nth - 1.) / 2. * float(np.sum(wt * uh * eval_legendre(nth - 1, tb)))
+    a = (2. * nth - 1.) / 2. * np.float64(np.sum(wt * uh * eval_legendre(nth - 1, tb)))
     asq = a * a * (2. / (2. * nth - 1.))
     with np.errstate(divide="ignore", invalid="ignore"):
         return float(np.log((2. * nth - 1.) / (2 * asq)) / (2. * np.log(nth - 1.)))

@@ -43,24 +43,21 @@ struct JumpPair {
 };
 
 // Table layout (doubles): LGL nodes, LGL weights, LG nodes, LG weights, LG
-// basis at +1, LG basis at -1 (each [kMaxNodes+1][kMaxNodes]), then the pair
-// matrices.
+// basis at +1, LG basis at -1 (each [kMaxNodes+1][kMaxNodes]); Legendre
+// values P_k at the LGL and at the LG nodes ([kMaxNodes+1][k][i], each
+// kMaxNodes * kNT); then the pair matrices.
 enum { kLglX = 0, kLglW = 1, kLgX = 2, kLgW = 3, kLgTop = 4, kLgBot = 5, kNodeTables = 6 };
+constexpr size_t kLegLgl = (size_t)kNodeTables * kNT;
+constexpr size_t kLegLg = kLegLgl + (size_t)kMaxNodes * kNT;
+constexpr size_t kTabHead = kLegLg + (size_t)kMaxNodes * kNT;
+
+// P_k at node i of the n-node LGL (lg = false) or LG (lg = true) rule
+__device__ __forceinline__ double leg_at(const double* tab, bool lg, int n, int k, int i) {
+    return tab[(lg ? kLegLg : kLegLgl) + (size_t)n * kMaxNodes * kMaxNodes + (size_t)k * kMaxNodes + i];
+}
 
 __device__ __forceinline__ const double* ntab(const double* tab, int which, int n) {
     return tab + (size_t)which * kNT + (size_t)n * kMaxNodes;
-}
-
-// Legendre polynomial P_n(x) by the three-term recurrence.
-__device__ __forceinline__ double legendre(int n, double x) {
-    if (n == 0) return 1.;
-    double p0 = 1., p1 = x;
-    for (int k = 1; k < n; ++k) {
-        const double p2 = ((2. * k + 1.) * x * p1 - k * p0) / (k + 1.);
-        p0 = p1;
-        p1 = p2;
-    }
-    return p1;
 }
 
 // top/bot[enode_off[e] + ij] = sum_a u[e, ij, a] l_a(+1 / -1)
@@ -197,18 +194,17 @@ spt_jump_kernel(OpView<double> v, const double* __restrict__ tab, const JumpPair
 
 // Per column: uh[i][j] = sum_cells (dth/2) sum_a wth_a u, W = wx wy uh, then
 // a_nx,j = (2nx-1)(2j+1)/4 sum_i sum_q P_{nx-1}(x_i) W[i][q] P_j(y_q) and its
-// transpose counterpart, and lp = (term_x + term_y) / 2.
+// transpose counterpart (contracted one index at a time), and
+// lp = (term_x + term_y) / 2.
 __global__ void hp_col_kernel(OpView<double> v, const double* __restrict__ tab, const double* __restrict__ u,
                               double* __restrict__ col_lp) {
     __shared__ double W[kMaxNodes * kMaxNodes];
-    __shared__ double ax[kMaxNodes], ay[kMaxNodes];
+    __shared__ double rx[kMaxNodes], ry[kMaxNodes], ax[kMaxNodes], ay[kMaxNodes];
     const int c = blockIdx.x;
     const ColDev C = v.cols[c];
     const int nx = C.nx, ny = C.ny, nn = nx * ny;
     const double* wx = ntab(tab, kLglW, nx);
     const double* wy = ntab(tab, kLglW, ny);
-    const double* xx = ntab(tab, kLglX, nx);
-    const double* yy = ntab(tab, kLglX, ny);
     for (int ij = threadIdx.x; ij < nn; ij += blockDim.x) {
         double uh = 0.;
         for (int e = C.elem_begin; e < C.elem_end; ++e) {
@@ -222,22 +218,28 @@ __global__ void hp_col_kernel(OpView<double> v, const double* __restrict__ tab, 
         W[ij] = wx[ij / ny] * wy[ij % ny] * uh;
     }
     __syncthreads();
+    // rx[q] = sum_i P_{nx-1}(x_i) W[i][q]; ry[i] = sum_q W[i][q] P_{ny-1}(y_q)
+    if ((int)threadIdx.x < ny) {
+        const int q = threadIdx.x;
+        double s = 0.;
+        for (int i = 0; i < nx; ++i) s += leg_at(tab, false, nx, nx - 1, i) * W[i * ny + q];
+        rx[q] = s;
+    } else if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + nx) {
+        const int i = threadIdx.x - 32;
+        double s = 0.;
+        for (int q = 0; q < ny; ++q) s += W[i * ny + q] * leg_at(tab, false, ny, ny - 1, q);
+        ry[i] = s;
+    }
+    __syncthreads();
     if ((int)threadIdx.x < ny) {
         const int j = threadIdx.x;
         double s = 0.;
-        for (int i = 0; i < nx; ++i) {
-            const double li = legendre(nx - 1, xx[i]);
-            for (int q = 0; q < ny; ++q) s += li * W[i * ny + q] * legendre(j, yy[q]);
-        }
+        for (int q = 0; q < ny; ++q) s += rx[q] * leg_at(tab, false, ny, j, q);
         ax[j] = (2. * nx - 1.) * (2. * j + 1.) / 4. * s;
-    }
-    if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + nx) {
+    } else if ((int)threadIdx.x >= 32 && (int)threadIdx.x < 32 + nx) {
         const int i = threadIdx.x - 32;
         double s = 0.;
-        for (int p = 0; p < nx; ++p) {
-            const double lp = legendre(i, xx[p]);
-            for (int q = 0; q < ny; ++q) s += lp * W[p * ny + q] * legendre(ny - 1, yy[q]);
-        }
+        for (int p = 0; p < nx; ++p) s += leg_at(tab, false, nx, i, p) * ry[p];
         ay[i] = (2. * i + 1.) * (2. * ny - 1.) / 4. * s;
     }
     __syncthreads();
@@ -265,17 +267,15 @@ __global__ void hp_cell_kernel(OpView<double> v, const double* __restrict__ tab,
     const double* wx = ntab(tab, kLglW, C.nx);
     const double* wy = ntab(tab, kLglW, C.ny);
     const double* wt = ntab(tab, kLgW, nth);
-    const double* tb = ntab(tab, kLgX, nth);
+    // lanes over (node, angle) pairs: coalesced reads of the element
     double part = 0.;
-    for (int a = lane; a < nth; a += 32) {
-        double s = 0.;
-        for (int ij = 0; ij < nn; ++ij) s += wx[ij / C.ny] * wy[ij % C.ny] * u[E.dof_off + (int64_t)ij * nth + a];
-        const double uh = (C.dx * C.dy) / 4. * s;
-        part += wt[a] * uh * legendre(nth - 1, tb[a]);
+    for (int t = lane; t < nn * nth; t += 32) {
+        const int ij = t / nth, a = t % nth;
+        part += wx[ij / C.ny] * wy[ij % C.ny] * u[E.dof_off + t] * wt[a] * leg_at(tab, true, nth, nth - 1, a);
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
     if (lane == 0) {
-        const double an = (2. * nth - 1.) / 2. * part;
+        const double an = (2. * nth - 1.) / 2. * ((C.dx * C.dy) / 4. * part);
         const double asq = an * an * (2. / (2. * nth - 1.));
         cell_lp[e] = log((2. * nth - 1.) / (2. * asq)) / (2. * log((double)nth - 1.));
     }
@@ -333,6 +333,7 @@ AmrTables* get_amr(rtg_handle* h) {
     try {
         // node tables
         std::vector<double> tab((size_t)kNodeTables * kNT, 0.);
+        tab.reserve(kTabHead);
         double xw[2][kMaxNodes];
         for (int n = 1; n <= kMaxNodes; ++n) {
             quad_lgl(n, xw[0], xw[1]);
@@ -348,6 +349,27 @@ AmrTables* get_amr(rtg_handle* h) {
                 tab[(size_t)kLgBot * kNT + n * kMaxNodes + i] = lagrange(xw[0], n, i, -1.);
             }
         }
+        tab.resize(kTabHead, 0.);
+        for (int lgrule = 0; lgrule < 2; ++lgrule)
+            for (int n = 1; n <= kMaxNodes; ++n) {
+                const double* xs = &tab[(size_t)(lgrule ? kLgX : kLglX) * kNT + (size_t)n * kMaxNodes];
+                for (int i = 0; i < n; ++i) {
+                    // P_k(x) by the three-term recurrence
+                    double p0 = 1., p1 = xs[i];
+                    for (int k = 0; k < kMaxNodes; ++k) {
+                        const double pk = k == 0 ? 1. : (k == 1 ? xs[i] : 0.);
+                        double val = pk;
+                        if (k >= 2) {
+                            const double p2 = ((2. * (k - 1) + 1.) * xs[i] * p1 - (k - 1) * p0) / k;
+                            p0 = p1;
+                            p1 = p2;
+                            val = p2;
+                        }
+                        tab[(lgrule ? kLegLg : kLegLgl) + (size_t)n * kMaxNodes * kMaxNodes + (size_t)k * kMaxNodes + i] =
+                            val;
+                    }
+                }
+            }
         auto nodes = [&](int which, int n) { return &tab[(size_t)which * kNT + (size_t)n * kMaxNodes]; };
         // angular neighbours: the column's cells in theta order, cyclic
         std::vector<int32_t> cnbr(2 * (size_t)ne, 0);

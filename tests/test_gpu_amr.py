@@ -98,3 +98,34 @@ def test_indicators_on_adaptive_mesh_match_oracle():
     assert [ind.cell_hp_steer(k, kk) for k, kk in cells] == \
         [AO.cell_form(mesh, k, kk, AO.cell_lp(mesh, u, k, kk, V)) for k, kk in cells]
     ind.close()
+
+
+@pytest.mark.parametrize("field", ["zero", "constant"])
+def test_indicators_edge_fields(field):
+    """A zero field (every jump exactly 0 and every lp infinite: the top
+    coefficients vanish): errors, flags and forms as the oracle's, including
+    the threshold ties (0 >= tol * 0 flags everything).  A constant field:
+    every jump zero to rounding (which cells pass a threshold set by rounding
+    residue is not compared)."""
+    from rtg import ErrorIndicator, Projection, workloads as W
+    mesh = W.hanging_hp_mesh()
+    proj = Projection(mesh, (lambda x, y, th: 0. * x) if field == "zero" else (lambda x, y, th: 0. * x + 2.5))
+    u = np.asarray(proj.to_vector())
+    for kind in ("ang", "spt"):
+        ind = ErrorIndicator(proj, "all", "hp", (0.5, 0.5))
+        (ind.error_angular_jump if kind == "ang" else ind.error_spatial_jump)()
+        ref = AO.indicator(mesh, u, kind, "all", "hp", (0.5, 0.5))
+        cols = sorted(mesh.cols.keys())
+        assert ind.error == pytest.approx(ref["error"], abs=1e-13)
+        if field == "constant":
+            assert ind.error <= 1e-12
+            ind.close()
+            continue
+        assert [ind.cols[k].do_ref for k in cols] == [ref["cols"][k]["do_ref"] for k in cols]
+        assert [ind.cols[k].ref_form for k in cols] == [ref["cols"][k]["ref_form"] for k in cols]
+        cells = [(k, kk) for k in cols for kk in sorted(mesh.cols[k].cells)]
+        assert [ind.cols[k].cells[kk].do_ref for k, kk in cells] == [ref["cols"][k]["cells"][kk]["do_ref"]
+                                                                      for k, kk in cells]
+        assert [ind.cols[k].cells[kk].ref_form for k, kk in cells] == [ref["cols"][k]["cells"][kk]["ref_form"]
+                                                                        for k, kk in cells]
+        ind.close()
