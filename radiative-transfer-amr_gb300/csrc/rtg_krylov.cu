@@ -449,8 +449,15 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
 
     inf.rhs_norm = norm2(h, ws, ws->b, s);
     const double tol = std::max(o->rtol * inf.rhs_norm, o->atol);
-    double res = residual64(h, ws, ws->b, ws->x, ws->r, s);
-    inf.fp64_applies++;
+    double res;
+    if (o->nonzero_guess) {
+        res = residual64(h, ws, ws->b, ws->x, ws->r, s);
+        inf.fp64_applies++;
+    } else {
+        // x0 = 0: r0 = b, no apply
+        axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->b, 0., ws->r, N), count_launch();
+        res = inf.rhs_norm;
+    }
     inf.res0 = res;
     hv.push_back(res);
     int applies32 = 0, applies64 = 0;
