@@ -276,6 +276,19 @@ __global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z) {
     }
 }
 
+// Row length (values) of an element's upwind map in precision T: nup rounded
+// up so that a row is a whole number of 16-byte units and the number of units
+// is odd (rows of consecutive outputs then start in different 16-byte bank
+// groups, so 16-byte loads of a quarter warp do not conflict).
+template <typename T>
+__host__ __device__ __forceinline__ int map_ld(int nup) {
+    constexpr int kVec = 16 / (int)sizeof(T);
+    if (nup <= 0) return 0;
+    int r = (nup + kVec - 1) / kVec * kVec;
+    if ((r / kVec) % 2 == 0) r += kVec;
+    return r;
+}
+
 // Asynchronous global -> shared copies (cp.async): every copy of a staging
 // loop is in flight at once and no register holds the data.
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
@@ -302,15 +315,43 @@ __device__ __forceinline__ bool on_face(int F, int i, int j, int nx, int ny) {
 // Upwind maps of the elements that take the one-phase path: for element e
 // with nup upwind values (the facing node lines of its active couplings, in
 // coupling order, then jj, then a), G_e = -B_e C_e maps them to the element's
-// values: z_e = B_e rin_e + G_e z_upwind.  G is stored [u][l] (l = ij*nth + r),
-// each element's block starting on a 16-byte boundary.  Shared memory of
-// the path (after rhs and zpre): upwind values [nup, padded to 16 bytes] |
-// G_e [nup*nloc, padded] | B_e [nth*nn*nn].
+// values: z_e = B_e rin_e + G_e z_upwind.  G is stored by output row
+// (l = ij*nth + r), each row map_ld<T>(nup) values long (zero padded), each
+// element's block on a 16-byte boundary; FP32 and FP64 copies have their own
+// offsets.  Shared memory of the path (after rhs and zpre): upwind values
+// [map_ld, zero padded] | G_e [nloc * map_ld] | B_e [nth*nn*nn].
+// acc + sum over 16-byte units q0 <= q < q1 of a map row times the upwind
+// values (16-byte loads; four independent partial sums in FP32, two in FP64)
+__device__ __forceinline__ float map_row(const float* g, const float* zl, int q0, int q1, float acc) {
+    float a0 = acc, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    const float4* g4 = reinterpret_cast<const float4*>(g);
+    const float4* z4 = reinterpret_cast<const float4*>(zl);
+    for (int q = q0; q < q1; ++q) {
+        const float4 gv = g4[q], zv = z4[q];
+        a0 = fmaf(gv.x, zv.x, a0);
+        a1 = fmaf(gv.y, zv.y, a1);
+        a2 = fmaf(gv.z, zv.z, a2);
+        a3 = fmaf(gv.w, zv.w, a3);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+__device__ __forceinline__ double map_row(const double* g, const double* zl, int q0, int q1, double acc) {
+    double a0 = acc, a1 = 0.;
+    const double2* g2 = reinterpret_cast<const double2*>(g);
+    const double2* z2 = reinterpret_cast<const double2*>(zl);
+    for (int q = q0; q < q1; ++q) {
+        const double2 gv = g2[q], zv = z2[q];
+        a0 = fma(gv.x, zv.x, a0);
+        a1 = fma(gv.y, zv.y, a1);
+    }
+    return a0 + a1;
+}
+
 template <typename T>
 struct UpwindMap {
     const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
     const int32_t* nup = nullptr;    // per element: upwind values
-    const int64_t* goff = nullptr;   // per element: first entry of G_e
+    const int64_t* goff = nullptr;   // per element: first entry of G_e (this precision's copy)
     const int64_t* uoff = nullptr;   // per element: first entry of its upwind index list
     const int64_t* up = nullptr;     // upwind value offsets into z
     const T* G = nullptr;
@@ -370,14 +411,14 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             // then z = zpre + G_e z_upwind once the upwind values arrive
             constexpr int kVec = 16 / sizeof(T);   // values per 16-byte copy
             const int nup = um.nup[e];
-            const int nupp = (nup + kVec - 1) / kVec * kVec;
-            const int gsz = nup * nloc, gszp = (gsz + kVec - 1) / kVec * kVec;
+            const int ld = map_ld<T>(nup);
+            const int gsz = ld * nloc;             // a multiple of kVec
             T* zl = Bs;
-            T* Gs = Bs + nupp;
-            T* Bg = Gs + gszp;
+            T* Gs = Bs + ld;
+            T* Bg = Gs + gsz;
             const T* Gg = um.G + um.goff[e];
             const int64_t* up = um.up + um.uoff[e];
-            for (int t = threadIdx.x; t < gszp / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
+            for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
             for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bg + t, B + t);
             for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
                 const int ij = l / nth;
@@ -399,11 +440,13 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 trace[kTr * e + 1] = globaltimer_ns();
                 ck0 = clock64();
             }
-            for (int u = threadIdx.x; u < nup; u += blockDim.x) {
-                const int64_t o = u == threadIdx.x ? my_up : __ldg(up + u);
+            for (int u = threadIdx.x; u < ld; u += blockDim.x) {
                 T val = T(0);
-                if (!load_published(z + o, val, status)) s_abort = 1;
-                zl[u] = val;
+                if (u < nup) {
+                    const int64_t o = u == threadIdx.x ? my_up : __ldg(up + u);
+                    if (!load_published(z + o, val, status)) s_abort = 1;
+                }
+                zl[u] = val;   // padding: zero
             }
             __syncthreads();
             if (s_abort) break;
@@ -413,25 +456,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             // (free once zpre is formed).  FP32 is latency bound and keeps one
             // thread per output (the extra barrier costs more than it saves).
             const bool split = sizeof(T) == 8 && 2 * nloc <= (int)blockDim.x;
-            const int uh = split ? (nup + 1) / 2 : nup;
+            const int nvec = ld / kVec;                 // 16-byte units per row
+            const int vh = split ? (nvec + 1) / 2 : nvec;
             T part = T(0);
             const int t = threadIdx.x;
             const int l = split ? t % nloc : t;
             const int half = split ? t / nloc : 0;
             if (!split || t < 2 * nloc) {
                 for (int l2 = l; l2 < nloc; l2 += blockDim.x) {
-                    const int u0 = half ? uh : 0, u1 = half ? nup : uh;
-                    T a0 = half ? T(0) : zpre[l2], a1 = T(0), a2 = T(0), a3 = T(0);
-                    const T* g = Gs + l2;
-                    int u = u0;
-                    for (; u + 4 <= u1; u += 4) {
-                        a0 += g[(u + 0) * nloc] * zl[u + 0];
-                        a1 += g[(u + 1) * nloc] * zl[u + 1];
-                        a2 += g[(u + 2) * nloc] * zl[u + 2];
-                        a3 += g[(u + 3) * nloc] * zl[u + 3];
-                    }
-                    for (; u < u1; ++u) a0 += g[u * nloc] * zl[u];
-                    part = (a0 + a1) + (a2 + a3);
+                    const int q0 = half ? vh : 0, q1 = half ? nvec : vh;
+                    part = map_row(Gs + (size_t)l2 * ld, zl, q0, q1, half ? T(0) : zpre[l2]);
                     if (half) rhs[l2] = part;
                     else if (!split) st_relaxed(z + E.dof_off + l2, part);
                 }
@@ -641,15 +675,15 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
 }
 
 // Builds the upwind maps G_e = -B_e C_e of the one-phase elements in FP64
-// (and their FP32 copies): entry (u, l) with u = (coupling k, jj, a) and
-// l = (ij, r) is -dcoeff_k Et_k[a][r] sum_q B_r[ij][f_q] Es_k[jj][q] over the
+// (and their FP32 copies; rows of map_ld values, padding left zero): entry
+// (u, l) with u = (coupling k, jj, a) and l = (ij, r) is -dcoeff_k Et_k[a][r] sum_q B_r[ij][f_q] Es_k[jj][q] over the
 // nodes f_q of coupling k's face that are not inflow-boundary nodes.  One CTA
 // per element.
 __global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restrict__ active,
                                         const double* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                                         const int32_t* __restrict__ elems, const int32_t* __restrict__ nup_e,
-                                        const int64_t* __restrict__ goff, double* __restrict__ G64,
-                                        float* __restrict__ G32) {
+                                        const int64_t* __restrict__ goff64, const int64_t* __restrict__ goff32,
+                                        double* __restrict__ G64, float* __restrict__ G32) {
     const int e = elems[blockIdx.x];
     const ElemDev E = v.elems[e];
     const ColDev C = v.cols[E.col];
@@ -679,8 +713,8 @@ __global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restr
             acc += B[(int64_t)r * nn * nn + (int64_t)(i * C.ny + j) * nn + ij] * v.mort[cp.es + jj * n0 + q];
         }
         const double val = -v.cplc[k] * et * acc;
-        G64[goff[e] + t] = val;
-        G32[goff[e] + t] = (float)val;
+        G64[goff64[e] + (int64_t)l * map_ld<double>(nup) + u] = val;
+        G32[goff32[e] + (int64_t)l * map_ld<float>(nup) + u] = (float)val;
     }
 }
 
@@ -711,7 +745,7 @@ struct Sweep {
     // one-phase elements (upwind maps)
     uint8_t* d_gok = nullptr;
     int32_t* d_gnup = nullptr;
-    int64_t *d_goff = nullptr, *d_uoff = nullptr, *d_up = nullptr;
+    int64_t *d_goff64 = nullptr, *d_goff32 = nullptr, *d_uoff = nullptr, *d_up = nullptr;
     double* d_G64 = nullptr;
     float* d_G32 = nullptr;
     int64_t gmax32 = 0, gmax64 = 0;     // largest staged region (values) per precision
@@ -882,8 +916,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
         std::vector<uint8_t> gok(ne, 0);
         std::vector<int32_t> gnup(ne, 0), gel;
-        std::vector<int64_t> goff(ne, 0), uoff(ne, 0), up;
-        int64_t gtot = 0;
+        std::vector<int64_t> goff64(ne, 0), goff32(ne, 0), uoff(ne, 0), up;
+        int64_t gtot64 = 0, gtot32 = 0;
         for (int e = 0; e < ne; ++e) {
             const ElemDev& E = t.elems[e];
             const ColDev& C = t.cols[E.col];
@@ -891,20 +925,22 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             int64_t nup = 0;
             for (int k = E.cpl_begin; k < E.cpl_end; ++k)
                 if (active[k]) nup += (int64_t)t.cgeo[k].m1 * t.cgeo[k].nth1;
-            // upwind values and G_e padded to 16 bytes (4 floats), then B_e
+            // upwind values (one map row long), G_e, then B_e
             const int64_t bsize = (int64_t)E.nth * C.nx * C.ny * C.nx * C.ny;
-            auto pad = [](int64_t n, int64_t q) { return (n + q - 1) / q * q; };
-            const int64_t region32 = pad(nup, 4) + pad(nup * nloc, 4) + bsize;
-            const int64_t region64 = pad(nup, 2) + pad(nup * nloc, 2) + bsize;
+            const int64_t ld32 = map_ld<float>((int)nup), ld64 = map_ld<double>((int)nup);
+            const int64_t region32 = ld32 + ld32 * nloc + bsize;
+            const int64_t region64 = ld64 + ld64 * nloc + bsize;
             uint8_t ok = 0;
             if (region32 * 4 + 2 * rhs_cap * 4 <= (int64_t)kSweepSmemBudget) ok |= 1;
             if (region64 * 8 + 2 * rhs_cap * 8 <= (int64_t)kSweepSmemBudget) ok |= 2;
             if (!ok) continue;
             gok[e] = ok;
             gnup[e] = (int32_t)nup;
-            goff[e] = gtot;
+            goff64[e] = gtot64;
+            goff32[e] = gtot32;
             uoff[e] = (int64_t)up.size();
-            gtot += pad(nup * nloc, 4);
+            gtot64 += ld64 * nloc;
+            gtot32 += ld32 * nloc;
             for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
                 if (!active[k]) continue;
                 const CplGeo& g = t.cgeo[k];
@@ -915,30 +951,35 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             if (ok & 2) s->gmax64 = std::max(s->gmax64, region64), ++s->n_onephase64;
             for (int p = 0; p < 2; ++p)
                 if (ok & (1 << p)) {
-                    s->g_read[p] += pad(nup * nloc, p ? 2 : 4);
+                    s->g_read[p] += (p ? ld64 : ld32) * nloc;
                     s->up_read[p] += nup;
                 }
             gel.push_back(e);
         }
-        s->g_entries = gtot;
+        s->g_entries = gtot64 + gtot32;
         s->d_gok = sw_alloc<uint8_t>(s, ne);
         s->d_gnup = sw_alloc<int32_t>(s, ne);
-        s->d_goff = sw_alloc<int64_t>(s, ne);
+        s->d_goff64 = sw_alloc<int64_t>(s, ne);
+        s->d_goff32 = sw_alloc<int64_t>(s, ne);
         s->d_uoff = sw_alloc<int64_t>(s, ne);
         s->d_up = sw_alloc<int64_t>(s, up.size());
-        s->d_G64 = sw_alloc<double>(s, gtot);
-        s->d_G32 = sw_alloc<float>(s, gtot);
+        s->d_G64 = sw_alloc<double>(s, gtot64);
+        s->d_G32 = sw_alloc<float>(s, gtot32);
+        RTG_CUDA(cudaMemset(s->d_G64, 0, sizeof(double) * std::max<int64_t>(gtot64, 1)));
+        RTG_CUDA(cudaMemset(s->d_G32, 0, sizeof(float) * std::max<int64_t>(gtot32, 1)));
         int32_t* d_gel = sw_alloc<int32_t>(s, gel.size());
         RTG_CUDA(cudaMemcpy(s->d_gok, gok.data(), ne, cudaMemcpyHostToDevice));
         RTG_CUDA(cudaMemcpy(s->d_gnup, gnup.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
-        RTG_CUDA(cudaMemcpy(s->d_goff, goff.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_goff64, goff64.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_goff32, goff32.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
         RTG_CUDA(cudaMemcpy(s->d_uoff, uoff.data(), sizeof(int64_t) * ne, cudaMemcpyHostToDevice));
         if (!up.empty())
             RTG_CUDA(cudaMemcpy(s->d_up, up.data(), sizeof(int64_t) * up.size(), cudaMemcpyHostToDevice));
         if (!gel.empty()) {
             RTG_CUDA(cudaMemcpy(d_gel, gel.data(), sizeof(int32_t) * gel.size(), cudaMemcpyHostToDevice));
             build_upwind_map_kernel<<<(int)gel.size(), 256, 0, st>>>(h->v64, s->d_active, s->d_inv64, s->d_inv_off,
-                                                                    d_gel, s->d_gnup, s->d_goff, s->d_G64, s->d_G32), count_launch();
+                                                                    d_gel, s->d_gnup, s->d_goff64, s->d_goff32, s->d_G64,
+                                                                    s->d_G32), count_launch();
             RTG_CUDA(cudaGetLastError());
         }
     }
@@ -984,7 +1025,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     UpwindMap<T> um;
     um.ok = s->d_gok;
     um.nup = s->d_gnup;
-    um.goff = s->d_goff;
+    um.goff = f64 ? s->d_goff64 : s->d_goff32;
     um.uoff = s->d_uoff;
     um.up = s->d_up;
     um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
