@@ -281,7 +281,7 @@ float* flex_basis<float>(Workspace* ws, int m) {
 template <typename T>
 GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T* V, int m,
                   double tol_abs, int max_it, std::vector<double>* hist, int* applies,
-                  PcState& pc, T* zbuf, T* tbuf, cudaStream_t s) {
+                  PcState& pc, cudaStream_t s) {
     const int64_t N = ws->N;
     GmresResult res;
     const OpView<T>& v = view<T>(h);
@@ -316,29 +316,27 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         std::fill(g.begin(), g.end(), 0.);
         g[0] = beta;
         const int mode = pc.mode;   // fixed for the cycle
-        const bool flex = mode >= 2;
+        // every preconditioned mode keeps M(v_j) (for the sweep alone this is
+        // right preconditioning: x += Z y = P^{-1} V y without a last sweep)
+        const bool flex = mode >= 1;
         T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
         int j = 0;
         for (; j < m && total < max_it; ++j) {
             T* vj = V + (int64_t)j * N;
             T* vn = V + (int64_t)(j + 1) * N;
             if (flex) {
-                T* zj = Z + (int64_t)j * N;       // flexible: w = A M(v_j), M(v_j) kept
+                T* zj = Z + (int64_t)j * N;       // w = A M(v_j), M(v_j) kept
                 apply_sweep<T>(h, vj, zj, s);
                 ++pc.sweeps;
                 if (mode == 2) {
                     apply_coarse<T>(h, vj, zj, s);
                     ++pc.coarse;
                     ++*applies;
-                } else {
+                } else if (mode == 3) {
                     apply_learned<T>(h, zj, s);
                     ++pc.learned;
                 }
                 launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zj, wbuf, s);
-            } else if (mode == 1) {
-                apply_sweep<T>(h, vj, zbuf, s);   // right preconditioning: w = A P^{-1} v_j
-                ++pc.sweeps;
-                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zbuf, wbuf, s);
             } else {
                 launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
             }
@@ -395,13 +393,6 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         if (flex) {
             // x += Z y
             combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N), count_launch();
-        } else if (mode == 1) {
-            // x += P^{-1} (V y)
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(0., tbuf, 0., tbuf, N), count_launch();
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(tbuf, V, N, j, ws->hdev, 1., N), count_launch();
-            apply_sweep<T>(h, tbuf, zbuf, s);
-            ++pc.sweeps;
-            axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., zbuf, 1., xT, N), count_launch();
         } else {
             combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N), count_launch();
         }
@@ -474,7 +465,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
         int used = 0;
         while (res > tol && used < o->max_it) {
             GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
-                                           o->max_it - used, &hv, &applies64, pc, ws->z64, ws->t64, s);
+                                           o->max_it - used, &hv, &applies64, pc, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(1., ws->w64, 1., ws->x, N), count_launch();
             const double prev = res;
@@ -499,7 +490,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
             const int inner_cap = std::min(o->max_it - used, 20 * m);
             GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, ws->s32, ws->V32, m,
                                           std::max(inner_rtol, tol / res), inner_cap,
-                                          nullptr, &applies32, pc, ws->z32, ws->t32, s);
+                                          nullptr, &applies32, pc, s);
             used += std::max(gr.iters, 1);
             axpby_kernel<float, double><<<grid_for(N), 256, 0, s>>>(res, ws->d32, 1., ws->x, N), count_launch();
             const double prev = res;
