@@ -94,6 +94,71 @@ __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, co
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// Fused Gram-Schmidt pass: w -= sum_{q<k} h[q] V_q, then out[q] = <V_q, w>
+// for q < k (kNorm false) or out[0] = <w, w> (kNorm true), with one read of V
+// and w.  Reductions as in multi_dot_kernel (last block, fixed order).
+constexpr int kFuseMax = 32;   // vectors of the fused pass (longer bases use the separate kernels)
+
+template <typename T, bool kNorm>
+__global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
+                                const double* __restrict__ h, int64_t n, double* __restrict__ partial,
+                                unsigned int* __restrict__ ticket, double* __restrict__ out,
+                                const double* __restrict__ add, double* __restrict__ out_sum) {
+    constexpr int K = kNorm ? 1 : kFuseMax;
+    __shared__ Acc<T> hs[kFuseMax];
+    __shared__ double red[K][kRedThreads / 32];
+    __shared__ int s_last;
+    if ((int)threadIdx.x < k) hs[threadIdx.x] = (Acc<T>)h[threadIdx.x];
+    __syncthreads();
+    const int nout = kNorm ? 1 : k;
+    Acc<T> acc[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) acc[q] = Acc<T>(0);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        Acc<T> sv = w[i];
+        for (int q = 0; q < k; ++q) sv = fma(-hs[q], (Acc<T>)V[(int64_t)q * ldv + i], sv);
+        w[i] = (T)sv;
+        if (kNorm) {
+            acc[0] = fma(sv, sv, acc[0]);
+        } else {
+            // the second read of V_q[i] hits the cache line the first one loaded
+#pragma unroll
+            for (int q = 0; q < K; ++q)
+                if (q < k) acc[q] = fma((Acc<T>)V[(int64_t)q * ldv + i], sv, acc[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        if (q >= nout) break;
+        Acc<T> sw = acc[q];
+        for (int o = 16; o > 0; o >>= 1) sw += __shfl_down_sync(0xffffffffu, sw, o);
+        if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = (double)sw;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nout) {
+        double sb = 0.;
+        for (int wq = 0; wq < kRedThreads / 32; ++wq) sb += red[threadIdx.x][wq];
+        partial[(int64_t)blockIdx.x * nout + threadIdx.x] = sb;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < nout; q += blockDim.x >> 5) {
+        double sq = 0.;
+        for (int b = lane; b < (int)gridDim.x; b += 32) sq += __ldcg(partial + (int64_t)b * nout + q);
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
+        if (lane == 0) {
+            out[q] = sq;
+            if (add) out_sum[q] = sq + add[q];
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
 // w -= sum_q h[q] V_q
 template <typename T>
 __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
@@ -347,10 +412,18 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             double* nr = ws->hdev + 3 * (m + 2);
             // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
             dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s);
-            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
-            dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
-            multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
-            dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
+            if (j + 1 <= kFuseMax) {
+                // w -= V h1 fused with h2 = V^T w; then w -= V h2 fused with ||w||^2
+                axpy_dot_kernel<T, false><<<kRedBlocks, kRedThreads, 0, s>>>(
+                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho), count_launch();
+                axpy_dot_kernel<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(
+                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr), count_launch();
+            } else {
+                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
+                dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
+                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
+                dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
+            }
             normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N), count_launch();
             RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
                                      cudaMemcpyDeviceToHost, s));
