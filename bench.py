@@ -592,8 +592,6 @@ def run_batched(args):
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                     "note": "inputs resident; the batched entry point takes device vectors"},
             "gpu_launches": int(n_launch),
-            "gpu_launches_note": "launch statements run by librtg; replays of the captured restart-cycle graph "
-                                 "are not counted",
             "clocks": clk.summary()}
 
 

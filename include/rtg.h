@@ -165,8 +165,8 @@ typedef struct rtg_solve_info {
 int         rtg_abi_version(void);
 const char* rtg_last_error(void);
 /* Kernels the library has launched since it was loaded (host-side count of
- * launch statements, all handles and streams; captured graphs count when
- * recorded, not when replayed). */
+ * launch statements, all handles and streams; a replay of a captured graph
+ * counts the kernels it holds). */
 int64_t rtg_launch_count(void);
 /* kind 0: Legendre-Gauss-Lobatto (x, y), 1: Legendre-Gauss (th); ascending on
  * [-1, 1]; n in [1, 16]. */

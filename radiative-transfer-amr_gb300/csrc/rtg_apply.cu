@@ -127,6 +127,7 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
                  const int4* __restrict__ items,
                  int stage_w, const TX* __restrict__ x, TX* __restrict__ y) {
     extern __shared__ unsigned char smraw[];
+    if (v.stop && *v.stop) return;
     const int4 it = items[blockIdx.x];
     const int ci = it.x;
     if (v.skip && v.skip[ci]) return;
@@ -370,6 +371,7 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileIte
     __shared__ int4 s_el[kMaxItemCells];      // per item cell: first entry, end entry, local row, nth
     __shared__ int s_po[kMaxItemCells + 1];   // prefix of boundary nodes x nth
     T* smt = reinterpret_cast<T*>(smt4);
+    if (v.stop && *v.stop) return;
     const TileItem it = items[blockIdx.x];
     const int ci = it.col;
     if (v.skip && v.skip[ci]) return;
@@ -645,6 +647,7 @@ template <typename T, typename TX, bool kParity>
 __global__ void __launch_bounds__(kApplyThreads)
 apply_global_kernel(OpView<T> v, const float* __restrict__ mortf, uint32_t flags, const int32_t* __restrict__ cols,
                     const TX* __restrict__ x, TX* __restrict__ y) {
+    if (v.stop && *v.stop) return;
     const int ci = cols[blockIdx.x];
     if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];

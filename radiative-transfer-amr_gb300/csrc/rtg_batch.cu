@@ -253,6 +253,7 @@ struct BatchWs {
     int32_t *kvalid = nullptr, *done = nullptr;
     int32_t *col_inst = nullptr, *col_skip = nullptr;   // per column: instance, skip flag
     cudaGraphExec_t cycle = nullptr;
+    long long cycle_kernels = 0;   // kernels one replay of the cycle runs
     std::vector<void*> allocs;
 };
 
@@ -465,15 +466,20 @@ int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* 
             cudaStream_t cap;
             RTG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
             cudaGraph_t graph;
+            const long long n0 = launch_counter().load();
             RTG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
             record_cycle(h, w, cap);
             RTG_CUDA(cudaStreamEndCapture(cap, &graph));
+            // recorded launches are counted when the graph runs
+            w->cycle_kernels = launch_counter().load() - n0;
+            launch_counter().fetch_sub(w->cycle_kernels);
             RTG_CUDA(cudaGraphInstantiate(&w->cycle, graph, 0));
             RTG_CUDA(cudaGraphDestroy(graph));
             RTG_CUDA(cudaStreamDestroy(cap));
         }
         for (int cyc = 0; cyc < max_cycles; ++cyc) {
             RTG_CUDA(cudaGraphLaunch(w->cycle, s));
+            launch_counter().fetch_add(w->cycle_kernels);
             fp32_applies += m + 1;
             sweeps += m + 1;
             RTG_CUDA(cudaMemcpyAsync(done.data(), w->done, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost, s));

@@ -123,6 +123,7 @@ struct OpView {
     int32_t ncols;
     int32_t nelem;
     const int32_t* skip = nullptr;   // per column: nonzero = leave the column out (batched solve)
+    const int* stop = nullptr;       // nonzero: the launch does nothing (a finished Krylov iteration)
 };
 
 struct HostTables {
@@ -203,7 +204,7 @@ template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace,
-                 const int32_t* skip = nullptr);
+                 const int32_t* skip = nullptr, const int* stop = nullptr);
 void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
 void sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);
@@ -224,7 +225,7 @@ template <typename T>
 void nn_moments(rtg_handle* h, const T* z, float* mom, float* scale, cudaStream_t s);
 void nn_forward(const float* params, const float* feat, int64_t rows, float* coef, cudaStream_t s);
 template <typename T>
-void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s);
+void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s, const int* stop = nullptr);
 template <typename T>
 void nn_stats(rtg_handle* h, const T* z, const T* err, const float* scale, float weight, float* S, cudaStream_t s);
 int64_t nn_work_floats();
@@ -233,7 +234,7 @@ void nn_loss_grad(const float* params, const float* feat, const float* mom, cons
 void nn_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float b1, float b2,
              float eps, float wd, cudaStream_t s);
 template <typename T>
-void apply_learned(rtg_handle* h, T* z, cudaStream_t s);
+void apply_learned(rtg_handle* h, T* z, cudaStream_t s, const int* stop = nullptr);
 
 // Two-level preconditioner (rtg_coarse.cu): column diffusion correction
 void build_coarse(rtg_handle* h, cudaStream_t s);

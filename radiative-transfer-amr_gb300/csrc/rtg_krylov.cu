@@ -18,6 +18,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <map>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -45,9 +47,10 @@ template <typename T>
 __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, const T* __restrict__ w,
                                  int64_t n, double* __restrict__ partial, unsigned int* __restrict__ ticket,
                                  double* __restrict__ out, const double* __restrict__ add,
-                                 double* __restrict__ out_sum) {
+                                 double* __restrict__ out_sum, const int* __restrict__ stop) {
     __shared__ double red[kDotGroup][kRedThreads / 32];
     __shared__ int s_last;
+    if (stop && *stop) return;   // every block: the ticket stays untouched
     for (int g0 = 0; g0 < k; g0 += kDotGroup) {
         const int gk = min(kDotGroup, k - g0);
         Acc<T> acc[kDotGroup];
@@ -103,8 +106,10 @@ template <typename T, bool kNorm>
 __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
                                 const double* __restrict__ h, int64_t n, double* __restrict__ partial,
                                 unsigned int* __restrict__ ticket, double* __restrict__ out,
-                                const double* __restrict__ add, double* __restrict__ out_sum) {
+                                const double* __restrict__ add, double* __restrict__ out_sum,
+                                const int* __restrict__ stop) {
     constexpr int K = kNorm ? 1 : kFuseMax;
+    if (stop && *stop) return;
     __shared__ Acc<T> hs[kFuseMax];
     __shared__ double red[K][kRedThreads / 32];
     __shared__ int s_last;
@@ -177,13 +182,73 @@ __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, in
 // out = w / sqrt(nrm2sq[0]); hcol[k] = sqrt(nrm2sq[0])
 template <typename T>
 __global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, const double* nrm2sq,
-                                 double* hcol, int k, int64_t n) {
-    const double nr = sqrt(nrm2sq[0]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) hcol[k] = nr;
-    const Acc<T> inv = (Acc<T>)(nr > 0. ? 1. / nr : 0.);
+                                 double* hcol, int k, int64_t n, const int* __restrict__ stop) {
+    if (stop && *stop) return;
+    // one FP64 square root and division per block (GB300's FP64 rate is low)
+    __shared__ Acc<T> s_inv;
+    if (threadIdx.x == 0) {
+        const double nr = sqrt(nrm2sq[0]);
+        if (blockIdx.x == 0) hcol[k] = nr;
+        s_inv = (Acc<T>)(nr > 0. ? 1. / nr : 0.);
+    }
+    __syncthreads();
+    const Acc<T> inv = s_inv;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (T)(Acc<T>(w[i]) * inv);
+}
+
+// Arnoldi step j on the device (one thread): take the new Hessenberg column
+// hcol[0..j+1], apply the previous Givens rotations, form rotation j, update
+// g and the residual estimate |g[j+1]|; slot[2j] = estimate, slot[2j+1] = stop
+// code (0 go on, 1 converged or breakdown, 2 last allowed step, 3 non-finite),
+// and a nonzero code raises *stop so that the step after it does nothing.
+__global__ void arnoldi_kernel(const double* __restrict__ hcol, int j, int ldh, double* __restrict__ H,
+                               double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g,
+                               double* __restrict__ slot, int* __restrict__ stop,
+                               const double* __restrict__ cyc) {
+    const double tol = cyc[0];
+    const bool last = j + 1 == (int)cyc[1];
+    if (*stop) {
+        slot[2 * j] = 0.;
+        slot[2 * j + 1] = -1.;   // not run
+        return;
+    }
+    double* hc = H + (int64_t)j * ldh;
+    for (int q = 0; q <= j + 1; ++q) hc[q] = hcol[q];
+    for (int q = 0; q < j; ++q) {
+        const double a = hc[q], b = hc[q + 1];
+        hc[q] = cs[q] * a + sn[q] * b;
+        hc[q + 1] = -sn[q] * a + cs[q] * b;
+    }
+    const double a = hc[j], b = hc[j + 1];
+    const double rr = hypot(a, b);
+    cs[j] = rr > 0. ? a / rr : 1.;
+    sn[j] = rr > 0. ? b / rr : 0.;
+    hc[j] = rr;
+    hc[j + 1] = 0.;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    const double est = fabs(g[j + 1]);
+    int code = 0;
+    if (!isfinite(est)) code = 3;
+    else if (est <= tol || rr == 0.) code = 1;
+    else if (last) code = 2;
+    slot[2 * j] = est;
+    slot[2 * j + 1] = (double)code;
+    if (code) *stop = code;
+}
+
+// Start of a restart cycle on the device: g = (beta, 0, ...), stop cleared,
+// cyc = (tolerance, steps allowed this cycle) for arnoldi_kernel.
+__global__ void cycle_init_kernel(double* __restrict__ g, int n, double beta, int* __restrict__ stop,
+                                  double* __restrict__ cyc, double tol, int steps) {
+    for (int q = threadIdx.x; q < n; q += blockDim.x) g[q] = q == 0 ? beta : 0.;
+    if (threadIdx.x == 0) {
+        *stop = 0;
+        cyc[0] = tol;
+        cyc[1] = (double)steps;
+    }
 }
 
 // y = a*x + b*y over full vectors of possibly different types (FP32 when both
@@ -237,6 +302,17 @@ struct Workspace {
     float* Z32 = nullptr;
     double* partial = nullptr;  // kRedBlocks x (m+1)
     unsigned int* ticket = nullptr;   // last-block ticket of multi_dot_kernel (0 between launches)
+    // device Arnoldi state of the lagged-check inner loop
+    int* stop = nullptr;
+    double *dH = nullptr, *dcs = nullptr, *dsn = nullptr, *dg = nullptr, *dslot = nullptr;
+    double* hslot = nullptr;          // pinned: per step estimate and code
+    double* hHg = nullptr;            // pinned: H and g read back at the end of a cycle
+    std::vector<cudaEvent_t> ev;      // one per step
+    double* cyc = nullptr;            // device: tolerance and steps of the current cycle
+    // graphs of one inner step, by (value size, preconditioner mode, step, restart length)
+    std::map<std::tuple<int, int, int, int>, std::pair<cudaGraphExec_t, long long>> graphs;   // exec, kernels
+    cudaStream_t cap = nullptr;       // capture stream
+    bool warm[2] = {false, false};    // a cycle ran uncaptured (plans and launch shapes exist), per precision
     double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
     std::vector<void*> allocs;
@@ -279,6 +355,18 @@ Workspace* get_ws(rtg_handle* h, int m) {
     ws->partial = dalloc<double>(ws, (int64_t)kRedBlocks * (m + 2));
     ws->ticket = dalloc<unsigned int>(ws, 1);
     RTG_CUDA(cudaMemset(ws->ticket, 0, sizeof(unsigned int)));
+    ws->stop = dalloc<int>(ws, 1);
+    RTG_CUDA(cudaMemset(ws->stop, 0, sizeof(int)));
+    ws->dH = dalloc<double>(ws, (int64_t)(m + 1) * m);
+    ws->dcs = dalloc<double>(ws, m);
+    ws->dsn = dalloc<double>(ws, m);
+    ws->dg = dalloc<double>(ws, m + 1);
+    ws->dslot = dalloc<double>(ws, 2 * m);
+    ws->cyc = dalloc<double>(ws, 2);
+    RTG_CUDA(cudaMallocHost(&ws->hslot, sizeof(double) * 2 * m));
+    RTG_CUDA(cudaMallocHost(&ws->hHg, sizeof(double) * ((size_t)(m + 1) * m + m + 1)));
+    ws->ev.assign(m, nullptr);
+    for (auto& e : ws->ev) RTG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     ws->hdev = dalloc<double>(ws, 4 * (m + 2));
     RTG_CUDA(cudaMallocHost(&ws->hhost, sizeof(double) * 4 * (m + 2)));
     return ws;
@@ -286,9 +374,9 @@ Workspace* get_ws(rtg_handle* h, int m) {
 
 template <typename T>
 void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, double* out,
-          const double* add, double* out_sum, cudaStream_t s) {
+          const double* add, double* out_sum, cudaStream_t s, const int* stop = nullptr) {
     multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
-                                                          out_sum), count_launch();
+                                                          out_sum, stop), count_launch();
 }
 
 template <typename T>
@@ -343,6 +431,13 @@ float* flex_basis<float>(Workspace* ws, int m) {
 // GMRES(m) for A_II d = r0 in precision T starting from d = 0.  rhs is given
 // in T (scaled); stops when the estimated residual <= tol_abs or after
 // max_it iterations.  Returns the solution in xT (T).  hist gets estimates.
+//
+// Inner loop: the Givens rotations and the convergence test run on the
+// device (arnoldi_kernel), and the host reads step j's outcome only after it
+// has queued step j+1, so the GPU never waits for the host between steps.
+// A step that follows the last one finds *stop raised and every launch of it
+// returns at once.  The two-level preconditioner (mode 2) and restart lengths
+// above the fused Gram-Schmidt limit keep a host check per step.
 template <typename T>
 GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T* V, int m,
                   double tol_abs, int max_it, std::vector<double>* hist, int* applies,
@@ -355,6 +450,10 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
     // r = rhs - A x = rhs (x = 0)
     int total = 0;
     bool first = true;
+    double* h1 = ws->hdev;
+    double* h2 = ws->hdev + (m + 2);
+    double* ho = ws->hdev + 2 * (m + 2);
+    double* nr = ws->hdev + 3 * (m + 2);
     while (total < max_it) {
         // r = rhs - A x  into V_0 (unnormalised), beta = ||r||
         if (first) {
@@ -365,11 +464,9 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             axpby_kernel<T, T><<<grid_for(N), 256, 0, s>>>(1., rhs, -1., wbuf, N), count_launch();
         }
         first = false;
-        dots<T>(ws, wbuf, 0, 1, wbuf, N, ws->hdev + 3 * (m + 2), nullptr, nullptr, s);
-        normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ws->hdev + 3 * (m + 2),
-                                                         ws->hdev + 2 * (m + 2), 0, N), count_launch();
-        RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev + 2 * (m + 2), sizeof(double),
-                                 cudaMemcpyDeviceToHost, s));
+        dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
+        normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, nr, ho, 0, N, nullptr), count_launch();
+        RTG_CUDA(cudaMemcpyAsync(ws->hhost, ho, sizeof(double), cudaMemcpyDeviceToHost, s));
         RTG_CUDA(cudaStreamSynchronize(s));
         const double beta = ws->hhost[0];
         res.res = beta;
@@ -378,82 +475,162 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             res.converged = true;
             break;
         }
-        std::fill(g.begin(), g.end(), 0.);
-        g[0] = beta;
         const int mode = pc.mode;   // fixed for the cycle
         // every preconditioned mode keeps M(v_j) (for the sweep alone this is
         // right preconditioning: x += Z y = P^{-1} V y without a last sweep)
         const bool flex = mode >= 1;
+        const bool lagged = mode != 2 && m <= kFuseMax;
         T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
-        int j = 0;
-        for (; j < m && total < max_it; ++j) {
+        const int* stop = lagged ? ws->stop : nullptr;
+        OpView<T> vs = v;
+        vs.stop = stop;
+        // counts of one step
+        auto count_step = [&](int times) {
+            if (flex) pc.sweeps += times;
+            if (mode == 2) pc.coarse += times;
+            if (mode == 3) pc.learned += times;
+            *applies += times * (mode == 2 ? 2 : 1);
+        };
+        // one Arnoldi step on stream s: w = A M(v_j), CGS2 against V, v_{j+1} = w / ||w||
+        auto step = [&](int j, cudaStream_t s) {
             T* vj = V + (int64_t)j * N;
             T* vn = V + (int64_t)(j + 1) * N;
             if (flex) {
-                T* zj = Z + (int64_t)j * N;       // w = A M(v_j), M(v_j) kept
-                apply_sweep<T>(h, vj, zj, s);
-                ++pc.sweeps;
+                T* zj = Z + (int64_t)j * N;
+                apply_sweep<T>(h, vj, zj, s, nullptr, nullptr, stop);
                 if (mode == 2) {
                     apply_coarse<T>(h, vj, zj, s);
-                    ++pc.coarse;
-                    ++*applies;
                 } else if (mode == 3) {
-                    apply_learned<T>(h, zj, s);
-                    ++pc.learned;
+                    apply_learned<T>(h, zj, s, stop);
                 }
-                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, zj, wbuf, s);
+                launch_apply<T>(h, vs, RTG_SYSTEM | RTG_MASK_ROWS, zj, wbuf, s);
             } else {
-                launch_apply<T>(h, v, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
+                launch_apply<T>(h, vs, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
             }
-            ++*applies;
-            double* h1 = ws->hdev;
-            double* h2 = ws->hdev + (m + 2);
-            double* ho = ws->hdev + 2 * (m + 2);
-            double* nr = ws->hdev + 3 * (m + 2);
             // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
-            dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s);
+            dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s, stop);
             if (j + 1 <= kFuseMax) {
                 // w -= V h1 fused with h2 = V^T w; then w -= V h2 fused with ||w||^2
                 axpy_dot_kernel<T, false><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho), count_launch();
+                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho, stop), count_launch();
                 axpy_dot_kernel<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr), count_launch();
+                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr, stop), count_launch();
             } else {
                 multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
                 dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
                 multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
                 dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
             }
-            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N), count_launch();
-            RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
+            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N, stop), count_launch();
+        };
+        int j = 0;   // steps of this cycle that count
+        if (lagged) {
+            const int steps = std::min(m, max_it - total);
+            cycle_init_kernel<<<1, 64, 0, s>>>(ws->dg, m + 1, beta, ws->stop, ws->cyc, tol_abs, steps),
+                count_launch();
+            const int pi = sizeof(T) == 8 ? 1 : 0;
+            auto full_step = [&](int q, cudaStream_t st) {
+                step(q, st);
+                arnoldi_kernel<<<1, 1, 0, st>>>(ho, q, m + 1, ws->dH, ws->dcs, ws->dsn, ws->dg, ws->dslot, ws->stop,
+                                               ws->cyc), count_launch();
+            };
+            int issued = 0, code = 0;
+            for (int q = 0; q < steps; ++q) {
+                if (ws->warm[pi]) {
+                    // replay the captured step (captured on first use)
+                    const auto key = std::make_tuple((int)sizeof(T), mode, q, m);
+                    auto it = ws->graphs.find(key);
+                    if (it == ws->graphs.end()) {
+                        if (!ws->cap) RTG_CUDA(cudaStreamCreateWithFlags(&ws->cap, cudaStreamNonBlocking));
+                        cudaGraph_t graph;
+                        const long long n0 = launch_counter().load();
+                        RTG_CUDA(cudaStreamBeginCapture(ws->cap, cudaStreamCaptureModeThreadLocal));
+                        full_step(q, ws->cap);
+                        RTG_CUDA(cudaStreamEndCapture(ws->cap, &graph));
+                        // recorded launches are counted when the graph runs
+                        const long long nk = launch_counter().load() - n0;
+                        launch_counter().fetch_sub(nk);
+                        cudaGraphExec_t exec;
+                        RTG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+                        RTG_CUDA(cudaGraphDestroy(graph));
+                        it = ws->graphs.emplace(key, std::make_pair(exec, nk)).first;
+                    }
+                    RTG_CUDA(cudaGraphLaunch(it->second.first, s));
+                    launch_counter().fetch_add(it->second.second);
+                } else {
+                    full_step(q, s);
+                }
+                count_step(1);
+                RTG_CUDA(cudaMemcpyAsync(ws->hslot + 2 * q, ws->dslot + 2 * q, 2 * sizeof(double),
+                                         cudaMemcpyDeviceToHost, s));
+                RTG_CUDA(cudaEventRecord(ws->ev[q], s));
+                issued = q + 1;
+                if (q >= 1) {
+                    RTG_CUDA(cudaEventSynchronize(ws->ev[q - 1]));
+                    code = (int)ws->hslot[2 * (q - 1) + 1];
+                    if (code > 0) {
+                        j = q;   // steps 0 .. q-1 count; step q ran as a no-op
+                        break;
+                    }
+                }
+            }
+            if (code <= 0) {
+                RTG_CUDA(cudaEventSynchronize(ws->ev[issued - 1]));
+                code = (int)ws->hslot[2 * (issued - 1) + 1];
+                j = issued;
+            }
+            // undo the counts of a step that did nothing
+            count_step(-(issued - j));
+            ws->warm[pi] = true;
+            if (code == 3) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+            for (int q = 0; q < j; ++q)
+                if (hist) hist->push_back(ws->hslot[2 * q]);
+            total += j;
+            res.res = ws->hslot[2 * (j - 1)];
+            res.converged = res.res <= tol_abs;
+            // H (j columns) and g back to the host for the triangular solve
+            RTG_CUDA(cudaMemcpyAsync(ws->hHg, ws->dH, sizeof(double) * (size_t)(m + 1) * j, cudaMemcpyDeviceToHost, s));
+            RTG_CUDA(cudaMemcpyAsync(ws->hHg + (size_t)(m + 1) * m, ws->dg, sizeof(double) * (j + 1),
                                      cudaMemcpyDeviceToHost, s));
             RTG_CUDA(cudaStreamSynchronize(s));
-            ++total;
-            double* hc = &H[(size_t)j * (m + 1)];
-            for (int q = 0; q <= j; ++q) hc[q] = ws->hhost[2 * (m + 2) + q];
-            hc[j + 1] = ws->hhost[2 * (m + 2) + j + 1];
-            // Givens
-            for (int q = 0; q < j; ++q) {
-                const double a = hc[q], b = hc[q + 1];
-                hc[q] = cs[q] * a + sn[q] * b;
-                hc[q + 1] = -sn[q] * a + cs[q] * b;
-            }
-            const double a = hc[j], b = hc[j + 1];
-            const double rr = std::hypot(a, b);
-            cs[j] = rr > 0. ? a / rr : 1.;
-            sn[j] = rr > 0. ? b / rr : 0.;
-            hc[j] = rr;
-            hc[j + 1] = 0.;
-            g[j + 1] = -sn[j] * g[j];
-            g[j] = cs[j] * g[j];
-            const double est = std::fabs(g[j + 1]);
-            if (!std::isfinite(est)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
-            if (hist) hist->push_back(est);
-            res.res = est;
-            if (est <= tol_abs || rr == 0.) {
-                ++j;
-                res.converged = est <= tol_abs;
-                break;
+            std::copy(ws->hHg, ws->hHg + (size_t)(m + 1) * j, H.begin());
+            std::copy(ws->hHg + (size_t)(m + 1) * m, ws->hHg + (size_t)(m + 1) * m + j + 1, g.begin());
+        } else {
+            std::fill(g.begin(), g.end(), 0.);
+            g[0] = beta;
+            for (; j < m && total < max_it; ++j) {
+                step(j, s);
+                count_step(1);
+                RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
+                                         cudaMemcpyDeviceToHost, s));
+                RTG_CUDA(cudaStreamSynchronize(s));
+                ++total;
+                double* hc = &H[(size_t)j * (m + 1)];
+                for (int q = 0; q <= j; ++q) hc[q] = ws->hhost[2 * (m + 2) + q];
+                hc[j + 1] = ws->hhost[2 * (m + 2) + j + 1];
+                // Givens
+                for (int q = 0; q < j; ++q) {
+                    const double a = hc[q], b = hc[q + 1];
+                    hc[q] = cs[q] * a + sn[q] * b;
+                    hc[q + 1] = -sn[q] * a + cs[q] * b;
+                }
+                const double a = hc[j], b = hc[j + 1];
+                const double rr = std::hypot(a, b);
+                cs[j] = rr > 0. ? a / rr : 1.;
+                sn[j] = rr > 0. ? b / rr : 0.;
+                hc[j] = rr;
+                hc[j + 1] = 0.;
+                g[j + 1] = -sn[j] * g[j];
+                g[j] = cs[j] * g[j];
+                const double est = std::fabs(g[j + 1]);
+                if (!std::isfinite(est)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+                if (hist) hist->push_back(est);
+                res.res = est;
+                if (est <= tol_abs || rr == 0.) {
+                    ++j;
+                    res.converged = est <= tol_abs;
+                    break;
+                }
             }
         }
         // y = H^{-1} g (upper triangular j x j)
@@ -486,6 +663,12 @@ void free_workspace(rtg_handle* h) {
     if (!h->ws) return;
     for (void* p : h->ws->allocs) cudaFree(p);
     if (h->ws->hhost) cudaFreeHost(h->ws->hhost);
+    if (h->ws->hslot) cudaFreeHost(h->ws->hslot);
+    if (h->ws->hHg) cudaFreeHost(h->ws->hHg);
+    for (cudaEvent_t e : h->ws->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& kv : h->ws->graphs) cudaGraphExecDestroy(kv.second.first);
+    if (h->ws->cap) cudaStreamDestroy(h->ws->cap);
     delete h->ws;
     h->ws = nullptr;
 }

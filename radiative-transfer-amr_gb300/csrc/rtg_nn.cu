@@ -501,6 +501,7 @@ template <typename T>
 __global__ void nn_colstats_kernel(OpView<T> v, const T* __restrict__ z, float* __restrict__ phi,
                                    float* __restrict__ em, float* __restrict__ cm, double* __restrict__ colsq) {
     extern __shared__ float sm[];
+    if (v.stop && *v.stop) return;
     const ColDev C = v.cols[blockIdx.x];
     const int nij = C.nx * C.ny, ncell = C.elem_end - C.elem_begin;
     float* s0w = sm;                           // [ncell][nij]
@@ -628,6 +629,7 @@ __global__ void nn_correct_kernel(OpView<T> v, const float* __restrict__ coef, c
                                   const float* __restrict__ em, const float* __restrict__ cm,
                                   const int32_t* __restrict__ nbr8, const int64_t* __restrict__ row_off,
                                   T* __restrict__ z) {
+    if (v.stop && *v.stop) return;
     const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     for (int e = blockIdx.x * wpb + (threadIdx.x >> 5); e < v.nelem; e += gridDim.x * wpb) {
         const ElemDev E = v.elems[e];
@@ -830,8 +832,9 @@ void nn_set_params(rtg_handle* h, const float* params, cudaStream_t s) {
 bool nn_has_params(rtg_handle* h) { return h->nn && h->nn->has_params; }
 
 template <typename T>
-static void colstats(rtg_handle* h, NNWs* w, const T* z, bool with_sq, cudaStream_t s) {
-    const OpView<T>& v = nview<T>(h);
+static void colstats(rtg_handle* h, NNWs* w, const T* z, bool with_sq, cudaStream_t s, const int* stop = nullptr) {
+    OpView<T> v = nview<T>(h);
+    v.stop = stop;
     int max_nij = 1;
     for (const ColDev& C : h->host.cols) max_nij = std::max(max_nij, C.nx * C.ny);
     const size_t cells = (size_t)std::max(1, h->host.max_cells_col);
@@ -853,10 +856,11 @@ void nn_moments(rtg_handle* h, const T* z, float* mom, float* scale, cudaStream_
 }
 
 template <typename T>
-void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s) {
+void nn_correct(rtg_handle* h, const float* coef, T* z, cudaStream_t s, const int* stop) {
     NNWs* w = get_nn(h);
-    const OpView<T>& v = nview<T>(h);
-    colstats<T>(h, w, z, false, s);
+    OpView<T> v = nview<T>(h);
+    v.stop = stop;
+    colstats<T>(h, w, z, false, s, stop);
     nn_correct_kernel<T><<<elem_grid(v.nelem), 256, 0, s>>>(v, coef, w->phi, w->em, w->cm, w->nbr8, w->row_off, z), count_launch();
     RTG_CUDA(cudaGetLastError());
 }
@@ -892,19 +896,19 @@ void nn_adam(float* params, const float* grad, float* m, float* v, int step, flo
 
 // z += L z with the handle's coefficients (z is the sweep output)
 template <typename T>
-void apply_learned(rtg_handle* h, T* z, cudaStream_t s) {
+void apply_learned(rtg_handle* h, T* z, cudaStream_t s, const int* stop) {
     NNWs* w = get_nn(h);
     if (!w->has_params) throw RtgError{RTG_ERR_ARG, "no network set on the handle"};
-    nn_correct<T>(h, w->coef, z, s);
+    nn_correct<T>(h, w->coef, z, s, stop);
 }
 
 template void nn_moments<double>(rtg_handle*, const double*, float*, float*, cudaStream_t);
 template void nn_moments<float>(rtg_handle*, const float*, float*, float*, cudaStream_t);
-template void nn_correct<double>(rtg_handle*, const float*, double*, cudaStream_t);
-template void nn_correct<float>(rtg_handle*, const float*, float*, cudaStream_t);
+template void nn_correct<double>(rtg_handle*, const float*, double*, cudaStream_t, const int*);
+template void nn_correct<float>(rtg_handle*, const float*, float*, cudaStream_t, const int*);
 template void nn_stats<double>(rtg_handle*, const double*, const double*, const float*, float, float*, cudaStream_t);
 template void nn_stats<float>(rtg_handle*, const float*, const float*, const float*, float, float*, cudaStream_t);
-template void apply_learned<double>(rtg_handle*, double*, cudaStream_t);
-template void apply_learned<float>(rtg_handle*, float*, cudaStream_t);
+template void apply_learned<double>(rtg_handle*, double*, cudaStream_t, const int*);
+template void apply_learned<float>(rtg_handle*, float*, cudaStream_t, const int*);
 
 }  // namespace rtg

@@ -261,11 +261,14 @@ __device__ __forceinline__ bool load_published(const T* p, T& out, int* status) 
     }
 }
 
-// Writes the sentinel over the values of z the sweep will publish (elements
-// of columns left out keep their values).
+// Starts a sweep: resets the claim counter and writes the sentinel over the
+// values of z the sweep will publish (elements of columns left out keep their
+// values).  Device-side, so that a captured graph can replay it.
 template <typename T>
-__global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z) {
+__global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z, unsigned int* __restrict__ next) {
     using U = typename Sentinel<T>::U;
+    if (v.stop && *v.stop) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *next = 0u;
     U* q = reinterpret_cast<U*>(z);
     for (int e = blockIdx.x; e < ne; e += gridDim.x) {
         const ElemDev E = v.elems[e];
@@ -383,6 +386,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     __shared__ int s_str[kMaxCplStaged];
     __shared__ long long s_base[kMaxCplStaged];
     __shared__ T s_dc[kMaxCplStaged];
+    if (v.stop && *v.stop) return;
     for (;;) {
         if (threadIdx.x == 0) {
             s_idx = (int)atomicAdd(next, 1u);
@@ -718,9 +722,6 @@ __global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restr
     }
 }
 
-// Starts a sweep: reset the work counter.  Device-side so that a captured
-// graph can replay it.
-__global__ void sweep_begin_kernel(unsigned int* next) { *next = 0u; }
 
 }  // namespace
 
@@ -992,16 +993,17 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
 // the phases after that: waiting for the upwind lines, forming T, forming the
 // couplings, the face columns of B and the stores.
 template <typename T>
-void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip) {
+void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip,
+                 const int* stop) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
     v.skip = skip;
-    sweep_begin_kernel<<<1, 1, 0, st>>>(s->d_next), count_launch();
+    v.stop = stop;
     {
         const int ne = (int)h->host.elems.size();
-        sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z), count_launch();
+        sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z, s->d_next), count_launch();
     }
     size_t& smem = f64 ? s->smem64 : s->smem32;
     int& bcap = f64 ? s->bcap64 : s->bcap32;
@@ -1071,9 +1073,9 @@ int sweep_status(rtg_handle* h, cudaStream_t st) {
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t);
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t, unsigned long long*,
-                                  const int32_t*);
+                                  const int32_t*, const int*);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t, unsigned long long*,
-                                 const int32_t*);
+                                 const int32_t*, const int*);
 
 int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
 int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
