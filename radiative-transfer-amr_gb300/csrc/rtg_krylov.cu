@@ -239,15 +239,31 @@ __global__ void arnoldi_kernel(const double* __restrict__ hcol, int j, int ldh, 
     if (code) *stop = code;
 }
 
-// Start of a restart cycle on the device: g = (beta, 0, ...), stop cleared,
-// cyc = (tolerance, steps allowed this cycle) for arnoldi_kernel.
-__global__ void cycle_init_kernel(double* __restrict__ g, int n, double beta, int* __restrict__ stop,
-                                  double* __restrict__ cyc, double tol, int steps) {
+// Start of a restart cycle on the device: g = (beta, 0, ...) with beta = ||r||
+// from *beta_dev, cyc = (tolerance, steps allowed this cycle, beta, code) for
+// arnoldi_kernel and the host; a residual already within tolerance (code 1)
+// or non-finite (code 3) raises *stop at once, otherwise it is cleared.
+__global__ void cycle_init_kernel(double* __restrict__ g, int n, const double* __restrict__ beta_dev,
+                                  int* __restrict__ stop, double* __restrict__ cyc, double tol, int steps) {
+    const double beta = *beta_dev;
     for (int q = threadIdx.x; q < n; q += blockDim.x) g[q] = q == 0 ? beta : 0.;
     if (threadIdx.x == 0) {
-        *stop = 0;
+        const int code = !isfinite(beta) ? 3 : (beta <= tol ? 1 : 0);
+        *stop = code;
         cyc[0] = tol;
         cyc[1] = (double)steps;
+        cyc[2] = beta;
+        cyc[3] = (double)code;
+    }
+}
+
+// y = H^{-1} g for the j x j upper-triangular Hessenberg factor (one thread)
+__global__ void ysolve_kernel(const double* __restrict__ H, int ldh, const double* __restrict__ g, int j,
+                              double* __restrict__ y) {
+    for (int q = j - 1; q >= 0; --q) {
+        double sacc = g[q];
+        for (int c = q + 1; c < j; ++c) sacc -= H[(int64_t)c * ldh + q] * y[c];
+        y[q] = sacc / H[(int64_t)q * ldh + q];
     }
 }
 
@@ -306,7 +322,6 @@ struct Workspace {
     int* stop = nullptr;
     double *dH = nullptr, *dcs = nullptr, *dsn = nullptr, *dg = nullptr, *dslot = nullptr;
     double* hslot = nullptr;          // pinned: per step estimate and code
-    double* hHg = nullptr;            // pinned: H and g read back at the end of a cycle
     std::vector<cudaEvent_t> ev;      // one per step
     double* cyc = nullptr;            // device: tolerance and steps of the current cycle
     // graphs of one inner step, by (value size, preconditioner mode, step, restart length)
@@ -362,9 +377,8 @@ Workspace* get_ws(rtg_handle* h, int m) {
     ws->dsn = dalloc<double>(ws, m);
     ws->dg = dalloc<double>(ws, m + 1);
     ws->dslot = dalloc<double>(ws, 2 * m);
-    ws->cyc = dalloc<double>(ws, 2);
-    RTG_CUDA(cudaMallocHost(&ws->hslot, sizeof(double) * 2 * m));
-    RTG_CUDA(cudaMallocHost(&ws->hHg, sizeof(double) * ((size_t)(m + 1) * m + m + 1)));
+    ws->cyc = dalloc<double>(ws, 4);
+    RTG_CUDA(cudaMallocHost(&ws->hslot, sizeof(double) * (2 * m + 2)));   // steps, then beta and start code
     ws->ev.assign(m, nullptr);
     for (auto& e : ws->ev) RTG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     ws->hdev = dalloc<double>(ws, 4 * (m + 2));
@@ -466,20 +480,23 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         first = false;
         dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
         normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, nr, ho, 0, N, nullptr), count_launch();
-        RTG_CUDA(cudaMemcpyAsync(ws->hhost, ho, sizeof(double), cudaMemcpyDeviceToHost, s));
-        RTG_CUDA(cudaStreamSynchronize(s));
-        const double beta = ws->hhost[0];
-        res.res = beta;
-        if (!std::isfinite(beta)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
-        if (beta <= tol_abs) {
-            res.converged = true;
-            break;
-        }
         const int mode = pc.mode;   // fixed for the cycle
         // every preconditioned mode keeps M(v_j) (for the sweep alone this is
         // right preconditioning: x += Z y = P^{-1} V y without a last sweep)
         const bool flex = mode >= 1;
         const bool lagged = mode != 2 && m <= kFuseMax;
+        double beta = 0.;
+        if (!lagged) {
+            RTG_CUDA(cudaMemcpyAsync(ws->hhost, ho, sizeof(double), cudaMemcpyDeviceToHost, s));
+            RTG_CUDA(cudaStreamSynchronize(s));
+            beta = ws->hhost[0];
+            res.res = beta;
+            if (!std::isfinite(beta)) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+            if (beta <= tol_abs) {
+                res.converged = true;
+                break;
+            }
+        }
         T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
         const int* stop = lagged ? ws->stop : nullptr;
         OpView<T> vs = v;
@@ -526,8 +543,10 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         int j = 0;   // steps of this cycle that count
         if (lagged) {
             const int steps = std::min(m, max_it - total);
-            cycle_init_kernel<<<1, 64, 0, s>>>(ws->dg, m + 1, beta, ws->stop, ws->cyc, tol_abs, steps),
+            cycle_init_kernel<<<1, 64, 0, s>>>(ws->dg, m + 1, ho, ws->stop, ws->cyc, tol_abs, steps),
                 count_launch();
+            RTG_CUDA(cudaMemcpyAsync(ws->hslot + 2 * m, ws->cyc + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            double* start = ws->hslot + 2 * m;   // beta, start code (read with step 0's outcome)
             const int pi = sizeof(T) == 8 ? 1 : 0;
             auto full_step = [&](int q, cudaStream_t st) {
                 step(q, st);
@@ -545,7 +564,14 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                         cudaGraph_t graph;
                         const long long n0 = launch_counter().load();
                         RTG_CUDA(cudaStreamBeginCapture(ws->cap, cudaStreamCaptureModeThreadLocal));
-                        full_step(q, ws->cap);
+                        try {
+                            full_step(q, ws->cap);
+                        } catch (...) {
+                            cudaGraph_t broken = nullptr;
+                            cudaStreamEndCapture(ws->cap, &broken);
+                            if (broken) cudaGraphDestroy(broken);
+                            throw;
+                        }
                         RTG_CUDA(cudaStreamEndCapture(ws->cap, &graph));
                         // recorded launches are counted when the graph runs
                         const long long nk = launch_counter().load() - n0;
@@ -566,7 +592,8 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 RTG_CUDA(cudaEventRecord(ws->ev[q], s));
                 issued = q + 1;
                 if (q >= 1) {
-                    RTG_CUDA(cudaEventSynchronize(ws->ev[q - 1]));
+                    RTG_CUDA(cudaEventSynchronize(ws->ev[q - 1]));   // start[] is valid from here on
+                    if (start[1] > 0.) break;                        // the cycle had nothing to do
                     code = (int)ws->hslot[2 * (q - 1) + 1];
                     if (code > 0) {
                         j = q;   // steps 0 .. q-1 count; step q ran as a no-op
@@ -576,8 +603,19 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             }
             if (code <= 0) {
                 RTG_CUDA(cudaEventSynchronize(ws->ev[issued - 1]));
-                code = (int)ws->hslot[2 * (issued - 1) + 1];
-                j = issued;
+                if (!(start[1] > 0.)) {
+                    code = (int)ws->hslot[2 * (issued - 1) + 1];
+                    j = issued;
+                }
+            }
+            beta = start[0];
+            if (start[1] > 0.) {
+                // the residual was already within tolerance (or not finite): no step counts
+                count_step(-issued);
+                res.res = beta;
+                if ((int)start[1] == 3) throw RtgError{RTG_ERR_NONFINITE, "non-finite residual in GMRES"};
+                res.converged = true;
+                break;
             }
             // undo the counts of a step that did nothing
             count_step(-(issued - j));
@@ -588,13 +626,8 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             total += j;
             res.res = ws->hslot[2 * (j - 1)];
             res.converged = res.res <= tol_abs;
-            // H (j columns) and g back to the host for the triangular solve
-            RTG_CUDA(cudaMemcpyAsync(ws->hHg, ws->dH, sizeof(double) * (size_t)(m + 1) * j, cudaMemcpyDeviceToHost, s));
-            RTG_CUDA(cudaMemcpyAsync(ws->hHg + (size_t)(m + 1) * m, ws->dg, sizeof(double) * (j + 1),
-                                     cudaMemcpyDeviceToHost, s));
-            RTG_CUDA(cudaStreamSynchronize(s));
-            std::copy(ws->hHg, ws->hHg + (size_t)(m + 1) * j, H.begin());
-            std::copy(ws->hHg + (size_t)(m + 1) * m, ws->hHg + (size_t)(m + 1) * m + j + 1, g.begin());
+            // y = H^{-1} g on the device (into hdev, where the combine reads it)
+            ysolve_kernel<<<1, 1, 0, s>>>(ws->dH, m + 1, ws->dg, j, ws->hdev), count_launch();
         } else {
             std::fill(g.begin(), g.end(), 0.);
             g[0] = beta;
@@ -633,13 +666,15 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 }
             }
         }
-        // y = H^{-1} g (upper triangular j x j)
-        for (int q = j - 1; q >= 0; --q) {
-            double sacc = g[q];
-            for (int c = q + 1; c < j; ++c) sacc -= H[(size_t)c * (m + 1) + q] * y[c];
-            y[q] = sacc / H[(size_t)q * (m + 1) + q];
+        if (!lagged) {
+            // y = H^{-1} g (upper triangular j x j)
+            for (int q = j - 1; q >= 0; --q) {
+                double sacc = g[q];
+                for (int c = q + 1; c < j; ++c) sacc -= H[(size_t)c * (m + 1) + q] * y[c];
+                y[q] = sacc / H[(size_t)q * (m + 1) + q];
+            }
+            RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         }
-        RTG_CUDA(cudaMemcpyAsync(ws->hdev, y.data(), sizeof(double) * j, cudaMemcpyHostToDevice, s));
         if (flex) {
             // x += Z y
             combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N), count_launch();
@@ -664,7 +699,6 @@ void free_workspace(rtg_handle* h) {
     for (void* p : h->ws->allocs) cudaFree(p);
     if (h->ws->hhost) cudaFreeHost(h->ws->hhost);
     if (h->ws->hslot) cudaFreeHost(h->ws->hslot);
-    if (h->ws->hHg) cudaFreeHost(h->ws->hHg);
     for (cudaEvent_t e : h->ws->ev)
         if (e) cudaEventDestroy(e);
     for (auto& kv : h->ws->graphs) cudaGraphExecDestroy(kv.second.first);
