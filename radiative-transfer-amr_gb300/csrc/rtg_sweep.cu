@@ -350,6 +350,24 @@ __device__ __forceinline__ double map_row(const double* g, const double* zl, int
     return a0 + a1;
 }
 
+// sum_k col[k * cs] * v[k * vs] for k < n with four partial sums and the
+// loads unrolled 16 deep (block-inverse columns read from global memory on the
+// large elements need many loads in flight)
+template <typename T>
+__device__ __forceinline__ T strided_dot(const T* col, int cs, const T* v, int vs, int n) {
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    int k = 0;
+#pragma unroll 4
+    for (; k + 4 <= n; k += 4) {
+        a0 += col[(k + 0) * cs] * v[(k + 0) * vs];
+        a1 += col[(k + 1) * cs] * v[(k + 1) * vs];
+        a2 += col[(k + 2) * cs] * v[(k + 2) * vs];
+        a3 += col[(k + 3) * cs] * v[(k + 3) * vs];
+    }
+    for (; k < n; ++k) a0 += col[k * cs] * v[k * vs];
+    return (a0 + a1) + (a2 + a3);
+}
+
 template <typename T>
 struct UpwindMap {
     const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
@@ -433,11 +451,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             __syncthreads();
             for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
                 const int r = t / nn, ij = t % nn;
-                const T* col = Bg + r * nn * nn + ij;
-                T acc = T(0);
-#pragma unroll 4
-                for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
-                zpre[ij * nth + r] = acc;
+                zpre[ij * nth + r] = strided_dot(Bg + r * nn * nn + ij, nn, rhs + r, nth, nn);
             }
             long long ck0 = 0, ck1 = 0;
             if (trace && threadIdx.x == 0) {
@@ -491,8 +505,8 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             continue;
         }
         const bool staged = bsize <= bcap;
-        if (staged)
-            for (int t = threadIdx.x; t < bsize; t += blockDim.x) Bs[t] = __ldg(B + t);
+        if (staged)   // asynchronous copies: every load in flight at once
+            for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bs + t, B + t);
         const T* Bv = staged ? Bs : B;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
@@ -545,15 +559,12 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             for (int t = threadIdx.x; t < g.m1 * n0; t += blockDim.x) dst[t] = __ldg(v.mort + cp.es + t);
             for (int t = threadIdx.x; t < g.nth1 * nth; t += blockDim.x) dst[g.m1 * n0 + t] = __ldg(v.mort + cp.et + t);
         }
+        cp_async_wait_all();
         __syncthreads();
         // zpre = B rin, block stored as [r][k][ij]
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
-            const T* col = Bv + r * nn * nn + ij;
-            T acc = T(0);
-#pragma unroll 4
-            for (int k = 0; k < nn; ++k) acc += col[k * nn] * rhs[k * nth + r];
-            zpre[ij * nth + r] = acc;
+            zpre[ij * nth + r] = strided_dot(Bv + r * nn * nn + ij, nn, rhs + r, nth, nn);
         }
         // ---- couplings c on the face nodes, into rhs[ij * nth + r]
         long long ck0 = 0, ck1 = 0, ck2 = 0, ck3 = 0;   // phase clocks (thread 0, traced sweeps)
@@ -653,12 +664,17 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
             const T* col = Bv + r * nn * nn + ij;
-            T acc = zpre[ij * nth + r];
-            for (int f = 0; f < nf; ++f) {
-                const int k = s_face[f];
-                acc -= col[k * nn] * rhs[k * nth + r];
+            T a0 = zpre[ij * nth + r], a1 = T(0), a2 = T(0), a3 = T(0);
+            int f = 0;
+#pragma unroll 2
+            for (; f + 4 <= nf; f += 4) {
+                a0 -= col[s_face[f + 0] * nn] * rhs[s_face[f + 0] * nth + r];
+                a1 -= col[s_face[f + 1] * nn] * rhs[s_face[f + 1] * nth + r];
+                a2 -= col[s_face[f + 2] * nn] * rhs[s_face[f + 2] * nth + r];
+                a3 -= col[s_face[f + 3] * nn] * rhs[s_face[f + 3] * nth + r];
             }
-            st_relaxed(z + E.dof_off + (int64_t)ij * nth + r, acc);
+            for (; f < nf; ++f) a0 -= col[s_face[f] * nn] * rhs[s_face[f] * nth + r];
+            st_relaxed(z + E.dof_off + (int64_t)ij * nth + r, (a0 + a1) + (a2 + a3));
         }
         // the stored values are the publication (downstream elements wait on
         // the values themselves); the barrier ends this element's use of the
