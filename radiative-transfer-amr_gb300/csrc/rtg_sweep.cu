@@ -35,7 +35,8 @@ namespace rtg {
 namespace {
 
 constexpr int kSweepThreads = 256;
-constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse
+constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse (2 CTAs per SM)
+constexpr size_t kSweepSmemSmall = 72 * 1024;    // the alternative the first sweep also times (3 CTAs per SM)
 constexpr int kMaxCplStaged = 32;               // active couplings staged per element
 constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
@@ -371,6 +372,8 @@ __device__ __forceinline__ T strided_dot(const T* col, int cs, const T* v, int v
 template <typename T>
 struct UpwindMap {
     const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
+    const int32_t* reg = nullptr;    // per element: values of its staged region (this precision)
+    int reg_cap = 0;                 // ... and the largest region this launch's shared memory holds
     const int32_t* nup = nullptr;    // per element: upwind values
     const int64_t* goff = nullptr;   // per element: first entry of G_e (this precision's copy)
     const int64_t* uoff = nullptr;   // per element: first entry of its upwind index list
@@ -428,7 +431,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         // ---- independent of the sweep: block inverse, residual, mortars
         const T* B = inv + inv_elem_off[e];
         const int bsize = nth * nn * nn;
-        if (um.ok && (um.ok[e] & kOkBit)) {
+        if (um.ok && (um.ok[e] & kOkBit) && um.reg[e] <= um.reg_cap) {
             // ---- one-phase path: zpre = B rin and G_e staged before the wait,
             // then z = zpre + G_e z_upwind once the upwind values arrive
             constexpr int kVec = 16 / sizeof(T);   // values per 16-byte copy
@@ -505,8 +508,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             continue;
         }
         const bool staged = bsize <= bcap;
-        if (staged)   // asynchronous copies: every load in flight at once
+        if (staged) {   // asynchronous copies: every load in flight at once
             for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bs + t, B + t);
+        } else {
+            // too large for shared memory: pull the block into L2 now (one
+            // prefetch per 128-byte line, all in flight) for the products below
+            const char* b0 = reinterpret_cast<const char*>(B);
+            const int64_t nbytes = (int64_t)bsize * sizeof(T);
+            for (int64_t o = (int64_t)threadIdx.x * 128; o < nbytes; o += (int64_t)blockDim.x * 128)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(b0 + o));
+        }
         const T* Bv = staged ? Bs : B;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
@@ -753,8 +764,16 @@ struct Sweep {
     int64_t inv_entries = 0;
     int max_nloc = 0;
     int64_t max_b = 0, max_c = 0;
-    size_t smem64 = 0, smem32 = 0;
-    int bcap64 = 0, bcap32 = 0, grid64 = 0, grid32 = 0;
+    // launch shapes per precision (0 FP32, 1 FP64): two shared-memory budgets,
+    // the faster one chosen by timing the first sweep of the handle
+    struct Shape {
+        size_t smem = 0;
+        int bcap = 0, grid = 0, reg_cap = 0;
+    };
+    Shape shape[2][2];
+    int pick[2] = {-1, -1};
+    float shape_ms[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    int32_t *d_greg32 = nullptr, *d_greg64 = nullptr;
     int n_lagged = 0;
     std::vector<void*> allocs;
     unsigned int* d_next = nullptr;      // work counter
@@ -932,7 +951,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     {
         const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
         std::vector<uint8_t> gok(ne, 0);
-        std::vector<int32_t> gnup(ne, 0), gel;
+        std::vector<int32_t> gnup(ne, 0), gel, greg32(ne, 0), greg64(ne, 0);
         std::vector<int64_t> goff64(ne, 0), goff32(ne, 0), uoff(ne, 0), up;
         int64_t gtot64 = 0, gtot32 = 0;
         for (int e = 0; e < ne; ++e) {
@@ -953,6 +972,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             if (!ok) continue;
             gok[e] = ok;
             gnup[e] = (int32_t)nup;
+            greg32[e] = (int32_t)region32;
+            greg64[e] = (int32_t)region64;
             goff64[e] = gtot64;
             goff32[e] = gtot32;
             uoff[e] = (int64_t)up.size();
@@ -975,6 +996,10 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         }
         s->g_entries = gtot64 + gtot32;
         s->d_gok = sw_alloc<uint8_t>(s, ne);
+        s->d_greg32 = sw_alloc<int32_t>(s, ne);
+        s->d_greg64 = sw_alloc<int32_t>(s, ne);
+        RTG_CUDA(cudaMemcpy(s->d_greg32, greg32.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMemcpy(s->d_greg64, greg64.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
         s->d_gnup = sw_alloc<int32_t>(s, ne);
         s->d_goff64 = sw_alloc<int64_t>(s, ne);
         s->d_goff32 = sw_alloc<int64_t>(s, ne);
@@ -1021,35 +1046,72 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         const int ne = (int)h->host.elems.size();
         sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z, s->d_next), count_launch();
     }
-    size_t& smem = f64 ? s->smem64 : s->smem32;
-    int& bcap = f64 ? s->bcap64 : s->bcap32;
-    int& grid = f64 ? s->grid64 : s->grid32;
+    const int pi = f64 ? 1 : 0;
     const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
-    if (grid == 0) {
-        const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
-        const int64_t fit = (int64_t)((kSweepSmemBudget - std::min(rhs_bytes, kSweepSmemBudget)) / sizeof(T));
-        bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
-        // the one-phase elements use the region of Bs and cs for their maps
-        const int64_t gmax = f64 ? s->gmax64 : s->gmax32;
-        smem = sizeof(T) * (size_t)(2 * rhs_cap + std::max<int64_t>((int64_t)bcap + s->max_c, gmax));
-        raise_smem_limit((const void*)sweep_persistent_kernel<T>, smem);
-        int per_sm = 0, dev = 0, nsm = 0;
-        RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
-                                                               smem));
-        RTG_CUDA(cudaGetDevice(&dev));
-        RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
-    }
     UpwindMap<T> um;
     um.ok = s->d_gok;
+    um.reg = f64 ? s->d_greg64 : s->d_greg32;
     um.nup = s->d_gnup;
     um.goff = f64 ? s->d_goff64 : s->d_goff32;
     um.uoff = s->d_uoff;
     um.up = s->d_up;
     um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
-    sweep_persistent_kernel<T><<<grid, kSweepThreads, smem, st>>>(
-        v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next, s->d_status,
-        um, rhs_cap, bcap, (int)s->max_c, trace), count_launch();
+    auto launch = [&](const Sweep::Shape& sh) {
+        um.reg_cap = sh.reg_cap;
+        sweep_persistent_kernel<T><<<sh.grid, kSweepThreads, sh.smem, st>>>(
+            v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next,
+            s->d_status, um, rhs_cap, sh.bcap, (int)s->max_c, trace), count_launch();
+    };
+    if (s->pick[pi] < 0) {
+        // the two launch shapes: larger per-CTA shared memory (more one-phase
+        // elements and staged blocks, 2 CTAs per SM) or smaller (3 CTAs per
+        // SM, for meshes whose levels hold many elements)
+        int dev = 0, nsm = 0;
+        RTG_CUDA(cudaGetDevice(&dev));
+        RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        const size_t budgets[2] = {kSweepSmemBudget, kSweepSmemSmall};
+        for (int q = 0; q < 2; ++q) {
+            Sweep::Shape& sh = s->shape[pi][q];
+            const size_t budget = budgets[q];
+            const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
+            const int64_t fit = (int64_t)((budget - std::min(rhs_bytes, budget)) / sizeof(T));
+            sh.bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
+            sh.reg_cap = (int)std::max<int64_t>(0, (int64_t)(budget / sizeof(T)) - 2 * rhs_cap);
+            const int64_t gmax = std::min<int64_t>(f64 ? s->gmax64 : s->gmax32, sh.reg_cap);
+            sh.smem = sizeof(T) * (size_t)(2 * rhs_cap + std::max<int64_t>((int64_t)sh.bcap + s->max_c, gmax));
+            raise_smem_limit((const void*)sweep_persistent_kernel<T>, sh.smem);
+            int per_sm = 0;
+            RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
+                                                                   sh.smem));
+            sh.grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
+        }
+        // time both (after one warm-up each); the smaller budget must win by 3 %
+        cudaEvent_t e0, e1;
+        RTG_CUDA(cudaEventCreate(&e0));
+        RTG_CUDA(cudaEventCreate(&e1));
+        for (int q = 0; q < 2; ++q) {
+            float best = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                sweep_fill_kernel<T><<<std::max(1, std::min((int)h->host.elems.size(), 152 * 8)), 256, 0, st>>>(
+                    v, (int)h->host.elems.size(), z, s->d_next), count_launch();
+                RTG_CUDA(cudaEventRecord(e0, st));
+                launch(s->shape[pi][q]);
+                RTG_CUDA(cudaEventRecord(e1, st));
+                RTG_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep > 0) best = std::min(best, ms);
+            }
+            s->shape_ms[pi][q] = best;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        s->pick[pi] = s->shape_ms[pi][1] < 0.97f * s->shape_ms[pi][0] ? 1 : 0;
+        // the real sweep below starts from a fresh fill
+        sweep_fill_kernel<T><<<std::max(1, std::min((int)h->host.elems.size(), 152 * 8)), 256, 0, st>>>(
+            v, (int)h->host.elems.size(), z, s->d_next), count_launch();
+    }
+    launch(s->shape[pi][s->pick[pi]]);
     RTG_CUDA(cudaGetLastError());
 }
 
