@@ -97,6 +97,57 @@ __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, co
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// Arnoldi step j (one thread): take the new Hessenberg column (projections
+// hcol[0..j] and ||w||), apply the previous Givens rotations, form rotation j,
+// update g and the residual estimate |g[j+1]|; slot[2j] = estimate,
+// slot[2j+1] = stop code (0 go on, 1 converged or breakdown, 2 last allowed
+// step, 3 non-finite); a nonzero code raises *stop so that the step after it
+// does nothing.
+struct ArnoldiState {
+    const double* hcol;   // projections of the step (h1 + h2)
+    double* H;
+    double* cs;
+    double* sn;
+    double* g;
+    double* slot;
+    int* stop;
+    const double* cyc;
+    int j, ldh;
+};
+
+// hcol[0..j] are the projections, hjj1 = ||w|| the new subdiagonal entry
+__device__ void arnoldi_update(const ArnoldiState a_st, const double* hcol, double hjj1) {
+    const int j = a_st.j, ldh = a_st.ldh;
+    double *H = a_st.H, *cs = a_st.cs, *sn = a_st.sn, *g = a_st.g, *slot = a_st.slot;
+    int* stop = a_st.stop;
+    const double tol = a_st.cyc[0];
+    const bool last = j + 1 == (int)a_st.cyc[1];
+    double* hc = H + (int64_t)j * ldh;
+    for (int q = 0; q <= j; ++q) hc[q] = hcol[q];
+    hc[j + 1] = hjj1;
+    for (int q = 0; q < j; ++q) {
+        const double a = hc[q], b = hc[q + 1];
+        hc[q] = cs[q] * a + sn[q] * b;
+        hc[q + 1] = -sn[q] * a + cs[q] * b;
+    }
+    const double a = hc[j], b = hc[j + 1];
+    const double rr = hypot(a, b);
+    cs[j] = rr > 0. ? a / rr : 1.;
+    sn[j] = rr > 0. ? b / rr : 0.;
+    hc[j] = rr;
+    hc[j + 1] = 0.;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    const double est = fabs(g[j + 1]);
+    int code = 0;
+    if (!isfinite(est)) code = 3;
+    else if (est <= tol || rr == 0.) code = 1;
+    else if (last) code = 2;
+    slot[2 * j] = est;
+    slot[2 * j + 1] = (double)code;
+    if (code) *stop = code;
+}
+
 // Fused Gram-Schmidt pass: w -= sum_{q<k} h[q] V_q, then out[q] = <V_q, w>
 // for q < k (kNorm false) or out[0] = <w, w> (kNorm true), with one read of V
 // and w.  Reductions as in multi_dot_kernel (last block, fixed order).
@@ -107,7 +158,7 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
                                 const double* __restrict__ h, int64_t n, double* __restrict__ partial,
                                 unsigned int* __restrict__ ticket, double* __restrict__ out,
                                 const double* __restrict__ add, double* __restrict__ out_sum,
-                                const int* __restrict__ stop) {
+                                const int* __restrict__ stop, ArnoldiState ast) {
     constexpr int K = kNorm ? 1 : kFuseMax;
     if (stop && *stop) return;
     __shared__ Acc<T> hs[kFuseMax];
@@ -159,6 +210,8 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
         if (lane == 0) {
             out[q] = sq;
             if (add) out_sum[q] = sq + add[q];
+            // the norm pass of a device-driven step ends with the Arnoldi update
+            if (kNorm && ast.H) arnoldi_update(ast, ast.hcol, sqrt(sq));
         }
     }
     if (threadIdx.x == 0) *ticket = 0u;
@@ -198,50 +251,9 @@ __global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, c
         out[i] = (T)(Acc<T>(w[i]) * inv);
 }
 
-// Arnoldi step j on the device (one thread): take the new Hessenberg column
-// hcol[0..j+1], apply the previous Givens rotations, form rotation j, update
-// g and the residual estimate |g[j+1]|; slot[2j] = estimate, slot[2j+1] = stop
-// code (0 go on, 1 converged or breakdown, 2 last allowed step, 3 non-finite),
-// and a nonzero code raises *stop so that the step after it does nothing.
-__global__ void arnoldi_kernel(const double* __restrict__ hcol, int j, int ldh, double* __restrict__ H,
-                               double* __restrict__ cs, double* __restrict__ sn, double* __restrict__ g,
-                               double* __restrict__ slot, int* __restrict__ stop,
-                               const double* __restrict__ cyc) {
-    const double tol = cyc[0];
-    const bool last = j + 1 == (int)cyc[1];
-    if (*stop) {
-        slot[2 * j] = 0.;
-        slot[2 * j + 1] = -1.;   // not run
-        return;
-    }
-    double* hc = H + (int64_t)j * ldh;
-    for (int q = 0; q <= j + 1; ++q) hc[q] = hcol[q];
-    for (int q = 0; q < j; ++q) {
-        const double a = hc[q], b = hc[q + 1];
-        hc[q] = cs[q] * a + sn[q] * b;
-        hc[q + 1] = -sn[q] * a + cs[q] * b;
-    }
-    const double a = hc[j], b = hc[j + 1];
-    const double rr = hypot(a, b);
-    cs[j] = rr > 0. ? a / rr : 1.;
-    sn[j] = rr > 0. ? b / rr : 0.;
-    hc[j] = rr;
-    hc[j + 1] = 0.;
-    g[j + 1] = -sn[j] * g[j];
-    g[j] = cs[j] * g[j];
-    const double est = fabs(g[j + 1]);
-    int code = 0;
-    if (!isfinite(est)) code = 3;
-    else if (est <= tol || rr == 0.) code = 1;
-    else if (last) code = 2;
-    slot[2 * j] = est;
-    slot[2 * j + 1] = (double)code;
-    if (code) *stop = code;
-}
-
 // Start of a restart cycle on the device: g = (beta, 0, ...) with beta = ||r||
 // from *beta_dev, cyc = (tolerance, steps allowed this cycle, beta, code) for
-// arnoldi_kernel and the host; a residual already within tolerance (code 1)
+// the Arnoldi update and the host; a residual already within tolerance (code 1)
 // or non-finite (code 3) raises *stop at once, otherwise it is cleared.
 __global__ void cycle_init_kernel(double* __restrict__ g, int n, const double* __restrict__ beta_dev,
                                   int* __restrict__ stop, double* __restrict__ cyc, double tol, int steps) {
@@ -447,7 +459,7 @@ float* flex_basis<float>(Workspace* ws, int m) {
 // max_it iterations.  Returns the solution in xT (T).  hist gets estimates.
 //
 // Inner loop: the Givens rotations and the convergence test run on the
-// device (arnoldi_kernel), and the host reads step j's outcome only after it
+// device (at the end of the norm pass), and the host reads step j's outcome only after it
 // has queued step j+1, so the GPU never waits for the host between steps.
 // A step that follows the last one finds *stop raised and every launch of it
 // returns at once.  The two-level preconditioner (mode 2) and restart lengths
@@ -509,7 +521,8 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             *applies += times * (mode == 2 ? 2 : 1);
         };
         // one Arnoldi step on stream s: w = A M(v_j), CGS2 against V, v_{j+1} = w / ||w||
-        auto step = [&](int j, cudaStream_t s) {
+        // (with a device Arnoldi state the norm pass ends with the Arnoldi update)
+        auto step = [&](int j, cudaStream_t s, ArnoldiState ast) {
             T* vj = V + (int64_t)j * N;
             T* vn = V + (int64_t)(j + 1) * N;
             if (flex) {
@@ -529,9 +542,11 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             if (j + 1 <= kFuseMax) {
                 // w -= V h1 fused with h2 = V^T w; then w -= V h2 fused with ||w||^2
                 axpy_dot_kernel<T, false><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho, stop), count_launch();
+                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho, stop, ArnoldiState{}),
+                    count_launch();
                 axpy_dot_kernel<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr, stop), count_launch();
+                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr, stop, ast),
+                    count_launch();
             } else {
                 multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
                 dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
@@ -549,9 +564,8 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             double* start = ws->hslot + 2 * m;   // beta, start code (read with step 0's outcome)
             const int pi = sizeof(T) == 8 ? 1 : 0;
             auto full_step = [&](int q, cudaStream_t st) {
-                step(q, st);
-                arnoldi_kernel<<<1, 1, 0, st>>>(ho, q, m + 1, ws->dH, ws->dcs, ws->dsn, ws->dg, ws->dslot, ws->stop,
-                                               ws->cyc), count_launch();
+                ArnoldiState ast{ho, ws->dH, ws->dcs, ws->dsn, ws->dg, ws->dslot, ws->stop, ws->cyc, q, m + 1};
+                step(q, st, ast);
             };
             int issued = 0, code = 0;
             for (int q = 0; q < steps; ++q) {
@@ -632,7 +646,7 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             std::fill(g.begin(), g.end(), 0.);
             g[0] = beta;
             for (; j < m && total < max_it; ++j) {
-                step(j, s);
+                step(j, s, ArnoldiState{});
                 count_step(1);
                 RTG_CUDA(cudaMemcpyAsync(ws->hhost, ws->hdev, sizeof(double) * 3 * (m + 2),
                                          cudaMemcpyDeviceToHost, s));

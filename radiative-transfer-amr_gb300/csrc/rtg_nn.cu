@@ -536,20 +536,21 @@ __global__ void nn_colstats_kernel(OpView<T> v, const T* __restrict__ z, float* 
         phi[C.node_off + ij] = ph;
         phs[ij] = ph;
     }
-    // element means: nodes in order
-    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+    // element means: one warp per cell, lanes over nodes, fixed shuffle tree
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = wid; k < ncell; k += nw) {
         float acc = 0.f;
-        for (int ij = 0; ij < nij; ++ij) {
-            const float wij = (float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f;
-            acc = fmaf(wij, s0w[k * nij + ij], acc);
-        }
-        em[C.elem_begin + k] = acc / swt[k];
+        for (int ij = lane; ij < nij; ij += 32)
+            acc = fmaf((float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f, s0w[k * nij + ij], acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) em[C.elem_begin + k] = acc / swt[k];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (wid == 0) {
         float c = 0.f;
-        for (int ij = 0; ij < nij; ++ij) c = fmaf((float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f, phs[ij], c);
-        cm[blockIdx.x] = c;
+        for (int ij = lane; ij < nij; ij += 32) c = fmaf((float)(wx[ij / C.ny] * wy[ij % C.ny]) * 0.25f, phs[ij], c);
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+        if (lane == 0) cm[blockIdx.x] = c;
     }
     if (colsq && threadIdx.x < 32) {
         double sq = 0.;
