@@ -184,16 +184,22 @@ int  rtg_get_info(const rtg_handle* h, rtg_info* info);
  * must not alias. */
 int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y,
               void* stream);
-/* The FP32 apply is autotuned on its first use: columns are grouped into
- * degree classes (nx, ny, angular nodes of the column rounded up to a power
- * of two) and each class's work items are timed with 16, 32, 64 and 128
- * angular rows per item; the fastest is kept, and the tuned plan is kept
- * only if the whole apply beats the default item size (64 rows).  This
- * returns the table (host, cap_rows rows of 8 int32: nx, ny, nth class,
- * chosen rows (negated when the default plan won), then the time in ns with
- * each candidate, -1 if not run) and the number of classes, tuning first if
- * needed. */
+/* Each precision's apply is autotuned on its first use: every plan shape of
+ * the candidate list (16, 32 or 64 angular rows per work item; one CTA per
+ * column or per work item; one launch, or one launch per shared-memory class
+ * of the CTAs; FP32 also with the scattering product on the tensor cores) is
+ * built and the whole apply timed; the fastest is kept.  This returns the
+ * FP32 table (host, cap_rows rows of 9 int32: rows per item, items per CTA
+ * (0: the whole column), split launches (0/1), tensor-core scattering (0/1),
+ * chosen (0/1), time in ns (-1: not timed), work items, CTAs, launches) and
+ * the number of shapes, tuning first if needed. */
 int rtg_apply_tuning(rtg_handle* h, int32_t* table, int cap_rows, int* nclasses, void* stream);
+/* Fixes the apply plan of one precision to a shape instead of the autotuned
+ * one: shape = {rows per item, items per CTA (0: whole column), split
+ * launches (0/1), tensor-core scattering (0/1, FP32 only)}; NULL returns to
+ * autotuning on the next apply.  Synchronizes the device and drops the
+ * solver's captured graphs (they hold the old plan's launches). */
+int rtg_apply_shape(rtg_handle* h, int prec, const int32_t* shape);
 /* mask[N] (device, uint8): 1 for unknowns, 0 for inflow-boundary DOFs. */
 int rtg_interior_mask(rtg_handle* h, uint8_t* mask, void* stream);
 /* out = x with the entries of one part zeroed: part 0 keeps the unknowns,

@@ -256,17 +256,21 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
 }
 
 // ------------------------------------------------------------ tiled path
-// Work item: whole cells [cell_begin, cell_end) of one column, i.e. the
-// rectangle of angular rows R0 .. R0+M-1 times all nij spatial nodes.  The
-// scattering of the item is the product Y[m][ij] = sum_c W[R0+m][c] X[c][ij]
-// over all Nth angular nodes of the column; it runs from shared memory with
-// 4 x 4 register tiles (16 FMAs per eight loaded values).  The epilogue adds
-// extinction, streaming and face terms and writes y in global order.
-// The inflow face fluxes of the item's elements are factorised per coupling
-// (T[jj][r] = sum_a Et[a][r] x_nbr[jj][a], then sum_jj Es[jj][q] T[jj][r]) and
-// accumulated into Fy before the epilogue; T and Fy reuse the W region.
-// Shared memory: Xs[Nth][nijp] | WsT[Nth][Mp] (later T | Fy[Mp][nijp]) |
-// Ys[Mp][nijp] | cell tables.
+// One CTA per column: the column's input is staged once, transposed
+// (Xs[row][ij]), and the CTA walks the column's items.  An item is whole
+// cells [cell_begin, cell_end), i.e. the rectangle of angular rows
+// R0 .. R0+M-1 times all nij spatial nodes.  The scattering of the item is the
+// product Y[m][ij] = sum_c W[R0+m][c] X[c][ij] over all Nth angular nodes of
+// the column; it runs from shared memory with 4 x 4 register tiles (16 FMAs
+// per eight loaded values).  The epilogue adds extinction, streaming and face
+// terms and writes y in global order.  The inflow face fluxes of the item's
+// elements are factorised per coupling (T[jj][r] = sum_a Et[a][r]
+// x_nbr[jj][a], then sum_jj Es[jj][q] T[jj][r]) and accumulated into Fy
+// before the epilogue; T and Fy reuse the W region.  Every global -> shared
+// copy is a cp.async, so a staging loop has all its loads in flight.
+// Shared memory: Xs[Nth][nijp] | column table | cell rows and flags | item
+// region: WsT[Nth][Mp] (later T | Fy[Mp][nijp]) | Ys[Mp][nijp] |
+// row table[Mp][kRowVals] | row -> cell.
 //
 // FP64 (kParity) keeps the reference's drop rules without per-term tests on
 // the common path:
@@ -287,6 +291,8 @@ struct TileItem {
     int tsz;                  // values of T (padded to 4)
     int wcap;                 // values of the W region
     int ttot, ctot;           // work items of the two flux phases (ctot: boundary nodes x rows)
+    int M;                    // angular rows of the item
+    int cpl0;                 // coupling index of the item's first entry
 };
 
 // One coupling of a tiled item: where its neighbour line is, its mortars,
@@ -302,6 +308,7 @@ struct TileCpl {
     int k, tested;
 };
 constexpr int kMaxItemCpl = 96;
+static_assert(sizeof(TileCpl) == 64, "coupling records are copied in 16-byte pieces");
 constexpr int kMaxItemCells = 128;
 
 // Host-built tables of the FP64 tiled path.
@@ -362,58 +369,89 @@ __device__ __forceinline__ void store4(double* p, const double v[4]) {
     *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
 }
 
+// values of the per-row table: dxdydth/8 * wth_r, dx dth/4, dy dth/4, wth_r,
+// wth_r sin, wth_r cos, ThF_0..3 of the row's cell
+constexpr int kRowVals = 10;
+
+// threads of a tiled CTA: FP32 items are latency bound (more warps per SM),
+// FP64 ones register bound
+template <typename T>
+__host__ __device__ constexpr int tiled_threads() { return sizeof(T) == 8 ? 256 : 512; }
+
+// values of the per-column table: kw and sw per node, LGL weights in x and y,
+// the two derivative tables
+__host__ __device__ __forceinline__ int col_table_size(int nx, int ny) {
+    return (2 * nx * ny + nx + ny + nx * nx + ny * ny + 3) & ~3;
+}
+// ints before the item region: per cell its first row, flags, first coupling
+// and angular table offset, per row its cell; padded to 32 bytes
+__host__ __device__ __forceinline__ int col_int_words(int ncell, int nth_col) {
+    return (4 * ncell + 2 + nth_col + 7) & ~7;
+}
+
 template <typename T, bool kParity>
-__global__ void __launch_bounds__(kApplyThreads)
-apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileItem* __restrict__ items,
-                   const TileCpl* __restrict__ cpl_ent, const T* __restrict__ x, T* __restrict__ y) {
+__global__ void __launch_bounds__(tiled_threads<T>(), sizeof(T) == 8 ? 3 : 2)
+apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* __restrict__ groups,
+                   const TileItem* __restrict__ items, const TileCpl* __restrict__ cpl_ent, const T* __restrict__ x,
+                   T* __restrict__ y) {
     extern __shared__ double2 smt4[];
-    __shared__ TileCpl sc[kMaxItemCpl];
-    __shared__ int4 s_el[kMaxItemCells];      // per item cell: first entry, end entry, local row, nth
-    __shared__ int s_po[kMaxItemCells + 1];   // prefix of boundary nodes x nth
+    __shared__ __align__(16) TileCpl sc[kMaxItemCpl];
+    __shared__ float s_rcp[kMaxNodes + 1];    // 1/n rounded to float
     T* smt = reinterpret_cast<T*>(smt4);
     if (v.stop && *v.stop) return;
-    const TileItem it = items[blockIdx.x];
-    const int ci = it.col;
+    const int4 grp = groups[blockIdx.x];      // column, first item, end item
+    const int ci = grp.x;
     if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
+    // FP32 groups flagged in bit 0 leave the scattering to the tensor-core kernel
+    const bool scat = fl.scat && !(grp.w & 1);
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
-    const int nijp = (nij + 3) & ~3;
-    const int M = [&] {
-        int m = 0;
-        for (int k = it.cell_begin; k < it.cell_end; ++k) m += v.elems[C.elem_begin + k].nth;
-        return m;
-    }();
-    const int Mp = (M + 3) & ~3;
-    T* Xs = smt;                                  // [Nth][nijp]
-    T* WsT = Xs + (size_t)Nth * nijp;             // [Nth][Mp]
-    T* Ys = WsT + (size_t)it.wcap;                // [Mp][nijp]
-    T* Tb = WsT;                                  // after the product: T
-    T* Fy = WsT + it.tsz;                         //                    Fy[Mp][nijp]
-    int* cbeg = reinterpret_cast<int*>(Ys + (size_t)Mp * nijp);   // [ncell+1] local DOF start
-    int* crow = cbeg + ncell + 1;                                  // [ncell] first row
-    if (threadIdx.x == 0) {
-        int off = 0;
-        for (int k = 0; k < ncell; ++k) {
-            const ElemDev E = v.elems[C.elem_begin + k];
-            cbeg[k] = off;
-            crow[k] = E.row;
-            off += nij * E.nth;
+    const int nijp = (nij + 3) & ~3, Nthp = (Nth + 3) & ~3;
+    T* Xs = smt;                                                  // [Nth][nijp]
+    T* colt = Xs + (size_t)Nth * nijp;                            // column table
+    T* rowt = colt + col_table_size(C.nx, C.ny);                  // [Nthp][kRowVals]
+    int* crow = reinterpret_cast<int*>(rowt + (size_t)Nthp * kRowVals);   // [ncell+1] first row; crow[ncell] = Nth
+    int* cflg = crow + ncell + 1;                                          // [ncell] element flags
+    int* ccpl = cflg + ncell;                                              // [ncell+1] first coupling
+    int* cang = ccpl + ncell + 1;                                          // [ncell] angular table offset
+    int* rcell = cang + ncell;                                             // [Nth] cell of each row
+    T* ireg = reinterpret_cast<T*>(crow + col_int_words(ncell, Nth));    // item region
+    const T* kwn = colt;
+    const T* swn = colt + nij;
+    const T* wxs = colt + 2 * nij;
+    const T* wys = wxs + C.nx;
+    const T* Gxs = wys + C.ny;
+    const T* Gys = Gxs + C.nx * C.nx;
+    // per-cell tables and the column table
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+        const ElemDev E = v.elems[C.elem_begin + k];
+        crow[k] = E.row;
+        cflg[k] = E.flags;
+        ccpl[k] = E.cpl_begin;
+        cang[k] = E.ang;
+        if (k == ncell - 1) {
+            crow[ncell] = Nth;
+            ccpl[ncell] = E.cpl_end;
         }
-        cbeg[ncell] = off;
-        int eb = 0, po = 0;
-        for (int k = it.cell_begin; k < it.cell_end; ++k) {
-            const ElemDev E = v.elems[C.elem_begin + k];
-            const int nc = E.cpl_end - E.cpl_begin;
-            s_el[k - it.cell_begin] = make_int4(eb, eb + nc, E.row - it.row0, E.nth);
-            s_po[k - it.cell_begin] = po;
-            eb += nc;
-            po += boundary_nodes(C.nx, C.ny) * E.nth;
-        }
-        s_po[it.cell_end - it.cell_begin] = po;
+        for (int r = 0; r < E.nth; ++r) rcell[E.row + r] = k;
     }
-    const int nent = it.cpl_end - it.cpl_begin;
-    for (int q = threadIdx.x; q < nent; q += blockDim.x) sc[q] = cpl_ent[it.cpl_begin + q];
+    if (threadIdx.x <= kMaxNodes) s_rcp[threadIdx.x] = threadIdx.x ? __frcp_rn((float)threadIdx.x) : 0.f;
+    {
+        const T* Gx = v.G + gofs(C.nx);
+        const T* Gy = v.G + gofs(C.ny);
+        const int o1 = nij, o2 = 2 * nij, o3 = o2 + C.nx, o4 = o3 + C.ny, o5 = o4 + C.nx * C.nx;
+        const int tot = o5 + C.ny * C.ny;
+        for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+            const T* src = q < o1   ? v.kw + C.node_off + q
+                           : q < o2 ? v.sw + C.node_off + (q - o1)
+                           : q < o3 ? v.lglw + C.nx * kMaxNodes + (q - o2)
+                           : q < o4 ? v.lglw + C.ny * kMaxNodes + (q - o3)
+                           : q < o5 ? Gx + (q - o4)
+                                    : Gy + (q - o5);
+            cp_async_small<sizeof(T)>(colt + q, src);
+        }
+    }
     __syncthreads();
     const T* xc = x + C.dof_off;
     // stage x transposed: Xs[row][ij]; pad columns are zero (d grows per
@@ -421,225 +459,481 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const TileIte
     {
         int k = 0;
         for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
-            while (d >= cbeg[k + 1]) ++k;
-            const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
-            const int l = d - cbeg[k];
-            Xs[(crow[k] + l % nth) * nijp + l / nth] = xc[d];
+            while (d >= nij * crow[k + 1]) ++k;
+            const int nth = crow[k + 1] - crow[k];
+            const int l = d - nij * crow[k];
+            const int ij = small_div(l, s_rcp[nth]);
+            cp_async_small<sizeof(T)>(Xs + (crow[k] + l - ij * nth) * nijp + ij, xc + d);
         }
     }
     if (nijp != nij)
         for (int t = threadIdx.x; t < Nth * (nijp - nij); t += blockDim.x)
             Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = T(0);
-    const T* Wg = v.W + v.W_off[C.sig];
-    if (fl.scat) {
-        for (int t = threadIdx.x; t < Nth * Mp; t += blockDim.x) {
-            const int c = t / Mp, m = t % Mp;
-            // FP64: the diagonal joins the extinction term in the epilogue
-            const bool use = m < M && !(kParity && c == it.row0 + m);
-            WsT[t] = use ? __ldg(Wg + (int64_t)(it.row0 + m) * Nth + c) : T(0);
-        }
+    // the column's row table
+    for (int R = threadIdx.x; R < Nth; R += blockDim.x) {
+        const int k = rcell[R];
+        const int e = C.elem_begin + k;
+        const int r = R - crow[k], nth = crow[k + 1] - crow[k];
+        const T* A = v.ang + cang[k];
+        T* rw = rowt + R * kRowVals;
+        const T ar = A[r];
+        rw[0] = v.econst[4 * e] * ar;
+        rw[1] = v.econst[4 * e + 1];
+        rw[2] = v.econst[4 * e + 2];
+        rw[3] = ar;
+        rw[4] = A[nth + r];
+        rw[5] = A[2 * nth + r];
+#pragma unroll
+        for (int F = 0; F < 4; ++F) rw[6 + F] = A[(3 + F) * nth + r];
     }
-    __syncthreads();
-    if (fl.scat) {
-        const int tm = Mp / 4, tn = nijp / 4;
-        // FP64: only nodes of class 1 read the product
-        const uint64_t fullm = kParity ? (nij <= 64 ? par.colfull[ci] : ~0ull) : ~0ull;
-        for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
-            const int m0 = 4 * (tile / tn), j0 = 4 * (tile % tn);
-            if (kParity && j0 < 64 && !((fullm >> j0) & 0xFull)) continue;
-            T acc[4][4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-#pragma unroll 4
-            for (int c = 0; c < Nth; ++c) {
-                T wv[4], xa[4];
-                load4(WsT + c * Mp + m0, wv);
-                load4(Xs + c * nijp + j0, xa);
+    const T* Wg = v.W + v.W_off[C.sig];
+    const T small = T(kSmall);
+    const T dxdy8 = v.colc[ci];
+    const float rny = __frcp_rn((float)C.ny);
+    T* yc = y + C.dof_off;
+    for (int iq = grp.y; iq < grp.z; ++iq) {
+        const TileItem it = items[iq];
+        const int M = it.M, Mp = (M + 3) & ~3;
+        T* WsT = ireg;                                // [Nth][Mp]
+        T* Ys = WsT + (size_t)it.wcap;                // [Mp][nijp]
+        T* Tb = WsT;                                  // after the product: T
+        T* Fy = WsT + it.tsz;                         //                    Fy[Mp][nijp]
+        // the item's couplings (64-byte records, four 16-byte copies each)
+        {
+            const int nent = it.cpl_end - it.cpl_begin;
+            const char* src = reinterpret_cast<const char*>(cpl_ent + it.cpl_begin);
+            char* dst = reinterpret_cast<char*>(sc);
+            for (int q = threadIdx.x; q < nent * (int)(sizeof(TileCpl) / 16); q += blockDim.x)
+                cp_async16(dst + 16 * q, src + 16 * q);
+        }
+        if (scat) {
+            // W^T staged by rows of W^T, so consecutive threads read consecutive values
+            const T* WTg = v.WT + v.W_off[C.sig];
+            const float rMp = __frcp_rn((float)Mp);
+            for (int t = threadIdx.x; t < Nth * Mp; t += blockDim.x) {
+                const int c = small_div(t, rMp), m = t - c * Mp;
+                // FP64: the diagonal joins the extinction term in the epilogue
+                const bool use = m < M && !(kParity && c == it.row0 + m);
+                if (use)
+                    cp_async_small<sizeof(T)>(WsT + t, WTg + (int64_t)c * Nth + it.row0 + m);
+                else
+                    WsT[t] = T(0);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        if (scat) {
+            const int tm = Mp / 4, tn = nijp / 4;
+            const float rtn = __frcp_rn((float)tn);
+            // FP64: only nodes of class 1 read the product
+            const uint64_t fullm = kParity ? (nij <= 64 ? par.colfull[ci] : ~0ull) : ~0ull;
+            for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
+                const int tq = small_div(tile, rtn);
+                const int m0 = 4 * tq, j0 = 4 * (tile - tq * tn);
+                if (kParity && j0 < 64 && !((fullm >> j0) & 0xFull)) continue;
+                T acc[4][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
-            }
+                    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+#pragma unroll 4
+                for (int c = 0; c < Nth; ++c) {
+                    T wv[4], xa[4];
+                    load4(WsT + c * Mp + m0, wv);
+                    load4(Xs + c * nijp + j0, xa);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
-        }
-    }
-    __syncthreads();
-    // inflow face fluxes of the item's elements into Fy (the W region is free)
-    if (fl.bc) {
-        for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = T(0);
-        // T[jj][r] of every coupling, flattened over (coupling, jj, r); t
-        // grows per thread, so the coupling index only moves forward
-        {
-            int c = 0;
-            for (int t = threadIdx.x; t < it.ttot; t += blockDim.x) {
-                while (t >= sc[c].toff + sc[c].m1 * sc[c].nth) ++c;
-                const TileCpl& en = sc[c];
-                if (kParity && en.tested) continue;   // summed term by term below
-                const int q = t - en.toff, jj = q / en.nth, r = q % en.nth;
-                const T* Et = (kParity ? par.mortc : v.mort) + en.et;
-                const T* xl = x + en.base + (int64_t)jj * en.stride;
-                T acc = T(0);
-                for (int a = 0; a < en.nt1; ++a) acc = fma(Et[a * en.nth + r], xl[a], acc);
-                Tb[t] = acc;
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
             }
         }
         __syncthreads();
-        // one thread per (boundary node, row): the element's couplings on the
-        // node's faces in a fixed order, so the sum is deterministic
-        {
-            int k = 0;
-            for (int t = threadIdx.x; t < it.ctot; t += blockDim.x) {
-                while (t >= s_po[k + 1]) ++k;
-                const int4 el = s_el[k];
-                const int f = (t - s_po[k]) / el.w, r = (t - s_po[k]) % el.w;
-                int i, j;
-                boundary_node(f, C.nx, C.ny, i, j);
-                T acc = T(0);
-                for (int c = el.x; c < el.y; ++c) {
+        // inflow face fluxes of the item's elements into Fy (the W region is free)
+        if (fl.bc) {
+            for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = T(0);
+            // T[jj][r] of every coupling, flattened over (coupling, jj, r); t
+            // grows per thread, so the coupling index only moves forward
+            {
+                int c = 0;
+                for (int t = threadIdx.x; t < it.ttot; t += blockDim.x) {
+                    while (t >= sc[c].toff + sc[c].m1 * sc[c].nth) ++c;
                     const TileCpl& en = sc[c];
-                    const int F = en.face;
-                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                    (F == 3 && j == 0);
-                    if (!on) continue;
-                    const int q = (F % 2 == 0) ? j : i;
-                    if constexpr (kParity) {
-                        if (en.tested) {
-                            // keep dcoeff*Es*Et iff |.| > 1e-15, tested in FP32 with
-                            // an FP64 fallback within 1e-6 of the threshold
-                            const CplDev cp = v.cpls[en.k];
-                            const T* Es = v.mort + cp.es;
-                            const T* Et = v.mort + cp.et;
-                            const T dc = v.cplc[en.k];
-                            const float hi = 1.e-15f * (1.f + 1.e-6f), lo = 1.e-15f * (1.f - 1.e-6f);
-                            for (int jj = 0; jj < en.m1; ++jj) {
-                                const T des = dc * Es[jj * en.n0 + q];
-                                const float fdes = fabsf((float)des);
-                                const T* xl = x + en.base + (int64_t)jj * en.stride;
-                                T s = T(0);
-                                for (int a = 0; a < en.nt1; ++a) {
-                                    const T et = Et[a * en.nth + r];
-                                    const float pf = fdes * fabsf(par.mortf[cp.et + a * en.nth + r]);
-                                    bool keep = pf > hi;
-                                    if (!keep && pf >= lo) keep = tabs(des * et) > T(kBcTol);
-                                    s = fma(keep ? et : T(0), xl[a], s);
+                    if (kParity && en.tested) continue;   // summed term by term below
+                    const int q = t - en.toff, jj = small_div(q, s_rcp[en.nth]), r = q - jj * en.nth;
+                    const T* Et = (kParity ? par.mortc : v.mort) + en.et;
+                    const T* xl = x + en.base + (int64_t)jj * en.stride;
+                    // every load of the line issued before the sum (nt1 <= kMaxNodes)
+                    T acc = T(0);
+#pragma unroll
+                    for (int a = 0; a < kMaxNodes; ++a)
+                        if (a < en.nt1) acc = fma(Et[a * en.nth + r], xl[a], acc);
+                    Tb[t] = acc;
+                }
+            }
+            __syncthreads();
+            // one thread per (boundary node, row): the element's couplings on the
+            // node's faces in a fixed order, so the sum is deterministic
+            {
+                const float rM = __frcp_rn((float)M);
+                for (int t = threadIdx.x; t < it.ctot; t += blockDim.x) {
+                    const int f = small_div(t, rM), m = t - f * M;
+                    const int R = it.row0 + m, k = rcell[R];
+                    const int r = R - crow[k];
+                    const int c0 = ccpl[k] - it.cpl0, c1 = ccpl[k + 1] - it.cpl0;
+                    int i, j;
+                    boundary_node(f, C.nx, C.ny, i, j);
+                    T acc = T(0);
+                    for (int c = c0; c < c1; ++c) {
+                        const TileCpl& en = sc[c];
+                        const int F = en.face;
+                        const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) ||
+                                        (F == 2 && i == 0) || (F == 3 && j == 0);
+                        if (!on) continue;
+                        const int q = (F % 2 == 0) ? j : i;
+                        if constexpr (kParity) {
+                            if (en.tested) {
+                                // keep dcoeff*Es*Et iff |.| > 1e-15, tested in FP32 with
+                                // an FP64 fallback within 1e-6 of the threshold
+                                const CplDev cp = v.cpls[en.k];
+                                const T* Es = v.mort + cp.es;
+                                const T* Et = v.mort + cp.et;
+                                const T dc = v.cplc[en.k];
+                                const float hi = 1.e-15f * (1.f + 1.e-6f), lo = 1.e-15f * (1.f - 1.e-6f);
+                                for (int jj = 0; jj < en.m1; ++jj) {
+                                    const T des = dc * Es[jj * en.n0 + q];
+                                    const float fdes = fabsf((float)des);
+                                    const T* xl = x + en.base + (int64_t)jj * en.stride;
+                                    T s = T(0);
+                                    for (int a = 0; a < en.nt1; ++a) {
+                                        const T et = Et[a * en.nth + r];
+                                        const float pf = fdes * fabsf(par.mortf[cp.et + a * en.nth + r]);
+                                        bool keep = pf > hi;
+                                        if (!keep && pf >= lo) keep = tabs(des * et) > T(kBcTol);
+                                        s = fma(keep ? et : T(0), xl[a], s);
+                                    }
+                                    acc += des * s;
                                 }
-                                acc += des * s;
+                            } else {
+                                const T* Es = par.mortc + en.es;
+                                T sacc = T(0);
+                                for (int jj = 0; jj < en.m1; ++jj)
+                                    sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+                                acc += sacc;
                             }
                         } else {
-                            const T* Es = par.mortc + en.es;
+                            const T* Es = v.mort + en.es;
                             T sacc = T(0);
                             for (int jj = 0; jj < en.m1; ++jj)
                                 sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
-                            acc += sacc;
+                            acc = fma(T(en.dc), sacc, acc);
                         }
-                    } else {
-                        const T* Es = v.mort + en.es;
-                        T sacc = T(0);
-                        for (int jj = 0; jj < en.m1; ++jj)
-                            sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
-                        acc = fma(T(en.dc), sacc, acc);
                     }
+                    Fy[m * nijp + i * C.ny + j] = acc;
                 }
-                Fy[(el.z + r) * nijp + i * C.ny + j] = acc;
             }
+            __syncthreads();
         }
+        const int d0 = nij * it.row0, d1 = nij * (it.row0 + M);
+        int k = it.cell_begin;
+        for (int d = d0 + threadIdx.x; d < d1; d += blockDim.x) {
+            while (d >= nij * crow[k + 1]) ++k;
+            const int nth = crow[k + 1] - crow[k];
+            const int l = d - nij * crow[k];
+            const int ij = small_div(l, s_rcp[nth]), r = l - ij * nth;
+            const int i = small_div(ij, rny), j = ij - i * C.ny;
+            const int flg = cflg[k];
+            if (fl.mask_rows && bdry_node(flg >> 4, i, j, C.nx, C.ny)) {
+                yc[d] = T(0);
+                continue;
+            }
+            const int R = crow[k] + r;
+            const int m = R - it.row0;   // row within the item
+            const T* rw = rowt + R * kRowVals;
+            const T xself = Xs[R * nijp + ij];
+            const T mterm = rw[0] * kwn[ij];
+            T acc = T(0);
+            if constexpr (kParity) {
+                if (scat) {
+                    const int node = C.node_off + ij;
+                    const T swv = swn[ij];
+                    const T cw = dxdy8 * swv;
+                    const int cls = par.scls[node];
+                    T s = T(0);
+                    if (cls == 1) {
+                        s = Ys[m * nijp + ij];
+                    } else if (cls == 2 && par.kbase[node] >= 0) {
+                        // some terms kept, some dropped: the host's keep mask of row R
+                        uint64_t mk = par.kmask[par.kbase[node] + R];
+                        const T* wr = Wg + (int64_t)R * Nth;
+                        while (mk) {
+                            const int c = __ffsll((long long)mk) - 1;
+                            mk &= mk - 1;
+                            s = fma(wr[c], Xs[c * nijp + ij], s);
+                        }
+                    } else if (cls == 2) {
+                        // some terms kept, some dropped: test each one
+                        const bool skip_cross = !(tabs(swv) > small);
+                        const int c0 = skip_cross ? crow[k] : 0;
+                        const int c1 = skip_cross ? crow[k] + nth : Nth;
+                        const float cwf = fabsf((float)cw);
+                        const float hi = 1.e-14f * (1.f + 1.e-6f), lo = 1.e-14f * (1.f - 1.e-6f);
+                        const float* Wf = par.Wf + v.W_off[C.sig];
+                        for (int c = c0; c < c1; ++c) {
+                            const T wv = Wg[(int64_t)R * Nth + c];
+                            const float pf = cwf * fabsf(Wf[(int64_t)R * Nth + c]);
+                            bool keep = pf > hi;
+                            if (!keep && pf >= lo) keep = tabs(cw * wv) > small;
+                            s = fma(keep && c != R ? wv : T(0), Xs[c * nijp + ij], s);
+                        }
+                    }
+                    const T vd = (fl.merged ? mterm : T(0)) - cw * Wg[(int64_t)R * Nth + R];
+                    acc = -cw * s + (tabs(vd) > small ? vd : T(0)) * xself;
+                }
+                if (fl.mass && !fl.merged) acc += mterm * xself;
+            } else {
+                if (scat) acc = -dxdy8 * swn[ij] * Ys[m * nijp + ij];
+                if (fl.mass) acc += mterm * xself;
+            }
+            if (fl.ic) {
+                const T* xr = Xs + R * nijp;
+                T t1 = T(0), t2 = T(0);
+                const T* gy = Gys + j * C.ny;
+                for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
+                const T* gx = Gxs + i * C.nx;
+                for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * xr[ii * C.ny + j];
+                const T ic = rw[1] * wxs[i] * rw[4] * t1 + rw[2] * wys[j] * rw[5] * t2;
+                acc += T(fl.ic_sign) * ic;
+            }
+            if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
+                acc += Fy[m * nijp + ij];
+                // outflow faces: the diagonal term (rt/boundary_convection_matrix.py:276-346)
+                for (int F = 0; F < 4; ++F) {
+                    if (!(flg & (1 << F))) continue;
+                    const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
+                                    (F == 3 && j == 0);
+                    if (!on) continue;
+                    const T dc = (F % 2 == 0) ? rw[2] : rw[1];
+                    const T w = (F % 2 == 0) ? wys[j] : wxs[i];
+                    const T val = dc * w * rw[3] * rw[6 + F];
+                    if (!kParity || tabs(val) > T(kBcTol)) acc += val * xself;
+                }
+            }
+            yc[d] = acc;
+        }
+        // the next item overwrites the couplings and the item region
         __syncthreads();
     }
-    const T small = T(kSmall);
-    const T dxdy8 = v.colc[ci];
-    const T* Gx = v.G + gofs(C.nx);
-    const T* Gy = v.G + gofs(C.ny);
-    T* yc = y + C.dof_off;
-    const int d0 = cbeg[it.cell_begin], d1 = cbeg[it.cell_end];
-    int k = it.cell_begin;
-    for (int d = d0 + threadIdx.x; d < d1; d += blockDim.x) {
-        while (d >= cbeg[k + 1]) ++k;
-        const int e = C.elem_begin + k;
-        const int nth = (cbeg[k + 1] - cbeg[k]) / nij;
-        const int l = d - cbeg[k];
-        const int r = l % nth, ij = l / nth, j = ij % C.ny, i = ij / C.ny;
-        const ElemDev E = v.elems[e];
-        if (fl.mask_rows && bdry_node(E.flags >> 4, i, j, C.nx, C.ny)) {
-            yc[d] = T(0);
-            continue;
-        }
-        const int R = crow[k] + r;
-        const T* A = v.ang + E.ang;
-        const T xself = Xs[R * nijp + ij];
-        const int node = C.node_off + ij;
-        const T mterm = v.econst[4 * e] * A[r] * v.kw[node];
-        T acc = T(0);
-        if constexpr (kParity) {
-            if (fl.scat) {
-                const T swv = v.sw[node];
-                const T cw = dxdy8 * swv;
-                const int cls = par.scls[node];
-                T s = T(0);
-                if (cls == 1) {
-                    s = Ys[(R - it.row0) * nijp + ij];
-                } else if (cls == 2 && par.kbase[node] >= 0) {
-                    // some terms kept, some dropped: the host's keep mask of row R
-                    uint64_t mk = par.kmask[par.kbase[node] + R];
-                    const T* wr = Wg + (int64_t)R * Nth;
-                    while (mk) {
-                        const int c = __ffsll((long long)mk) - 1;
-                        mk &= mk - 1;
-                        s = fma(wr[c], Xs[c * nijp + ij], s);
-                    }
-                } else if (cls == 2) {
-                    // some terms kept, some dropped: test each one
-                    const bool skip_cross = !(tabs(swv) > small);
-                    const int c0 = skip_cross ? crow[k] : 0;
-                    const int c1 = skip_cross ? crow[k] + nth : Nth;
-                    const float cwf = fabsf((float)cw);
-                    const float hi = 1.e-14f * (1.f + 1.e-6f), lo = 1.e-14f * (1.f - 1.e-6f);
-                    const float* Wf = par.Wf + v.W_off[C.sig];
-                    for (int c = c0; c < c1; ++c) {
-                        const T wv = Wg[(int64_t)R * Nth + c];
-                        const float pf = cwf * fabsf(Wf[(int64_t)R * Nth + c]);
-                        bool keep = pf > hi;
-                        if (!keep && pf >= lo) keep = tabs(cw * wv) > small;
-                        s = fma(keep && c != R ? wv : T(0), Xs[c * nijp + ij], s);
-                    }
-                }
-                const T vd = (fl.merged ? mterm : T(0)) - cw * Wg[(int64_t)R * Nth + R];
-                acc = -cw * s + (tabs(vd) > small ? vd : T(0)) * xself;
-            }
-            if (fl.mass && !fl.merged) acc += mterm * xself;
-        } else {
-            if (fl.scat) acc = -dxdy8 * v.sw[node] * Ys[(R - it.row0) * nijp + ij];
-            if (fl.mass) acc += mterm * xself;
-        }
-        if (fl.ic) {
-            const T* xr = Xs + R * nijp;
-            T t1 = T(0), t2 = T(0);
-            const T* gy = Gy + j * C.ny;
-            for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
-            const T* gx = Gx + i * C.nx;
-            for (int ii = 0; ii < C.nx; ++ii) t2 += gx[ii] * xr[ii * C.ny + j];
-            const T ic = v.econst[4 * e + 1] * v.lglw[C.nx * kMaxNodes + i] * A[nth + r] * t1 +
-                         v.econst[4 * e + 2] * v.lglw[C.ny * kMaxNodes + j] * A[2 * nth + r] * t2;
-            acc += T(fl.ic_sign) * ic;
-        }
-        if (fl.bc && (i == 0 || j == 0 || i == C.nx - 1 || j == C.ny - 1)) {
-            acc += Fy[(R - it.row0) * nijp + ij];
-            // outflow faces: the diagonal term (rt/boundary_convection_matrix.py:276-346)
-            for (int F = 0; F < 4; ++F) {
-                if (!(E.flags & (1 << F))) continue;
-                const bool on = (F == 0 && i == C.nx - 1) || (F == 1 && j == C.ny - 1) || (F == 2 && i == 0) ||
-                                (F == 3 && j == 0);
-                if (!on) continue;
-                const T dc = (F % 2 == 0) ? v.econst[4 * e + 2] : v.econst[4 * e + 1];
-                const T w = (F % 2 == 0) ? v.lglw[C.ny * kMaxNodes + j] : v.lglw[C.nx * kMaxNodes + i];
-                const T val = dc * w * A[r] * A[(3 + F) * nth + r];
-                if (!kParity || tabs(val) > T(kBcTol)) acc += val * xself;
-            }
-        }
-        yc[d] = acc;
+}
+
+// ------------------------------------------------- tensor-core scattering
+// FP32 scattering product on the 5th-generation tensor cores: one CTA per
+// (column, tile of 128 angular rows): D[m][ij] = sum_c W[R0+m][c] X[c][ij],
+// then y[R0+m, ij] += -(dx dy / 8) sw_ij D[m][ij] (the tiled kernel has
+// written the other terms; rows of inflow-boundary nodes stay masked).
+// Operands are staged in K-chunks of kTcK angular nodes, each value split
+// into TF32 hi + lo parts (hi = round-to-nearest TF32, lo = value - hi), and
+// D accumulates A_lo B_hi + A_hi B_lo + A_hi B_hi with tcgen05.mma
+// (kind::tf32, M = 128, N = nij padded to 16, K = 8 per instruction, one
+// issuing thread) in tensor memory; tcgen05.commit signals the chunk's
+// completion on an mbarrier before the operands are restaged.  Shared-memory
+// operands use the canonical K-major layout without swizzle: 8-row x 16-byte
+// core matrices, K-adjacent ones 128 bytes apart, 8-row groups
+// kTcK/4 * 128 bytes apart.
+constexpr int kTcThreads = 256;
+constexpr int kTcM = 128;
+constexpr int kTcK = 32;
+
+struct TcItem {
+    int col, row0, rows, pad;
+};
+
+__host__ __device__ __forceinline__ int tc_np(int nij) { return nij <= 16 ? 16 : (nij + 15) & ~15; }
+__host__ __device__ __forceinline__ int tc_tmem_cols(int np) {
+    int c = 32;
+    while (c < np) c <<= 1;
+    return c;
+}
+// staged operands (floats): A hi/lo [kTcM x kTcK], B hi/lo [np x kTcK]
+__host__ __device__ __forceinline__ int tc_operand_floats(int np) { return 2 * (kTcM + np) * kTcK; }
+
+// float offset of (row, k) in the canonical layout
+__device__ __forceinline__ int tc_off(int row, int k) {
+    return (row >> 3) * (kTcK / 4) * 32 + (k >> 2) * 32 + (row & 7) * 4 + (k & 3);
+}
+
+__device__ __forceinline__ uint64_t tc_desc(const float* p) {
+    const uint64_t a = (uint64_t)__cvta_generic_to_shared(p);
+    const uint64_t lbo = 128, sbo = (kTcK / 4) * 128;
+    return ((a >> 4) & 0x3FFFull) | (((lbo >> 4) & 0x3FFFull) << 16) | (((sbo >> 4) & 0x3FFFull) << 32) |
+           (1ull << 46);   // descriptor version 1, base offset 0, no swizzle
+}
+
+__device__ __forceinline__ float tf32_hi(float v) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__global__ void __launch_bounds__(kTcThreads)
+scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items, const float* __restrict__ x,
+               float* __restrict__ y, int* __restrict__ status) {
+    extern __shared__ __align__(128) float tsm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+    __shared__ int s_crow[kMaxCellsStaged + 1];
+    __shared__ int s_cflg[kMaxCellsStaged];
+    if (v.stop && *v.stop) return;
+    const TcItem it = items[blockIdx.x];
+    if (v.skip && v.skip[it.col]) return;
+    const ColDev C = v.cols[it.col];
+    const ApplyFlags fl = decode(flags);
+    const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
+    const int np = tc_np(nij), ncols = tc_tmem_cols(np);
+    float* Ah = tsm;
+    float* Al = Ah + kTcM * kTcK;
+    float* Bh = Al + kTcM * kTcK;
+    float* Bl = Bh + np * kTcK;
+    int* rcell = reinterpret_cast<int*>(Bl + np * kTcK);   // [Nth] cell of each row
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < ncell; k += blockDim.x) {
+        const ElemDev E = v.elems[C.elem_begin + k];
+        s_crow[k] = E.row;
+        s_cflg[k] = E.flags;
+        if (k == ncell - 1) s_crow[ncell] = Nth;
+        for (int r = 0; r < E.nth; ++r) rcell[E.row + r] = k;
     }
+    if (threadIdx.x == 0) {
+        s_abort = 0;
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_tmem);
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s_tmem;
+    // kind::tf32: D F32 (bits 4-5 = 1), A and B TF32 (bits 7-9, 10-12 = 2),
+    // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(np >> 3) << 17) |
+                           ((uint32_t)(kTcM >> 4) << 24);
+    const float* W = v.W + v.W_off[C.sig];
+    const float* xc = x + C.dof_off;
+    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const int nchunk = (Nth + kTcK - 1) / kTcK;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int c0 = ch * kTcK;
+        // A = W rows R0 .. R0+127, columns c0 .. c0+kTcK-1 (zero outside)
+        for (int t = threadIdx.x; t < kTcM * kTcK; t += blockDim.x) {
+            const int m = t / kTcK, k = t % kTcK, c = c0 + k;
+            const float w = (m < it.rows && c < Nth) ? __ldg(W + (int64_t)(it.row0 + m) * Nth + c) : 0.f;
+            const float h = tf32_hi(w);
+            Ah[tc_off(m, k)] = h;
+            Al[tc_off(m, k)] = w - h;
+        }
+        // B (N x K, K-major): B[ij][k] = x at angular row c0 + k, node ij
+        for (int t = threadIdx.x; t < np * kTcK; t += blockDim.x) {
+            const int n = t / kTcK, k = t % kTcK, c = c0 + k;
+            float xv = 0.f;
+            if (n < nij && c < Nth) {
+                const int kc = rcell[c];
+                const int nth = s_crow[kc + 1] - s_crow[kc];
+                xv = __ldg(xc + nij * s_crow[kc] + n * nth + (c - s_crow[kc]));
+            }
+            const float h = tf32_hi(xv);
+            Bh[tc_off(n, k)] = h;
+            Bl[tc_off(n, k)] = xv - h;
+        }
+        // generic-proxy writes -> visible to the tensor cores
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int s = 0; s < kTcK / 8; ++s) {
+                const int o = 64 * s;   // two K-adjacent core matrices per K = 8
+                tc_mma(tmem, tc_desc(Al + o), tc_desc(Bh + o), idesc, ch > 0 || s > 0);
+                tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bl + o), idesc, 1);
+                tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bh + o), idesc, 1);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
+                         : "memory");
+        }
+        // the chunk's MMAs have read the operands before they are restaged
+        {
+            uint32_t done = 0;
+            for (int spin = 0; spin < (1 << 22) && !done; ++spin)
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                    "selp.u32 %0, 1, 0, p;\n\t}"
+                    : "=r"(done)
+                    : "r"(mb), "r"((uint32_t)(ch & 1))
+                    : "memory");
+            if (!done) s_abort = 1;
+        }
+        __syncthreads();
+        if (s_abort) break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (s_abort) {
+        if (threadIdx.x == 0 && status) atomicExch(status, RTG_ERR_TIMEOUT);
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows), columns
+        // [h np/2, (h+1) np/2) with h = w / 4
+        const int q = warp & 3, h = warp >> 2;
+        const int m = 32 * q + lane, R = it.row0 + m;
+        const bool valid = m < it.rows;
+        const int kc = valid ? rcell[R] : 0;
+        const int nth = s_crow[kc + 1] - s_crow[kc];
+        const int r = R - s_crow[kc];
+        const float dxdy8 = v.colc[it.col];
+        const int half = np / 2;
+        for (int cb = h * half; cb < (h + 1) * half; cb += 8) {
+            uint32_t d[8];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+                "tcgen05.wait::ld.sync.aligned;"
+                : "=r"(d[0]), "=r"(d[1]), "=r"(d[2]), "=r"(d[3]), "=r"(d[4]), "=r"(d[5]), "=r"(d[6]), "=r"(d[7])
+                : "r"(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)cb)
+                : "memory");
+            if (!valid) continue;
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const int ij = cb + jj;
+                if (ij >= nij) break;
+                const int i = ij / C.ny, j = ij % C.ny;
+                if (fl.mask_rows && bdry_node(s_cflg[kc] >> 4, i, j, C.nx, C.ny)) continue;
+                const int64_t dof = C.dof_off + (int64_t)nij * s_crow[kc] + (int64_t)ij * nth + r;
+                y[dof] += -dxdy8 * v.sw[C.node_off + ij] * __uint_as_float(d[jj]);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+static size_t tc_smem_bytes(int nij, int nth_col) {
+    return sizeof(float) * (size_t)tc_operand_floats(tc_np(nij)) + sizeof(int) * (size_t)nth_col + 16;
 }
 
 // ------------------------------------------------------------ global path
@@ -762,9 +1056,8 @@ __global__ void weight_forcing_kernel(OpView<double> v, const double* f, double*
 // outputs, heaviest chunks first, in two launch groups: with the column's W
 // staged too, or (large angular meshes) with W read through L2.
 constexpr int kChunk = 1024;
-// The FP64 apply is FP64-pipe bound and, with large items, all of them fit in
-// one wave, so the heaviest item sets the kernel time: smaller items balance
-// the SMs (the item size is tuned per handle, tune_plan64).
+// FP64 chunks of the per-output kernels are smaller: that path is FP64-pipe
+// bound, and smaller chunks balance the SMs.
 constexpr int kChunk64 = 256;
 
 struct ApplyGroup {
@@ -776,15 +1069,23 @@ struct ApplyGroup {
 
 constexpr int kTileRows = 64;       // default row cap (before tuning)
 constexpr int kTileOut = 2048;
-constexpr int kTuneCaps[] = {16, 32, 64, 128};
-constexpr int kNumTuneCaps = 4;
+// launches of the tiled kernel: groups that fit 4, 3, 2 or 1 CTAs per SM
+constexpr int kSmemClasses = 4;
 
-// Tuning record of one degree class: nx, ny, the column's angular nodes
-// rounded up to a power of two, the chosen row cap, and the measured time (ns)
-// of the class's items with each candidate cap (-1: not run).
+// Shape of a tiled plan: angular rows per item, items per CTA (0: the whole
+// column), and whether the CTAs are launched per shared-memory class (each
+// launch with its own dynamic shared memory) or in one launch.
+struct PlanShape {
+    int rows = kTileRows;
+    int gcap = 0;
+    int split = 0;
+    int tc = 0;    // FP32: scattering of the tiled columns on the tensor cores (scat_tc_kernel)
+};
+
+// One timed plan shape of the autotuner (time in ns, -1: not run).
 struct TuneRecord {
-    int nx, ny, nthb, cap;
-    int ns[kNumTuneCaps];
+    PlanShape shape;
+    int chosen, ns, items, groups, launches;
 };
 
 // Tables of the FP64 tiled path (drop rules resolved on the host): the
@@ -806,10 +1107,17 @@ struct ApplyPlan {
     ApplyGroup g[2];            // 0: input and W staged; 1: input staged, W read through L2
     int32_t* d_slow = nullptr;
     int nslow = 0;
-    TileItem* d_tiles = nullptr;   // tiled items
+    TileItem* d_tiles = nullptr;   // tiled items, grouped per CTA
     TileCpl* d_tile_cpl = nullptr; // their coupling entries
     int ntiles = 0;
-    size_t tile_smem = 0;
+    int4* d_tgroups = nullptr;     // per CTA: column, first item, end item
+    int tg_begin[kSmemClasses + 1] = {};   // CTAs of launch q: [tg_begin[q], tg_begin[q+1])
+    size_t tg_smem[kSmemClasses] = {};     // dynamic shared memory of launch q
+    size_t tile_smem = 0;                  // the largest of them
+    TcItem* d_tc = nullptr;                // tensor-core scattering CTAs
+    int ntc = 0;
+    size_t tc_smem = 0;
+    int* d_status = nullptr;               // RTG_ERR_TIMEOUT if a wait of scat_tc_kernel gave up
     const ParityTables* par = nullptr;   // FP64 tiled path
     bool own_par = false;
     std::vector<TuneRecord> tuning;
@@ -983,30 +1291,64 @@ static ParityTables* build_parity(const rtg_handle* h) {
     return pt;
 }
 
-// Tiled items of the FP32 path: consecutive cells of a column, at most
-// kTileRows angular rows and kTileOut outputs per item, when the column's
-// input, the item's W rows and its products fit in shared memory.
+// Tiled items: consecutive cells of a column, at most `rows` angular rows and
+// kTileOut outputs per item.  A CTA takes a group of consecutive items of one
+// column (gcap items, 0: all of them) and stages the column's input once.
+// Shared memory of a group: the column part (input, column table, cell
+// rows and flags) and the largest item region of its items.
+static size_t tile_col_bytes(size_t vsize, int nth_col, int nx, int ny, int ncell) {
+    const int nijp = (nx * ny + 3) & ~3, nthp = (nth_col + 3) & ~3;
+    return vsize * ((size_t)nth_col * nijp + (size_t)col_table_size(nx, ny) + (size_t)nthp * kRowVals) +
+           sizeof(int) * col_int_words(ncell, nth_col) + 16;
+}
+static size_t tile_item_bytes(size_t vsize, int nx, int ny, int wcap, int M) {
+    const int nijp = (nx * ny + 3) & ~3, Mp = (M + 3) & ~3;
+    return vsize * ((size_t)wcap + (size_t)Mp * nijp);
+}
 
-
-static size_t tile_smem_bytes(size_t vsize, int nth_col, int nij, int wcap, int M, int ncell) {
-    const int nijp = (nij + 3) & ~3, Mp = (M + 3) & ~3;
-    return vsize * ((size_t)nth_col * nijp + (size_t)wcap + (size_t)Mp * nijp) + sizeof(int) * (2 * ncell + 2) + 16;
+// Dynamic shared memory that lets q CTAs of the tiled kernel share an SM,
+// for q = 4, 3, 2, 1 (index 0..3).
+template <typename T>
+static void smem_class_limits(size_t lim[kSmemClasses]) {
+    int dev = 0, per_sm = 0, resv = 0;
+    RTG_CUDA(cudaGetDevice(&dev));
+    RTG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    RTG_CUDA(cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+    cudaFuncAttributes fa{};
+    RTG_CUDA(cudaFuncGetAttributes(&fa, apply_tiled_kernel<T, sizeof(T) == 8>));
+    // CTAs per SM that registers and threads allow
+    int maxb = 0;
+    RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, apply_tiled_kernel<T, sizeof(T) == 8>,
+                                                           tiled_threads<T>(), 0));
+    for (int q = 0; q < kSmemClasses; ++q) {
+        const int per = kSmemClasses - q;
+        const long long l = (long long)per_sm / per - resv - (long long)fa.sharedSizeBytes;
+        lim[q] = per > maxb ? 0 : (size_t)std::max(0ll, std::min(l, (long long)kSmemBudget));
+    }
 }
 
 // cap: per column, the largest number of angular rows of a tiled item;
 // include: per column, whether the plan covers it (null: every column);
 // par: the FP64 tiled path's tables (null: FP64 columns use the per-output
-// kernels).
+// kernels); gcap, split: see PlanShape.
 template <typename T>
 static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = nullptr,
                             const std::vector<char>* include = nullptr, int chunk64 = kChunk64,
-                            const ParityTables* par = nullptr) {
+                            const ParityTables* par = nullptr, int gcap = 0, int split = 0, int tc = 0) {
     const HostTables& t = h->host;
     constexpr bool parity = sizeof(T) == 8;
+    if (parity) tc = 0;
+    std::vector<std::pair<int64_t, TcItem>> tcv;
     ApplyPlan* p = new ApplyPlan();
     std::vector<std::pair<int64_t, int4>> items[2];
-    std::vector<std::pair<int64_t, TileItem>> tiles;
-    std::vector<std::vector<TileCpl>> tile_cpl;   // coupling entries per tiled item
+    struct GroupRec {
+        int64_t cost;
+        size_t smem;
+        int col;
+        std::vector<TileItem> its;
+        std::vector<std::vector<TileCpl>> ents;
+    };
+    std::vector<GroupRec> groups;
     std::vector<int32_t> slow;
     size_t need[2] = {0, 0};
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
@@ -1018,12 +1360,14 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         if ((!parity || par) && ncell <= kMaxCellsStaged) {
             // split the column into items of whole cells
             std::vector<TileItem> its;
+            std::vector<size_t> ibytes;
+            std::vector<int64_t> icost;
             bool fits = true;
             int k = 0;
             std::vector<std::vector<TileCpl>> ents;
-            std::vector<size_t> bytes;
             while (k < ncell && fits) {
-                TileItem ti{ci, k, k, t.elems[C.elem_begin + k].row, 0, 0, 0, 0, 0, 0};
+                TileItem ti{ci, k, k, t.elems[C.elem_begin + k].row, 0, 0, 0, 0, 0, 0, 0,
+                            t.elems[C.elem_begin + k].cpl_begin};
                 int M = 0, ncp = 0;
                 while (k < ncell) {
                     const ElemDev& E = t.elems[C.elem_begin + k];
@@ -1036,9 +1380,10 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                     ++k;
                 }
                 ti.cell_end = k;
+                ti.M = M;
                 if (ncp > kMaxItemCpl) fits = false;
                 std::vector<TileCpl> en;
-                int tsz = 0, csz = 0;
+                int tsz = 0;
                 for (int q = ti.cell_begin; q < ti.cell_end; ++q) {
                     const ElemDev& E = t.elems[C.elem_begin + q];
                     for (int kk = E.cpl_begin; kk < E.cpl_end; ++kk) {
@@ -1049,7 +1394,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                         tc.rowloc = E.row - ti.row0;
                         tc.nth = E.nth;
                         tc.toff = tsz;
-                        tc.coff = csz;
+                        tc.coff = 0;
                         tc.m1 = g.m1;
                         tc.nt1 = g.nth1;
                         tc.face = cp.face;
@@ -1062,35 +1407,42 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                         tc.tested = parity ? par->tested[kk] : 0;
                         en.push_back(tc);
                         tsz += g.m1 * E.nth;
-                        csz += tc.n0 * E.nth;
                     }
                 }
                 ti.ttot = tsz;
-                ti.ctot = 0;
-                for (int q = ti.cell_begin; q < ti.cell_end; ++q)
-                    ti.ctot += boundary_nodes(C.nx, C.ny) * t.elems[C.elem_begin + q].nth;
-                (void)csz;
+                ti.ctot = boundary_nodes(C.nx, C.ny) * M;
                 const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
                 // Fy and Ys are read and written four values at a time: keep
                 // every region a multiple of 4 values from the aligned base
                 ti.tsz = (tsz + 3) & ~3;
-                ti.wcap = std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
+                // without the scattering product (tensor-core path) the region holds T and Fy only
+                ti.wcap = tc ? ti.tsz + Mp * nijp : std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
                 if ((ti.wcap & 3) || (ti.tsz & 3) || (nijp & 3))
                     throw RtgError{RTG_ERR_ARG, "tiled apply: unaligned shared-memory region"};
-                const size_t b = tile_smem_bytes(sizeof(T), C.nth_col, nij, ti.wcap, M, ncell);
-                if (b > kSmemBudget) fits = false;
-                bytes.push_back(b);
+                ibytes.push_back(tile_item_bytes(sizeof(T), C.nx, C.ny, ti.wcap, M));
+                icost.push_back((int64_t)M * nij * (C.nth_col + C.nx + C.ny) + C.ndof);
                 ents.push_back(std::move(en));
                 its.push_back(ti);
             }
+            const size_t cb = tile_col_bytes(sizeof(T), C.nth_col, C.nx, C.ny, ncell);
+            for (size_t q = 0; q < its.size() && fits; ++q)
+                if (cb + ibytes[q] > kSmemBudget) fits = false;
+            if (tc && tc_smem_bytes(nij, C.nth_col) > kSmemBudget) fits = false;
             if (fits) {
-                for (size_t q = 0; q < its.size(); ++q) {
-                    const TileItem& ti = its[q];
-                    int M = 0;
-                    for (int r = ti.cell_begin; r < ti.cell_end; ++r) M += t.elems[C.elem_begin + r].nth;
-                    p->tile_smem = std::max(p->tile_smem, bytes[q]);
-                    tiles.push_back({(int64_t)M * nij * (C.nth_col + C.nx + C.ny) + C.ndof, ti});
-                    tile_cpl.push_back(std::move(ents[q]));
+                if (tc)
+                    for (int r0 = 0; r0 < C.nth_col; r0 += kTcM)
+                        tcv.push_back({(int64_t)std::min(kTcM, C.nth_col - r0) * C.nth_col * tc_np(nij),
+                                       TcItem{ci, r0, std::min(kTcM, C.nth_col - r0), 0}});
+                const size_t per = gcap > 0 ? (size_t)gcap : its.size();
+                for (size_t q0 = 0; q0 < its.size(); q0 += per) {
+                    GroupRec g{0, 0, ci, {}, {}};
+                    for (size_t q = q0; q < std::min(its.size(), q0 + per); ++q) {
+                        g.cost += icost[q];
+                        g.smem = std::max(g.smem, cb + ibytes[q]);
+                        g.its.push_back(its[q]);
+                        g.ents.push_back(std::move(ents[q]));
+                    }
+                    groups.push_back(std::move(g));
                 }
                 continue;
             }
@@ -1130,22 +1482,66 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
     }
     p->nslow = (int)slow.size();
     p->d_slow = (int32_t*)up(slow.data(), sizeof(int32_t) * slow.size());
-    std::vector<int> perm(tiles.size());
+    // CTAs: heaviest first within each launch; launches by shared-memory
+    // class, fewest CTAs per SM first (split), or all in one
+    size_t lim[kSmemClasses];
+    if (split && !groups.empty()) {
+        smem_class_limits<T>(lim);
+    } else {
+        for (int q = 0; q < kSmemClasses; ++q) lim[q] = kSmemBudget;
+    }
+    auto cls = [&](size_t b) {
+        for (int q = 0; q < kSmemClasses; ++q)
+            if (b <= lim[q]) return q;
+        return kSmemClasses - 1;
+    };
+    std::vector<int> perm(groups.size());
     for (size_t q = 0; q < perm.size(); ++q) perm[q] = (int)q;
-    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return tiles[a].first > tiles[b].first; });
+    // launch order: class 3 (one CTA per SM) first, then 2, 1, 0
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+        const int ca = cls(groups[a].smem), cb2 = cls(groups[b].smem);
+        if (ca != cb2) return ca > cb2;
+        return groups[a].cost > groups[b].cost;
+    });
     std::vector<TileItem> tv;
     std::vector<TileCpl> ent;
+    std::vector<int4> tg;
+    int counts[kSmemClasses] = {};
     for (int q : perm) {
-        TileItem ti = tiles[q].second;
-        ti.cpl_begin = (int)ent.size();
-        ent.insert(ent.end(), tile_cpl[q].begin(), tile_cpl[q].end());
-        ti.cpl_end = (int)ent.size();
-        tv.push_back(ti);
+        GroupRec& g = groups[q];
+        const int c = cls(g.smem);
+        const int first = (int)tv.size();
+        for (size_t i = 0; i < g.its.size(); ++i) {
+            TileItem ti = g.its[i];
+            ti.cpl_begin = (int)ent.size();
+            ent.insert(ent.end(), g.ents[i].begin(), g.ents[i].end());
+            ti.cpl_end = (int)ent.size();
+            tv.push_back(ti);
+        }
+        tg.push_back(make_int4(g.col, first, (int)tv.size(), tc ? 1 : 0));
+        const int slot = kSmemClasses - 1 - c;   // launch index
+        counts[slot]++;
+        p->tg_smem[slot] = std::max(p->tg_smem[slot], g.smem);
+        p->tile_smem = std::max(p->tile_smem, g.smem);
     }
+    p->tg_begin[0] = 0;
+    for (int q = 0; q < kSmemClasses; ++q) p->tg_begin[q + 1] = p->tg_begin[q] + counts[q];
     p->ntiles = (int)tv.size();
     p->par = parity ? par : nullptr;
     p->d_tiles = (TileItem*)up(tv.data(), sizeof(TileItem) * tv.size());
     p->d_tile_cpl = (TileCpl*)up(ent.data(), sizeof(TileCpl) * ent.size());
+    p->d_tgroups = (int4*)up(tg.data(), sizeof(int4) * tg.size());
+    std::stable_sort(tcv.begin(), tcv.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    std::vector<TcItem> tci;
+    for (auto& pr : tcv) {
+        tci.push_back(pr.second);
+        const ColDev& C = t.cols[pr.second.col];
+        p->tc_smem = std::max(p->tc_smem, tc_smem_bytes(C.nx * C.ny, C.nth_col));
+    }
+    p->ntc = (int)tci.size();
+    p->d_tc = (TcItem*)up(tci.data(), sizeof(TcItem) * tci.size());
+    p->d_status = (int*)up(nullptr, 0);
+    RTG_CUDA(cudaMemset(p->d_status, 0, sizeof(int)));
     return p;
 }
 
@@ -1161,6 +1557,7 @@ static void set_plan_attributes(const ApplyPlan* p) {
     constexpr bool f64 = sizeof(T) == 8;
     raise_smem_limit((const void*)apply_col_kernel<T, T, f64>, std::max(p->g[0].smem, p->g[1].smem));
     if (p->ntiles) raise_smem_limit((const void*)apply_tiled_kernel<T, f64>, p->tile_smem);
+    if (p->ntc) raise_smem_limit((const void*)scat_tc_kernel, p->tc_smem);
 }
 
 template <typename T>
@@ -1168,28 +1565,31 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
                      T* y, cudaStream_t s) {
     constexpr bool f64 = sizeof(T) == 8;
     RTG_LAUNCHED("a kernel before the apply");
-    {
-        if (plan->ntiles) {
-            TileParity<T> tp{};
-            if constexpr (f64) {
-                tp.scls = plan->par->d_scls;
-                tp.mortc = plan->par->d_mortc;
-                tp.mortf = v32.mort;
-                tp.Wf = v32.W;
-                tp.colfull = plan->par->d_colfull;
-                tp.kbase = plan->par->d_kbase;
-                tp.kmask = plan->par->d_kmask;
-            }
-            apply_tiled_kernel<T, f64><<<plan->ntiles, kApplyThreads, plan->tile_smem, s>>>(
-                v, tp, flags, plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
+    if (plan->ntiles) {
+        TileParity<T> tp{};
+        if constexpr (f64) {
+            tp.scls = plan->par->d_scls;
+            tp.mortc = plan->par->d_mortc;
+            tp.mortf = v32.mort;
+            tp.Wf = v32.W;
+            tp.colfull = plan->par->d_colfull;
+            tp.kbase = plan->par->d_kbase;
+            tp.kmask = plan->par->d_kmask;
+        }
+        for (int q = 0; q < kSmemClasses; ++q) {
+            const int n = plan->tg_begin[q + 1] - plan->tg_begin[q];
+            if (!n) continue;
+            apply_tiled_kernel<T, f64><<<n, tiled_threads<T>(), plan->tg_smem[q], s>>>(
+                v, tp, flags, plan->d_tgroups + plan->tg_begin[q], plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
             const cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 cudaFuncAttributes fa{};
                 cudaFuncGetAttributes(&fa, apply_tiled_kernel<T, f64>);
-                throw RtgError{RTG_ERR_CUDA, "launch of apply_tiled_kernel (items " + std::to_string(plan->ntiles) +
-                                                 ", dynamic smem " + std::to_string(plan->tile_smem) + ", max dynamic " +
-                                                 std::to_string(fa.maxDynamicSharedSizeBytes) + ", static " +
-                                                 std::to_string(fa.sharedSizeBytes) + "): " + cudaGetErrorString(e)};
+                throw RtgError{RTG_ERR_CUDA, "launch of apply_tiled_kernel (CTAs " + std::to_string(n) +
+                                                 ", dynamic smem " + std::to_string(plan->tg_smem[q]) +
+                                                 ", max dynamic " + std::to_string(fa.maxDynamicSharedSizeBytes) +
+                                                 ", static " + std::to_string(fa.sharedSizeBytes) +
+                                                 "): " + cudaGetErrorString(e)};
             }
         }
     }
@@ -1205,134 +1605,76 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
         apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y), count_launch();
         RTG_LAUNCHED("apply_global_kernel");
     }
+    if constexpr (!f64) {
+        if (plan->ntc && (flags & (RTG_SYSTEM | RTG_SCAT))) {
+            scat_tc_kernel<<<plan->ntc, kTcThreads, plan->tc_smem, s>>>(v, flags, plan->d_tc, x, y, plan->d_status),
+                count_launch();
+            RTG_LAUNCHED("scat_tc_kernel");
+        }
+    }
 }
 
-// Autotuner of the FP32 path: for every degree class of columns, time the
-// class's items with each candidate row cap (one warm-up, best of three
-// launches, CUDA events) and keep the fastest; then build the plan with the
-// chosen cap per column.
-static ApplyPlan* tune_plan32(rtg_handle* h, cudaStream_t s) {
-    const HostTables& t = h->host;
-    const int nc = (int)t.cols.size();
-    auto pow2 = [](int n) {
-        int b = 1;
-        while (b < n) b <<= 1;
-        return b;
-    };
-    std::map<std::tuple<int, int, int>, std::vector<int>> classes;
-    for (int ci = 0; ci < nc; ++ci) {
-        const ColDev& C = t.cols[ci];
-        classes[std::make_tuple(C.nx, C.ny, pow2(C.nth_col))].push_back(ci);
-    }
-    float *x = nullptr, *y = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    std::vector<int> cap(nc, kTileRows);
-    std::vector<TuneRecord> recs;
-    try {
-        RTG_CUDA(cudaMalloc(&x, sizeof(float) * std::max<int64_t>(t.ndof, 1)));
-        RTG_CUDA(cudaMalloc(&y, sizeof(float) * std::max<int64_t>(t.ndof, 1)));
-        RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * t.ndof, s));
-        RTG_CUDA(cudaEventCreate(&e0));
-        RTG_CUDA(cudaEventCreate(&e1));
-        const uint32_t flags = RTG_SYSTEM | RTG_MASK_ROWS;
-        for (const auto& kv : classes) {
-            std::vector<char> inc(nc, 0);
-            for (int ci : kv.second) inc[ci] = 1;
-            TuneRecord r{std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first), kTileRows, {}};
-            float best = 1e30f;
-            for (int q = 0; q < kNumTuneCaps; ++q) {
-                r.ns[q] = -1;
-                std::vector<int> cq(nc, kTuneCaps[q]);
-                ApplyPlan* p = make_plan<float>(h, &cq, &inc);
-                try {
-                    set_plan_attributes<float>(p);
-                    run_plan<float>(p, h->v32, h->v32, flags, x, y, s);
-                    float tbest = 1e30f;
-                    for (int rep = 0; rep < 3; ++rep) {
-                        RTG_CUDA(cudaEventRecord(e0, s));
-                        run_plan<float>(p, h->v32, h->v32, flags, x, y, s);
-                        RTG_CUDA(cudaEventRecord(e1, s));
-                        RTG_CUDA(cudaEventSynchronize(e1));
-                        float ms = 0.f;
-                        RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                        tbest = std::min(tbest, ms);
-                    }
-                    r.ns[q] = (int)(tbest * 1e6f);
-                    // a larger cap must win by 3% to displace a smaller one
-                    if (tbest < best * 0.97f) {
-                        best = tbest;
-                        r.cap = kTuneCaps[q];
-                    }
-                } catch (...) {
-                    free_plan(p);
-                    throw;
-                }
-                free_plan(p);
-            }
-            for (int ci : kv.second) cap[ci] = r.cap;
-            recs.push_back(r);
-        }
-    } catch (...) {
-        if (x) cudaFree(x);
-        if (y) cudaFree(y);
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
-        throw;
-    }
-    // a class timed alone sees an idle GPU: keep the tuned plan only if the
-    // whole apply is faster with it than with the default item size
-    ApplyPlan* tuned = make_plan<float>(h, &cap, nullptr);
-    ApplyPlan* dflt = nullptr;
-    try {
-        dflt = make_plan<float>(h, nullptr, nullptr);
-        float tt = 1e30f, td = 1e30f;
-        for (ApplyPlan* p : {tuned, dflt}) {
-            set_plan_attributes<float>(p);
-            run_plan<float>(p, h->v32, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
-            for (int rep = 0; rep < 3; ++rep) {
-                RTG_CUDA(cudaEventRecord(e0, s));
-                run_plan<float>(p, h->v32, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
-                RTG_CUDA(cudaEventRecord(e1, s));
-                RTG_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                (p == tuned ? tt : td) = std::min(p == tuned ? tt : td, ms);
-            }
-        }
-        if (td < tt) {
-            std::swap(tuned, dflt);
-            for (TuneRecord& r : recs) r.cap = -r.cap;   // negative: class choice not used
-        }
-    } catch (...) {
-        free_plan(tuned);
-        free_plan(dflt);
-        cudaFree(x);
-        cudaFree(y);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        throw;
-    }
-    free_plan(dflt);
-    cudaFree(x);
-    cudaFree(y);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    tuned->tuning = std::move(recs);
-    return tuned;
+static int plan_launches(const ApplyPlan* p) {
+    int n = (p->g[0].nitems > 0) + (p->g[1].nitems > 0) + (p->nslow > 0) + (p->ntc > 0);
+    for (int q = 0; q < kSmemClasses; ++q) n += p->tg_begin[q + 1] > p->tg_begin[q];
+    return n;
 }
 
-// FP64 apply: columns that fit in shared memory run the tiled kernel with the
-// drop rules resolved on the host (build_parity); the whole apply is timed
-// with 16, 32 and 64 angular rows per tiled item (best of three after a
-// warm-up) and the fastest plan is kept.
-static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
+// Builds the plan of one shape (FP64: with the host-resolved drop rules).
+template <typename T>
+static ApplyPlan* shape_plan(rtg_handle* h, const PlanShape& sh, const ParityTables* par) {
+    std::vector<int> cap(h->host.cols.size(), sh.rows);
+    return make_plan<T>(h, &cap, nullptr, kChunk64, par, sh.gcap, sh.split, sh.tc);
+}
+
+template <typename T>
+static const OpView<T>& view_of(const rtg_handle* h) {
+    if constexpr (sizeof(T) == 8)
+        return h->v64;
+    else
+        return h->v32;
+}
+
+// Times a plan: one warm-up, best of three whole applies (CUDA events); a
+// tensor-core plan whose waits gave up throws.
+template <typename T>
+static float time_plan(rtg_handle* h, ApplyPlan* p, const T* x, T* y, cudaEvent_t e0, cudaEvent_t e1,
+                       cudaStream_t s) {
+    set_plan_attributes<T>(p);
+    run_plan<T>(p, view_of<T>(h), h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+    float tt = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        RTG_CUDA(cudaEventRecord(e0, s));
+        run_plan<T>(p, view_of<T>(h), h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
+        RTG_CUDA(cudaEventRecord(e1, s));
+        RTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        tt = std::min(tt, ms);
+    }
+    if (p->ntc) {
+        int st = 0;
+        RTG_CUDA(cudaMemcpy(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st) throw RtgError{RTG_ERR_TIMEOUT, "scat_tc_kernel: a wait for the tensor cores gave up"};
+    }
+    return tt;
+}
+
+// Autotuner of the apply: every plan shape of the candidate list (rows per
+// item 16/32/64, one CTA per column or per item, one launch or one per
+// shared-memory class, FP32: with or without the tensor-core scattering) is
+// built and the whole apply timed; the fastest plan is kept.
+template <typename T>
+static ApplyPlan* tune_plan(rtg_handle* h, cudaStream_t s) {
+    constexpr bool f64 = sizeof(T) == 8;
     const int64_t N = h->host.ndof;
-    const int nc = (int)h->host.cols.size();
-    double *x = nullptr, *y = nullptr;
+    T *x = nullptr, *y = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ApplyPlan* best = nullptr;
     float tbest = 1e30f;
-    ParityTables* par = build_parity(h);
+    int ibest = -1;
+    ParityTables* par = f64 ? build_parity(h) : nullptr;
+    std::vector<TuneRecord> recs;
     auto release = [&] {
         if (x) cudaFree(x);
         if (y) cudaFree(y);
@@ -1340,64 +1682,106 @@ static ApplyPlan* tune_plan64(rtg_handle* h, cudaStream_t s) {
         if (e1) cudaEventDestroy(e1);
     };
     try {
-        RTG_CUDA(cudaMalloc(&x, sizeof(double) * std::max<int64_t>(N, 1)));
-        RTG_CUDA(cudaMalloc(&y, sizeof(double) * std::max<int64_t>(N, 1)));
-        RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * N, s));
+        RTG_CUDA(cudaMalloc(&x, sizeof(T) * std::max<int64_t>(N, 1)));
+        RTG_CUDA(cudaMalloc(&y, sizeof(T) * std::max<int64_t>(N, 1)));
+        RTG_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * N, s));
         RTG_CUDA(cudaEventCreate(&e0));
         RTG_CUDA(cudaEventCreate(&e1));
-        for (int rows : {16, 32, 64}) {
-            std::vector<int> cap(nc, rows);
-            ApplyPlan* p = make_plan<double>(h, &cap, nullptr, kChunk64, par);
+        std::vector<PlanShape> shapes;
+        for (int tc = 0; tc <= (f64 ? 0 : 1); ++tc)
+            for (int rows : {16, 32, 64})
+                for (int gcap : {0, 1})
+                    for (int split : {0, 1}) shapes.push_back(PlanShape{rows, gcap, split, tc});
+        for (const PlanShape& sh : shapes) {
+            ApplyPlan* p = shape_plan<T>(h, sh, par);
+            TuneRecord r{sh, 0, -1, p->ntiles, p->tg_begin[kSmemClasses], plan_launches(p)};
             float tt = 1e30f;
             try {
-                set_plan_attributes<double>(p);
-                run_plan<double>(p, h->v64, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
-                for (int rep = 0; rep < 3; ++rep) {
-                    RTG_CUDA(cudaEventRecord(e0, s));
-                    run_plan<double>(p, h->v64, h->v32, RTG_SYSTEM | RTG_MASK_ROWS, x, y, s);
-                    RTG_CUDA(cudaEventRecord(e1, s));
-                    RTG_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                    tt = std::min(tt, ms);
-                }
+                tt = time_plan<T>(h, p, x, y, e0, e1, s);
             } catch (...) {
                 free_plan(p);
                 throw;
             }
+            r.ns = (int)std::min(tt * 1e6f, 2.e9f);
+            recs.push_back(r);
             if (tt < tbest) {
                 free_plan(best);
                 best = p;
                 tbest = tt;
+                ibest = (int)recs.size() - 1;
             } else {
                 free_plan(p);
             }
         }
     } catch (...) {
         free_plan(best);
-        free_parity(par);
+        if (par) free_parity(par);
         release();
         throw;
     }
     release();
-    best->own_par = true;
+    recs[ibest].chosen = 1;
+    best->own_par = f64;
+    best->tuning = std::move(recs);
     return best;
+}
+
+// Replaces the apply plan of one precision by the plan of a given shape.
+template <typename T>
+static void force_shape(rtg_handle* h, const PlanShape& sh) {
+    constexpr bool f64 = sizeof(T) == 8;
+    ParityTables* par = f64 ? build_parity(h) : nullptr;
+    ApplyPlan* p = nullptr;
+    try {
+        p = shape_plan<T>(h, sh, par);
+    } catch (...) {
+        if (par) free_parity(par);
+        throw;
+    }
+    p->own_par = f64;
+    p->tuning.push_back(TuneRecord{sh, 1, -1, p->ntiles, p->tg_begin[kSmemClasses], plan_launches(p)});
+    set_plan_attributes<T>(p);
+    ApplyPlan*& slot = f64 ? h->plan64 : h->plan32;
+    free_plan(slot);
+    slot = p;
+}
+
+int apply_shape(rtg_handle* h, int prec, const int32_t* shape) {
+    if (!shape) {   // back to the autotuned plan on the next apply
+        ApplyPlan*& slot = prec == RTG_FP64 ? h->plan64 : h->plan32;
+        free_plan(slot);
+        slot = nullptr;
+        return 0;
+    }
+    const PlanShape sh{shape[0], shape[1], shape[2], shape[3]};
+    if (sh.rows < 1 || sh.rows > 1024 || sh.gcap < 0 || (sh.split != 0 && sh.split != 1) ||
+        (sh.tc != 0 && sh.tc != 1) || (prec == RTG_FP64 && sh.tc))
+        throw RtgError{RTG_ERR_ARG, "apply shape: rows in [1, 1024], gcap >= 0, split and tc 0 or 1 (tc: FP32 only)"};
+    if (prec == RTG_FP64)
+        force_shape<double>(h, sh);
+    else
+        force_shape<float>(h, sh);
+    return 0;
 }
 
 int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s) {
     if (!h->plan32) {
-        h->plan32 = tune_plan32(h, s);
+        h->plan32 = tune_plan<float>(h, s);
         set_plan_attributes<float>(h->plan32);
     }
     const auto& rec = h->plan32->tuning;
     const int n = (int)rec.size();
     for (int i = 0; i < std::min(n, cap_rows); ++i) {
-        int32_t* o = out + (size_t)i * (4 + kNumTuneCaps);
-        o[0] = rec[i].nx;
-        o[1] = rec[i].ny;
-        o[2] = rec[i].nthb;
-        o[3] = rec[i].cap;
-        for (int q = 0; q < kNumTuneCaps; ++q) o[4 + q] = rec[i].ns[q];
+        int32_t* o = out + (size_t)i * 9;
+        o[0] = rec[i].shape.rows;
+        o[1] = rec[i].shape.gcap;
+        o[2] = rec[i].shape.split;
+        o[3] = rec[i].shape.tc;
+        o[4] = rec[i].chosen;
+        o[5] = rec[i].ns;
+        o[6] = rec[i].items;
+        o[7] = rec[i].groups;
+        o[8] = rec[i].launches;
     }
     return n;
 }
@@ -1415,7 +1799,7 @@ void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, cons
     constexpr bool f64 = sizeof(T) == 8;
     ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
     if (!plan) {
-        plan = f64 ? tune_plan64(h, s) : tune_plan32(h, s);
+        plan = tune_plan<T>(h, s);
         set_plan_attributes<T>(plan);
     }
     run_plan<T>(plan, v, h->v32, flags, x, y, s);

@@ -133,6 +133,14 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
         a.sw = upload(h, t.sw);
         a.ang = upload(h, t.ang);
         a.W = upload(h, t.W);
+        std::vector<double> wt(t.W.size());
+        for (size_t sg = 0; sg + 1 < t.W_off.size(); ++sg) {
+            const int64_t o = t.W_off[sg];
+            const int n = t.sig_nth[sg];
+            for (int r = 0; r < n; ++r)
+                for (int c = 0; c < n; ++c) wt[o + (int64_t)c * n + r] = t.W[o + (int64_t)r * n + c];
+        }
+        a.WT = upload(h, wt);
         a.G = upload(h, t.G);
         a.lglw = upload(h, t.lglw);
         a.mort = upload(h, t.mort);
@@ -150,6 +158,7 @@ int rtg_create(const rtg_mesh_desc* mesh, const rtg_coeffs* coeffs, int device, 
         b.sw = upload(h, to_f32(t.sw));
         b.ang = upload(h, to_f32(t.ang));
         b.W = upload(h, to_f32(t.W));
+        b.WT = upload(h, to_f32(wt));
         b.G = upload(h, to_f32(t.G));
         b.lglw = upload(h, to_f32(t.lglw));
         b.mort = upload(h, to_f32(t.mort));
@@ -421,6 +430,20 @@ int rtg_apply_tuning(rtg_handle* h, int32_t* table, int cap_rows, int* nclasses,
     return guard("rtg_apply_tuning", [&] {
         if (!h || !nclasses || (cap_rows > 0 && !table)) throw RtgError{RTG_ERR_ARG, "null argument"};
         *nclasses = apply_tuning(h, table, cap_rows, (cudaStream_t)stream);
+    });
+}
+
+int rtg_apply_shape(rtg_handle* h, int prec, const int32_t* shape) {
+    return guard("rtg_apply_shape", [&] {
+        if (!h) throw RtgError{RTG_ERR_ARG, "null handle"};
+        if (prec != RTG_FP64 && prec != RTG_FP32) throw RtgError{RTG_ERR_ARG, "prec must be RTG_FP64 or RTG_FP32"};
+        // captured graphs hold the old plan's launches: finish the work in
+        // flight and drop them with the plan
+        RTG_CUDA(cudaSetDevice(h->device));
+        RTG_CUDA(cudaDeviceSynchronize());
+        free_workspace(h);
+        free_batch(h);
+        apply_shape(h, prec, shape);
     });
 }
 

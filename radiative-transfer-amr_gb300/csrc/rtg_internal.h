@@ -124,7 +124,28 @@ struct OpView {
     int32_t nelem;
     const int32_t* skip = nullptr;   // per column: nonzero = leave the column out (batched solve)
     const int* stop = nullptr;       // nonzero: the launch does nothing (a finished Krylov iteration)
+    const T* WT = nullptr;           // W transposed per signature: WT[c][R] = W[R][c]
 };
+
+#ifdef __CUDACC__
+// Asynchronous global -> shared copies (cp.async): many in flight per thread,
+// no registers held; cp_async_wait_all() before the barrier that publishes them.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+template <int kBytes>
+__device__ __forceinline__ void cp_async_small(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(kBytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// a / b for 0 <= a < 2^22, given rb = 1/b rounded to nearest float: (a + 1/2)/b
+// lies at least 1/(2b) from an integer and the two roundings move it by at
+// most (a + 1/2) 2^-23 / b < 1/(2b), so truncation gives the exact quotient.
+__device__ __forceinline__ int small_div(int a, float rb) { return (int)(((float)a + 0.5f) * rb); }
+#endif
 
 struct HostTables {
     std::vector<ColDev> cols;
@@ -198,6 +219,7 @@ void free_apply_plans(rtg_handle* h);
 // FP32 apply autotuning table (tunes on first use): rows of [nx, ny, nth_b,
 // cap, ns per candidate cap]; returns the number of degree classes
 int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s);
+int apply_shape(rtg_handle* h, int prec, const int32_t* shape);
 
 // Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
 template <typename T>

@@ -97,6 +97,7 @@ SIGNATURES = {
                                    C.c_void_p, C.c_void_p]),
     "rtg_sweep_info": (C.c_int, [C.c_void_p, i32p, i32p, i64p, C.c_void_p]),
     "rtg_apply_tuning": (C.c_int, [C.c_void_p, i32p, C.c_int, i32p, C.c_void_p]),
+    "rtg_apply_shape": (C.c_int, [C.c_void_p, C.c_int, i32p]),
     "rtg_error_angular_jump": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_error_spatial_jump": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_hp_steer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -1,6 +1,7 @@
-"""The FP32 apply autotuner: every degree class of columns is timed with each
-candidate item size and the fastest is kept; the tuned apply still matches the
-FP64 apply."""
+"""The apply autotuner: every plan shape of the candidate list (rows per work
+item, one CTA per column or per item, one launch or one per shared-memory
+class, scattering on CUDA cores or tensor cores) is timed and the fastest is
+kept; the tuned FP32 apply matches the FP64 apply."""
 import ctypes as C
 
 import numpy as np
@@ -8,7 +9,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = (16, 32, 64, 128)
+ROWS = (16, 32, 64)
 
 
 def test_tuning_table_and_tuned_apply():
@@ -18,18 +19,24 @@ def test_tuning_table_and_tuned_apply():
                             nref_ang=2, nref_spt=1)
     spec = W.gaussian_bump_problem(amp=3.0)
     ctx = DeviceContext(mesh, spec.kappa, spec.sigma, spec.Phi)
-    table = np.zeros((256, 8), dtype=np.int32)
-    ncls = C.c_int()
-    _lib.check(ctx.lib.rtg_apply_tuning(ctx.h, _lib.ptr(table, C.c_int32), 256, C.byref(ncls), None))
-    n = ncls.value
-    assert n >= 2
-    nx_ny_classes = {(c.ndofs[0], c.ndofs[1]) for c in mesh.cols.values()}
-    assert {(int(r[0]), int(r[1])) for r in table[:n]} == nx_ny_classes
-    for r in table[:n]:
-        cap = abs(int(r[3]))       # negative: the default plan won overall
-        assert cap in CANDIDATES
-        times = [t for t in r[4:] if t >= 0]
-        assert times and r[4 + CANDIDATES.index(cap)] <= min(times) / 0.97 + 1
+    table = np.zeros((256, 9), dtype=np.int32)
+    n = C.c_int()
+    _lib.check(ctx.lib.rtg_apply_tuning(ctx.h, _lib.ptr(table, C.c_int32), 256, C.byref(n), None))
+    rec = table[:n.value]
+    assert len(rec) == 24
+    assert {tuple(int(v) for v in r[:4]) for r in rec} == {(q, g, s, t) for q in ROWS for g in (0, 1)
+                                                           for s in (0, 1) for t in (0, 1)}
+    assert int(rec[:, 4].sum()) == 1
+    chosen = rec[rec[:, 4] == 1][0]
+    assert chosen[5] == rec[:, 5].min()
+    for r in rec:
+        assert r[5] > 0 and r[6] > 0 and r[7] > 0 and r[8] >= 1
+        if r[1] == 1:
+            assert r[7] == r[6]                       # one CTA per item
+        else:
+            assert r[7] <= min(len(mesh.cols), r[6])   # at most one CTA per column
+        if r[3] == 1:
+            assert r[8] >= 2                          # the tensor-core launch follows the tiled ones
     x = torch.randn(ctx.N, dtype=torch.float64, device=ctx.device)
     fl = _lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS
     y64 = ctx.apply(fl, x, prec=_lib.RTG_FP64)
