@@ -12,6 +12,7 @@
 // from global memory.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <map>
 #include <string>
 #include <tuple>
@@ -733,21 +734,26 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
 // (column, tile of 128 angular rows): D[m][ij] = sum_c W[R0+m][c] X[c][ij],
 // then y[R0+m, ij] += -(dx dy / 8) sw_ij D[m][ij] (the tiled kernel has
 // written the other terms; rows of inflow-boundary nodes stay masked).
-// Operands are staged in K-chunks of kTcK angular nodes, each value split
-// into TF32 hi + lo parts (hi = round-to-nearest TF32, lo = value - hi), and
-// D accumulates A_lo B_hi + A_hi B_lo + A_hi B_hi with tcgen05.mma
-// (kind::tf32, M = 128, N = nij padded to 16, K = 8 per instruction, one
-// issuing thread) in tensor memory; tcgen05.commit signals the chunk's
-// completion on an mbarrier before the operands are restaged.  Shared-memory
-// operands use the canonical K-major layout without swizzle: 8-row x 16-byte
-// core matrices, K-adjacent ones 128 bytes apart, 8-row groups
-// kTcK/4 * 128 bytes apart.
+// Each value is split into TF32 hi + lo parts (hi = round-to-nearest TF32,
+// lo = value - hi, exact in FP32) and D accumulates A_lo B_hi + A_hi B_lo +
+// A_hi B_hi with tcgen05.mma (kind::tf32, M = 128, N = nij padded to 16,
+// K = 8 per instruction, one issuing thread) in tensor memory.  The K axis
+// (the column's angular nodes) is walked in chunks of kTcK: W's hi/lo tile of
+// the chunk is built once per handle on the host in the shared-memory image
+// and arrives with one bulk copy (cp.async.bulk, completion counted on an
+// mbarrier); x is gathered with cp.async straight into its place and split
+// in place.  tcgen05.commit signals the chunk's MMAs on a second mbarrier
+// before the operands are restaged.  Operands use the canonical K-major
+// layout without swizzle: 8-row x 16-byte core matrices, K-adjacent ones 128
+// bytes apart, 8-row groups kTcK/4 * 128 bytes apart.
 constexpr int kTcThreads = 256;
 constexpr int kTcM = 128;
 constexpr int kTcK = 32;
+constexpr int kTcTileFloats = 2 * kTcM * kTcK;   // hi and lo of one W tile
 
 struct TcItem {
     int col, row0, rows, pad;
+    int64_t wtile;   // first W tile of the item's row tile (tiles of its chunks follow)
 };
 
 __host__ __device__ __forceinline__ int tc_np(int nij) { return nij <= 16 ? 16 : (nij + 15) & ~15; }
@@ -756,12 +762,14 @@ __host__ __device__ __forceinline__ int tc_tmem_cols(int np) {
     while (c < np) c <<= 1;
     return c;
 }
-// staged operands (floats): A hi/lo [kTcM x kTcK], B hi/lo [np x kTcK]
-__host__ __device__ __forceinline__ int tc_operand_floats(int np) { return 2 * (kTcM + np) * kTcK; }
 
-// float offset of (row, k) in the canonical layout
-__device__ __forceinline__ int tc_off(int row, int k) {
+// float offset of (row, k) in the canonical layout, and its inverse
+__host__ __device__ __forceinline__ int tc_off(int row, int k) {
     return (row >> 3) * (kTcK / 4) * 32 + (k >> 2) * 32 + (row & 7) * 4 + (k & 3);
+}
+__device__ __forceinline__ void tc_pos(int p, int& row, int& k) {
+    row = (p / ((kTcK / 4) * 32)) * 8 + ((p >> 2) & 7);
+    k = ((p >> 5) % (kTcK / 4)) * 4 + (p & 3);
 }
 
 __device__ __forceinline__ uint64_t tc_desc(const float* p) {
@@ -784,11 +792,24 @@ __device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint3
         "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
+// bounded wait for the completion of phase `parity` of an mbarrier
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t parity) {
+    uint32_t done = 0;
+    for (int spin = 0; spin < (1 << 22) && !done; ++spin)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(mb), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
 __global__ void __launch_bounds__(kTcThreads)
-scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items, const float* __restrict__ x,
-               float* __restrict__ y, int* __restrict__ status) {
+scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items, const float* __restrict__ wtc,
+               const float* __restrict__ x, float* __restrict__ y, int* __restrict__ status) {
     extern __shared__ __align__(128) float tsm[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar_mma, mbar_ld;
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     __shared__ int s_crow[kMaxCellsStaged + 1];
@@ -800,9 +821,8 @@ scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items
     const ApplyFlags fl = decode(flags);
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
     const int np = tc_np(nij), ncols = tc_tmem_cols(np);
-    float* Ah = tsm;
-    float* Al = Ah + kTcM * kTcK;
-    float* Bh = Al + kTcM * kTcK;
+    float* As = tsm;                       // W tile: hi [kTcM x kTcK] | lo
+    float* Bh = As + kTcTileFloats;        // x: hi [np x kTcK] | lo
     float* Bl = Bh + np * kTcK;
     int* rcell = reinterpret_cast<int*>(Bl + np * kTcK);   // [Nth] cell of each row
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -813,10 +833,12 @@ scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items
         if (k == ncell - 1) s_crow[ncell] = Nth;
         for (int r = 0; r < E.nth; ++r) rcell[E.row + r] = k;
     }
+    const uint32_t mb_mma = (uint32_t)__cvta_generic_to_shared(&mbar_mma);
+    const uint32_t mb_ld = (uint32_t)__cvta_generic_to_shared(&mbar_ld);
     if (threadIdx.x == 0) {
         s_abort = 0;
-        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb_mma) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb_ld) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -833,60 +855,71 @@ scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items
     // both K-major, N >> 3 at bit 17, M >> 4 at bit 24
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(np >> 3) << 17) |
                            ((uint32_t)(kTcM >> 4) << 24);
-    const float* W = v.W + v.W_off[C.sig];
     const float* xc = x + C.dof_off;
-    const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar);
+    const uint32_t as_addr = (uint32_t)__cvta_generic_to_shared(As);
     const int nchunk = (Nth + kTcK - 1) / kTcK;
     for (int ch = 0; ch < nchunk; ++ch) {
         const int c0 = ch * kTcK;
-        // A = W rows R0 .. R0+127, columns c0 .. c0+kTcK-1 (zero outside)
-        for (int t = threadIdx.x; t < kTcM * kTcK; t += blockDim.x) {
-            const int m = t / kTcK, k = t % kTcK, c = c0 + k;
-            const float w = (m < it.rows && c < Nth) ? __ldg(W + (int64_t)(it.row0 + m) * Nth + c) : 0.f;
-            const float h = tf32_hi(w);
-            Ah[tc_off(m, k)] = h;
-            Al[tc_off(m, k)] = w - h;
+        if (threadIdx.x == 0) {
+            // the chunk's W tile (hi and lo, in the shared-memory image) in one bulk copy
+            const float* src = wtc + (it.wtile + ch) * (int64_t)kTcTileFloats;
+            const uint32_t bytes = kTcTileFloats * sizeof(float);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb_ld), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    as_addr),
+                "l"(src), "r"(bytes), "r"(mb_ld)
+                : "memory");
         }
-        // B (N x K, K-major): B[ij][k] = x at angular row c0 + k, node ij
-        for (int t = threadIdx.x; t < np * kTcK; t += blockDim.x) {
-            const int n = t / kTcK, k = t % kTcK, c = c0 + k;
-            float xv = 0.f;
+        // x gathered into its place: consecutive threads fill consecutive
+        // shared-memory words (B[ij][k] = x at angular row c0 + k, node ij)
+        for (int p = threadIdx.x; p < np * kTcK; p += blockDim.x) {
+            int n, k;
+            tc_pos(p, n, k);
+            const int c = c0 + k;
             if (n < nij && c < Nth) {
                 const int kc = rcell[c];
                 const int nth = s_crow[kc + 1] - s_crow[kc];
-                xv = __ldg(xc + nij * s_crow[kc] + n * nth + (c - s_crow[kc]));
+                cp_async_small<4>(Bh + p, xc + nij * s_crow[kc] + n * nth + (c - s_crow[kc]));
+            } else {
+                Bh[p] = 0.f;
             }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        for (int p = threadIdx.x; p < np * kTcK; p += blockDim.x) {
+            const float xv = Bh[p];
             const float h = tf32_hi(xv);
-            Bh[tc_off(n, k)] = h;
-            Bl[tc_off(n, k)] = xv - h;
+            Bh[p] = h;
+            Bl[p] = xv - h;
         }
         // generic-proxy writes -> visible to the tensor cores
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!mbar_wait(mb_ld, (uint32_t)(ch & 1))) {
+                s_abort = 1;
+            } else {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const float* Ah = As;
+                const float* Al = As + kTcM * kTcK;
 #pragma unroll
-            for (int s = 0; s < kTcK / 8; ++s) {
-                const int o = 64 * s;   // two K-adjacent core matrices per K = 8
-                tc_mma(tmem, tc_desc(Al + o), tc_desc(Bh + o), idesc, ch > 0 || s > 0);
-                tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bl + o), idesc, 1);
-                tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bh + o), idesc, 1);
+                for (int s = 0; s < kTcK / 8; ++s) {
+                    const int o = 64 * s;   // two K-adjacent core matrices per K = 8
+                    tc_mma(tmem, tc_desc(Al + o), tc_desc(Bh + o), idesc, ch > 0 || s > 0);
+                    tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bl + o), idesc, 1);
+                    tc_mma(tmem, tc_desc(Ah + o), tc_desc(Bh + o), idesc, 1);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 mb_mma)
+                             : "memory");
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb)
-                         : "memory");
         }
+        __syncthreads();
+        if (s_abort) break;
         // the chunk's MMAs have read the operands before they are restaged
-        {
-            uint32_t done = 0;
-            for (int spin = 0; spin < (1 << 22) && !done; ++spin)
-                asm volatile(
-                    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                    "selp.u32 %0, 1, 0, p;\n\t}"
-                    : "=r"(done)
-                    : "r"(mb), "r"((uint32_t)(ch & 1))
-                    : "memory");
-            if (!done) s_abort = 1;
-        }
+        if (!mbar_wait(mb_mma, (uint32_t)(ch & 1))) s_abort = 1;
         __syncthreads();
         if (s_abort) break;
     }
@@ -932,8 +965,37 @@ scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items
     }
 }
 
+// W tiles of the tensor-core path for one signature: per row tile of 128 and
+// chunk of kTcK columns, hi then lo in the shared-memory image (zero outside
+// W); hi rounds to the nearest TF32 value (ties away from zero, the rounding
+// of cvt.rna), lo = w - hi.
+static void tc_w_tiles(const float* W, int n, std::vector<float>& out) {
+    const int mt = (n + kTcM - 1) / kTcM, kc = (n + kTcK - 1) / kTcK;
+    const size_t base = out.size();
+    out.resize(base + (size_t)mt * kc * kTcTileFloats, 0.f);
+    for (int t = 0; t < mt; ++t)
+        for (int ch = 0; ch < kc; ++ch) {
+            float* blk = out.data() + base + ((size_t)t * kc + ch) * kTcTileFloats;
+            for (int m = 0; m < kTcM; ++m)
+                for (int k = 0; k < kTcK; ++k) {
+                    const int R = t * kTcM + m, c = ch * kTcK + k;
+                    if (R >= n || c >= n) continue;
+                    const float w = W[(size_t)R * n + c];
+                    uint32_t b;
+                    std::memcpy(&b, &w, 4);
+                    uint32_t hb = b;
+                    if ((b & 0x7F800000u) != 0x7F800000u) hb = (b + 0x1000u) & 0xFFFFE000u;
+                    float hi;
+                    std::memcpy(&hi, &hb, 4);
+                    blk[tc_off(m, k)] = hi;
+                    blk[kTcM * kTcK + tc_off(m, k)] = w - hi;
+                }
+        }
+}
+
 static size_t tc_smem_bytes(int nij, int nth_col) {
-    return sizeof(float) * (size_t)tc_operand_floats(tc_np(nij)) + sizeof(int) * (size_t)nth_col + 16;
+    return sizeof(float) * ((size_t)kTcTileFloats + 2 * (size_t)tc_np(nij) * kTcK) + sizeof(int) * (size_t)nth_col +
+           16;
 }
 
 // ------------------------------------------------------------ global path
@@ -1115,6 +1177,7 @@ struct ApplyPlan {
     size_t tg_smem[kSmemClasses] = {};     // dynamic shared memory of launch q
     size_t tile_smem = 0;                  // the largest of them
     TcItem* d_tc = nullptr;                // tensor-core scattering CTAs
+    float* d_wtc = nullptr;                // their W tiles (hi/lo, shared-memory image)
     int ntc = 0;
     size_t tc_smem = 0;
     int* d_status = nullptr;               // RTG_ERR_TIMEOUT if a wait of scat_tc_kernel gave up
@@ -1339,6 +1402,8 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
     constexpr bool parity = sizeof(T) == 8;
     if (parity) tc = 0;
     std::vector<std::pair<int64_t, TcItem>> tcv;
+    std::map<int, int64_t> sig_tile;   // signature -> its first W tile
+    std::vector<float> wtiles;
     ApplyPlan* p = new ApplyPlan();
     std::vector<std::pair<int64_t, int4>> items[2];
     struct GroupRec {
@@ -1429,10 +1494,22 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                 if (cb + ibytes[q] > kSmemBudget) fits = false;
             if (tc && tc_smem_bytes(nij, C.nth_col) > kSmemBudget) fits = false;
             if (fits) {
-                if (tc)
+                if (tc) {
+                    auto its_ = sig_tile.find(C.sig);
+                    if (its_ == sig_tile.end()) {
+                        const int n = C.nth_col;
+                        std::vector<float> wf((size_t)n * n);
+                        for (size_t q = 0; q < wf.size(); ++q) wf[q] = (float)t.W[t.W_off[C.sig] + q];
+                        const int64_t first = (int64_t)(wtiles.size() / kTcTileFloats);
+                        tc_w_tiles(wf.data(), n, wtiles);
+                        its_ = sig_tile.emplace(C.sig, first).first;
+                    }
+                    const int kc = (C.nth_col + kTcK - 1) / kTcK;
                     for (int r0 = 0; r0 < C.nth_col; r0 += kTcM)
                         tcv.push_back({(int64_t)std::min(kTcM, C.nth_col - r0) * C.nth_col * tc_np(nij),
-                                       TcItem{ci, r0, std::min(kTcM, C.nth_col - r0), 0}});
+                                       TcItem{ci, r0, std::min(kTcM, C.nth_col - r0), 0,
+                                              its_->second + (int64_t)(r0 / kTcM) * kc}});
+                }
                 const size_t per = gcap > 0 ? (size_t)gcap : its.size();
                 for (size_t q0 = 0; q0 < its.size(); q0 += per) {
                     GroupRec g{0, 0, ci, {}, {}};
@@ -1540,6 +1617,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
     }
     p->ntc = (int)tci.size();
     p->d_tc = (TcItem*)up(tci.data(), sizeof(TcItem) * tci.size());
+    p->d_wtc = (float*)up(wtiles.data(), sizeof(float) * wtiles.size());
     p->d_status = (int*)up(nullptr, 0);
     RTG_CUDA(cudaMemset(p->d_status, 0, sizeof(int)));
     return p;
@@ -1607,7 +1685,8 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
     }
     if constexpr (!f64) {
         if (plan->ntc && (flags & (RTG_SYSTEM | RTG_SCAT))) {
-            scat_tc_kernel<<<plan->ntc, kTcThreads, plan->tc_smem, s>>>(v, flags, plan->d_tc, x, y, plan->d_status),
+            scat_tc_kernel<<<plan->ntc, kTcThreads, plan->tc_smem, s>>>(v, flags, plan->d_tc, plan->d_wtc, x, y,
+                                                                         plan->d_status),
                 count_launch();
             RTG_LAUNCHED("scat_tc_kernel");
         }
