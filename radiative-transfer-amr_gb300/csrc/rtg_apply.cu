@@ -390,8 +390,10 @@ __host__ __device__ __forceinline__ int col_int_words(int ncell, int nth_col) {
     return (4 * ncell + 2 + nth_col + 7) & ~7;
 }
 
-template <typename T, bool kParity>
-__global__ void __launch_bounds__(tiled_threads<T>(), sizeof(T) == 8 ? 3 : 2)
+// kProduct = false: the tensor-core kernel does the scattering product (FP32),
+// so the CTA neither stages W nor runs the product and fits three per SM
+template <typename T, bool kParity, bool kProduct = true>
+__global__ void __launch_bounds__(tiled_threads<T>(), sizeof(T) == 8 ? 3 : (kProduct ? 2 : 3))
 apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* __restrict__ groups,
                    const TileItem* __restrict__ items, const TileCpl* __restrict__ cpl_ent, const T* __restrict__ x,
                    T* __restrict__ y) {
@@ -405,8 +407,7 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
     if (v.skip && v.skip[ci]) return;
     const ColDev C = v.cols[ci];
     const ApplyFlags fl = decode(flags);
-    // FP32 groups flagged in bit 0 leave the scattering to the tensor-core kernel
-    const bool scat = fl.scat && !(grp.w & 1);
+    const bool scat = kProduct && fl.scat;
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
     const int nijp = (nij + 3) & ~3, Nthp = (Nth + 3) & ~3;
     T* Xs = smt;                                                  // [Nth][nijp]
@@ -1371,17 +1372,17 @@ static size_t tile_item_bytes(size_t vsize, int nx, int ny, int wcap, int M) {
 
 // Dynamic shared memory that lets q CTAs of the tiled kernel share an SM,
 // for q = 4, 3, 2, 1 (index 0..3).
-template <typename T>
+template <typename T, bool kProduct>
 static void smem_class_limits(size_t lim[kSmemClasses]) {
     int dev = 0, per_sm = 0, resv = 0;
     RTG_CUDA(cudaGetDevice(&dev));
     RTG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     RTG_CUDA(cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev));
     cudaFuncAttributes fa{};
-    RTG_CUDA(cudaFuncGetAttributes(&fa, apply_tiled_kernel<T, sizeof(T) == 8>));
+    RTG_CUDA(cudaFuncGetAttributes(&fa, apply_tiled_kernel<T, sizeof(T) == 8, kProduct>));
     // CTAs per SM that registers and threads allow
     int maxb = 0;
-    RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, apply_tiled_kernel<T, sizeof(T) == 8>,
+    RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, apply_tiled_kernel<T, sizeof(T) == 8, kProduct>,
                                                            tiled_threads<T>(), 0));
     for (int q = 0; q < kSmemClasses; ++q) {
         const int per = kSmemClasses - q;
@@ -1563,7 +1564,10 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
     // class, fewest CTAs per SM first (split), or all in one
     size_t lim[kSmemClasses];
     if (split && !groups.empty()) {
-        smem_class_limits<T>(lim);
+        if (tc)
+            smem_class_limits<T, false>(lim);
+        else
+            smem_class_limits<T, true>(lim);
     } else {
         for (int q = 0; q < kSmemClasses; ++q) lim[q] = kSmemBudget;
     }
@@ -1595,7 +1599,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
             ti.cpl_end = (int)ent.size();
             tv.push_back(ti);
         }
-        tg.push_back(make_int4(g.col, first, (int)tv.size(), tc ? 1 : 0));
+        tg.push_back(make_int4(g.col, first, (int)tv.size(), 0));
         const int slot = kSmemClasses - 1 - c;   // launch index
         counts[slot]++;
         p->tg_smem[slot] = std::max(p->tg_smem[slot], g.smem);
@@ -1634,7 +1638,12 @@ template <typename T>
 static void set_plan_attributes(const ApplyPlan* p) {
     constexpr bool f64 = sizeof(T) == 8;
     raise_smem_limit((const void*)apply_col_kernel<T, T, f64>, std::max(p->g[0].smem, p->g[1].smem));
-    if (p->ntiles) raise_smem_limit((const void*)apply_tiled_kernel<T, f64>, p->tile_smem);
+    if (p->ntiles) {
+        if (p->ntc)
+            raise_smem_limit((const void*)apply_tiled_kernel<T, f64, false>, p->tile_smem);
+        else
+            raise_smem_limit((const void*)apply_tiled_kernel<T, f64>, p->tile_smem);
+    }
     if (p->ntc) raise_smem_limit((const void*)scat_tc_kernel, p->tc_smem);
 }
 
@@ -1657,8 +1666,13 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
         for (int q = 0; q < kSmemClasses; ++q) {
             const int n = plan->tg_begin[q + 1] - plan->tg_begin[q];
             if (!n) continue;
-            apply_tiled_kernel<T, f64><<<n, tiled_threads<T>(), plan->tg_smem[q], s>>>(
-                v, tp, flags, plan->d_tgroups + plan->tg_begin[q], plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
+            const int4* grp = plan->d_tgroups + plan->tg_begin[q];
+            if (plan->ntc)
+                apply_tiled_kernel<T, f64, false><<<n, tiled_threads<T>(), plan->tg_smem[q], s>>>(
+                    v, tp, flags, grp, plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
+            else
+                apply_tiled_kernel<T, f64><<<n, tiled_threads<T>(), plan->tg_smem[q], s>>>(
+                    v, tp, flags, grp, plan->d_tiles, plan->d_tile_cpl, x, y), count_launch();
             const cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 cudaFuncAttributes fa{};
