@@ -187,8 +187,9 @@ int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y,
 /* Each precision's apply is autotuned on its first use: every plan shape of
  * the candidate list (16, 32 or 64 angular rows per work item; one CTA per
  * column or per work item; one launch, or one launch per shared-memory class
- * of the CTAs; FP32 also with the scattering product on the tensor cores) is
- * built and the whole apply timed; the fastest is kept.  This returns the
+ * of the CTAs; FP32 also, with one CTA per column and 32 or 64 rows, with the
+ * scattering product on the tensor cores) is built and the whole apply
+ * timed; the fastest is kept.  This returns the
  * FP32 table (host, cap_rows rows of 9 int32: rows per item, items per CTA
  * (0: the whole column), split launches (0/1), tensor-core scattering (0/1),
  * chosen (0/1), time in ns (-1: not timed), work items, CTAs, launches) and

@@ -302,15 +302,15 @@ struct TileItem {
 // term by term.
 struct TileCpl {
     int64_t base;             // neighbour line: x[base + jj*stride + a]
-    int rowloc, nth, toff, coff;
+    int nth, toff;            // the element's angular nodes; first value of its T block
     int m1, nt1, n0, face;
     int stride, es, et;
     float dc;
     int k, tested;
+    int pad[2];               // 64 bytes: copied in 16-byte pieces
 };
 constexpr int kMaxItemCpl = 96;
 static_assert(sizeof(TileCpl) == 64, "coupling records are copied in 16-byte pieces");
-constexpr int kMaxItemCells = 128;
 
 // Host-built tables of the FP64 tiled path.
 template <typename T>
@@ -1438,8 +1438,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                 while (k < ncell) {
                     const ElemDev& E = t.elems[C.elem_begin + k];
                     const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
-                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl ||
-                                  k - ti.cell_begin >= kMaxItemCells))
+                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl))
                         break;
                     M += nth;
                     ncp += nc;
@@ -1457,10 +1456,8 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                         const CplDev& cp = t.cpls[kk];
                         TileCpl tc{};
                         tc.base = g.base;
-                        tc.rowloc = E.row - ti.row0;
                         tc.nth = E.nth;
                         tc.toff = tsz;
-                        tc.coff = 0;
                         tc.m1 = g.m1;
                         tc.nt1 = g.nth1;
                         tc.face = cp.face;
@@ -1781,10 +1778,12 @@ static ApplyPlan* tune_plan(rtg_handle* h, cudaStream_t s) {
         RTG_CUDA(cudaEventCreate(&e0));
         RTG_CUDA(cudaEventCreate(&e1));
         std::vector<PlanShape> shapes;
-        for (int tc = 0; tc <= (f64 ? 0 : 1); ++tc)
-            for (int rows : {16, 32, 64})
-                for (int gcap : {0, 1})
-                    for (int split : {0, 1}) shapes.push_back(PlanShape{rows, gcap, split, tc});
+        for (int rows : {16, 32, 64})
+            for (int gcap : {0, 1})
+                for (int split : {0, 1}) shapes.push_back(PlanShape{rows, gcap, split, 0});
+        // tensor-core scattering (FP32): one CTA per column, items of 32 or 64 rows
+        if (!f64)
+            for (int rows : {32, 64}) shapes.push_back(PlanShape{rows, 0, 0, 1});
         for (const PlanShape& sh : shapes) {
             ApplyPlan* p = shape_plan<T>(h, sh, par);
             TuneRecord r{sh, 0, -1, p->ntiles, p->tg_begin[kSmemClasses], plan_launches(p)};

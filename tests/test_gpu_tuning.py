@@ -23,9 +23,9 @@ def test_tuning_table_and_tuned_apply():
     n = C.c_int()
     _lib.check(ctx.lib.rtg_apply_tuning(ctx.h, _lib.ptr(table, C.c_int32), 256, C.byref(n), None))
     rec = table[:n.value]
-    assert len(rec) == 24
-    assert {tuple(int(v) for v in r[:4]) for r in rec} == {(q, g, s, t) for q in ROWS for g in (0, 1)
-                                                           for s in (0, 1) for t in (0, 1)}
+    assert len(rec) == 14
+    assert {tuple(int(v) for v in r[:4]) for r in rec} == ({(q, g, s, 0) for q in ROWS for g in (0, 1)
+                                                            for s in (0, 1)} | {(32, 0, 0, 1), (64, 0, 0, 1)})
     assert int(rec[:, 4].sum()) == 1
     chosen = rec[rec[:, 4] == 1][0]
     assert chosen[5] == rec[:, 5].min()
