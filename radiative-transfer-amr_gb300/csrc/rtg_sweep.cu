@@ -236,7 +236,9 @@ __device__ __forceinline__ void st_relaxed(double* p, double x) {
 
 // Load a value of z that an upwind element publishes during this sweep:
 // spin (bounded) while it still holds the sentinel.  Returns false when the
-// wait gave up (timeout, or another CTA's status).
+// wait gave up (timeout, or another CTA's status).  The poll is one L2 round
+// trip per iteration: the status word and the clock are checked every 16th
+// iteration only, so they do not add a second round trip to each poll.
 template <typename T>
 __device__ __forceinline__ bool load_published(const T* p, T& out, int* status) {
     using U = typename Sentinel<T>::U;
@@ -247,17 +249,18 @@ __device__ __forceinline__ bool load_published(const T* p, T& out, int* status) 
         return true;
     }
     const long long t0 = clock64();
-    for (;;) {
-        __nanosleep(32);
+    for (unsigned it = 1;; ++it) {
         u = ld_relaxed(q);
         if (u != Sentinel<T>::bits) {
             out = from_bits<T>(u);
             return true;
         }
-        if (__ldcv(status) != 0) return false;
-        if (clock64() - t0 > kSpinLimitCycles) {
-            atomicExch(status, RTG_ERR_TIMEOUT);
-            return false;
+        if ((it & 15u) == 0u) {
+            if (__ldcv(status) != 0) return false;
+            if (clock64() - t0 > kSpinLimitCycles) {
+                atomicExch(status, RTG_ERR_TIMEOUT);
+                return false;
+            }
         }
     }
 }
