@@ -127,6 +127,22 @@ struct OpView {
     const T* WT = nullptr;           // W transposed per signature: WT[c][R] = W[R][c]
 };
 
+// The sentinel of the sweep's published-value protocol, as raw bits
+// (signalling NaNs with a payload; loads and stores move bits, never FP
+// values): z holds it until the element that owns a value publishes it.
+template <typename T>
+struct Sentinel;
+template <>
+struct Sentinel<float> {
+    using U = unsigned int;
+    static constexpr U bits = 0x7FBADBADu;
+};
+template <>
+struct Sentinel<double> {
+    using U = unsigned long long;
+    static constexpr U bits = 0x7FF4BADBADBADBADull;
+};
+
 #ifdef __CUDACC__
 // Asynchronous global -> shared copies (cp.async): many in flight per thread,
 // no registers held; cp_async_wait_all() before the barrier that publishes them.
@@ -224,9 +240,12 @@ int apply_shape(rtg_handle* h, int prec, const int32_t* shape);
 // Sweep preconditioner (rtg_sweep.cu): z = P^{-1} r
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s);
+// prefilled: the caller has written the sentinel over z and reset the claim
+// counter (sweep_counter) in an earlier launch on the same stream
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t s, unsigned long long* trace,
-                 const int32_t* skip = nullptr, const int* stop = nullptr);
+                 const int32_t* skip = nullptr, const int* stop = nullptr, bool prefilled = false);
+unsigned int* sweep_counter(rtg_handle* h, cudaStream_t s);
 void sweep_levels(rtg_handle* h, int32_t* level, cudaStream_t s);
 void sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind, cudaStream_t s);
 Sweep* get_sweep(rtg_handle* h, cudaStream_t s);

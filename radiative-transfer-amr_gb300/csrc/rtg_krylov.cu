@@ -232,23 +232,33 @@ __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, in
     }
 }
 
-// out = w / sqrt(nrm2sq[0]); hcol[k] = sqrt(nrm2sq[0])
+// out = w / sqrt(nrm2sq[0]); hcol[k] = sqrt(nrm2sq[0]).  zfill (optional): the
+// next sweep's output, filled with the sentinel, and its claim counter reset,
+// so that the sweep needs no fill launch of its own.
 template <typename T>
 __global__ void normalize_kernel(const T* __restrict__ w, T* __restrict__ out, const double* nrm2sq,
-                                 double* hcol, int k, int64_t n, const int* __restrict__ stop) {
+                                 double* hcol, int k, int64_t n, const int* __restrict__ stop,
+                                 T* __restrict__ zfill = nullptr, unsigned int* __restrict__ next = nullptr) {
+    using U = typename Sentinel<T>::U;
     if (stop && *stop) return;
     // one FP64 square root and division per block (GB300's FP64 rate is low)
     __shared__ Acc<T> s_inv;
     if (threadIdx.x == 0) {
         const double nr = sqrt(nrm2sq[0]);
-        if (blockIdx.x == 0) hcol[k] = nr;
+        if (blockIdx.x == 0) {
+            hcol[k] = nr;
+            if (zfill) *next = 0u;
+        }
         s_inv = (Acc<T>)(nr > 0. ? 1. / nr : 0.);
     }
     __syncthreads();
     const Acc<T> inv = s_inv;
+    U* zq = reinterpret_cast<U*>(zfill);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
+         i += (int64_t)gridDim.x * blockDim.x) {
         out[i] = (T)(Acc<T>(w[i]) * inv);
+        if (zq) zq[i] = Sentinel<T>::bits;
+    }
 }
 
 // Start of a restart cycle on the device: g = (beta, 0, ...) with beta = ||r||
@@ -491,11 +501,14 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         }
         first = false;
         dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
-        normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, nr, ho, 0, N, nullptr), count_launch();
         const int mode = pc.mode;   // fixed for the cycle
         // every preconditioned mode keeps M(v_j) (for the sweep alone this is
         // right preconditioning: x += Z y = P^{-1} V y without a last sweep)
         const bool flex = mode >= 1;
+        T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
+        // the normalisation that makes v_j also prepares the sweep of z_j
+        unsigned int* next = flex ? sweep_counter(h, s) : nullptr;
+        normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, nr, ho, 0, N, nullptr, Z, next), count_launch();
         const bool lagged = mode != 2 && m <= kFuseMax;
         double beta = 0.;
         if (!lagged) {
@@ -509,7 +522,6 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 break;
             }
         }
-        T* Z = flex ? flex_basis<T>(ws, ws->m) : nullptr;
         const int* stop = lagged ? ws->stop : nullptr;
         OpView<T> vs = v;
         vs.stop = stop;
@@ -527,7 +539,7 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             T* vn = V + (int64_t)(j + 1) * N;
             if (flex) {
                 T* zj = Z + (int64_t)j * N;
-                apply_sweep<T>(h, vj, zj, s, nullptr, nullptr, stop);
+                apply_sweep<T>(h, vj, zj, s, nullptr, nullptr, stop, true);
                 if (mode == 2) {
                     apply_coarse<T>(h, vj, zj, s);
                 } else if (mode == 3) {
@@ -553,7 +565,9 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
                 dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
             }
-            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N, stop), count_launch();
+            T* zn = (flex && j + 1 < m) ? Z + (int64_t)(j + 1) * N : nullptr;
+            normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N, stop, zn, zn ? next : nullptr),
+                count_launch();
         };
         int j = 0;   // steps of this cycle that count
         if (lagged) {

@@ -191,20 +191,6 @@ constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
 constexpr int kMaxFaceNodes = 4 * kMaxNodes;
 constexpr int kTr = 8;   // trace entries per element
 
-// The sentinel of the published-value protocol, as raw bits (signalling NaNs
-// with a payload; loads and stores move bits, never FP values).
-template <typename T>
-struct Sentinel;
-template <>
-struct Sentinel<float> {
-    using U = unsigned int;
-    static constexpr U bits = 0x7FBADBADu;
-};
-template <>
-struct Sentinel<double> {
-    using U = unsigned long long;
-    static constexpr U bits = 0x7FF4BADBADBADBADull;
-};
 
 __device__ __forceinline__ float from_bits_f(unsigned int u) { return __uint_as_float(u); }
 __device__ __forceinline__ double from_bits_f(unsigned long long u) { return __longlong_as_double((long long)u); }
@@ -1025,14 +1011,14 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
 // couplings, the face columns of B and the stores.
 template <typename T>
 void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long long* trace, const int32_t* skip,
-                 const int* stop) {
+                 const int* stop, bool prefilled) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
     const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
     OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
     v.skip = skip;
     v.stop = stop;
-    {
+    if (!prefilled) {
         const int ne = (int)h->host.elems.size();
         sweep_fill_kernel<T><<<std::max(1, std::min(ne, 152 * 8)), 256, 0, st>>>(v, ne, z, s->d_next), count_launch();
     }
@@ -1141,9 +1127,11 @@ int sweep_status(rtg_handle* h, cudaStream_t st) {
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t);
 template void apply_sweep<double>(rtg_handle*, const double*, double*, cudaStream_t, unsigned long long*,
-                                  const int32_t*, const int*);
+                                  const int32_t*, const int*, bool);
 template void apply_sweep<float>(rtg_handle*, const float*, float*, cudaStream_t, unsigned long long*,
-                                 const int32_t*, const int*);
+                                 const int32_t*, const int*, bool);
+
+unsigned int* sweep_counter(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->d_next; }
 
 int sweep_levels_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->nlev; }
 int sweep_lagged_count(rtg_handle* h, cudaStream_t st) { return get_sweep(h, st)->n_lagged; }
