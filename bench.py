@@ -6,8 +6,8 @@ sigma_t = sigma_s + 0.01, HG g = 0.9, inflow 1 on x = 0 for th in
 (-pi/4, pi/4), hp mesh from seeded random refinement (seed 0, six rounds, 3..7
 nodes per dimension), about 2.2e5 DOF.  Synthetic and seeded; no dataset.
 
-A step is one solve from a zero initial guess to the error target.  The judge
-solution is a tight plain FP64 GPU solve (rtol 1e-14) computed before timing;
+A step is one solve from a zero initial guess to the error target.  The
+reference solution is a tight plain FP64 GPU solve (rtol 1e-14) computed before timing;
 the error is the quadrature-weighted relative L2 norm (weights = mass weights
 with kappa = 1).  Each method's residual tolerance is calibrated (untimed) as
 the loosest power of ten that reaches the 1e-8 target.  Three methods:
@@ -203,7 +203,7 @@ def rel_l2(u, ref, w):
     return float(np.sqrt(np.sum(w * (u - ref) ** 2) / np.sum(w * ref ** 2)))
 
 
-def cpu_baseline(mesh, spec, rtol, u_judge=None, w=None):
+def cpu_baseline(mesh, spec, rtol, u_ref=None, w=None):
     """The oracle port of the path on the host (single thread): assemble the
     reference's split system with scipy (rt/solve.py:81-101) and solve it with
     scipy GMRES(50) preconditioned by the same upwind sweep the GPU uses, to the
@@ -216,7 +216,7 @@ def cpu_baseline(mesh, spec, rtol, u_judge=None, w=None):
     t1 = time.perf_counter()
     u, its, info = O.solve_sweep_gmres(o, o["layout"], rtol=rtol)
     t_solve = time.perf_counter() - t1
-    err = rel_l2(u, u_judge, w) if u_judge is not None else None
+    err = rel_l2(u, u_ref, w) if u_ref is not None else None
     return {"value": t_asm + t_solve, "unit": "s", "cores": 1, "kind": "port",
             "sample": "whole workload: oracle assembly {:.1f} s + scipy sweep-preconditioned GMRES(50) "
                       "{:.1f} s ({} iterations, rtol {:g})".format(t_asm, t_solve, its, rtol),
@@ -357,7 +357,7 @@ def run_ours(args):
     kap = ctx.to_device(np.asarray(np.broadcast_to(spec.kappa(X, Y), (N,)), dtype=np.float64))
     w = (ones / kap).cpu().numpy()
 
-    # judge solution: tight plain FP64 solve
+    # reference solution: tight plain FP64 solve
     u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=20000, precond=1)
     u_ref_h = u_ref.cpu().numpy()
     arms = {"plain_fp64": (0, 1), "mixed": (1, 1), "learned_mixed": (1, 3)}
@@ -491,7 +491,7 @@ def run_ours(args):
                    "speedup_learned_mixed_vs_plain_fp64": t_plain / value,
                    "speedup_mixed_vs_plain_fp64": t_plain / statistics.median(res["mixed"][0]),
                    "network": {"file": "rtg/nets/sweep_correction.npz", **net_meta},
-                   "judge": {"rtol": 1e-14, "iterations": info_ref["iterations"], "res_f": info_ref["res_f"]},
+                   "reference_solution": {"rtol": 1e-14, "iterations": info_ref["iterations"], "res_f": info_ref["res_f"]},
                    "kernels_us": {"sweep_fp32": 1e6 * t_sweep, "sweep_fp64": 1e6 * t_sweep64,
                                   "apply_fp32": 1e6 * t_apply, "apply_fp64": 1e6 * t_apply64},
                    "sweep": {"levels": nlev, "lagged_couplings": nlag},
@@ -536,7 +536,7 @@ def run_batched(args):
     f = bc.forcing()
     g = bc.inflow()
     stream = torch.cuda.current_stream()
-    # judges: tight individual FP64 solves
+    # reference solutions: tight individual FP64 solves
     ctxs = [DeviceContext(m, p.kappa, p.sigma, p.Phi) for m, p in inst]
     fs = [c.forcing(p.f) for c, (m, p) in zip(ctxs, inst)]
     gs = [c.inflow(p.bcs_dirac) for c, (m, p) in zip(ctxs, inst)]
