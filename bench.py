@@ -223,6 +223,36 @@ def cpu_baseline(mesh, spec, rtol, u_ref=None, w=None):
             "rel_l2_err": err}
 
 
+def _batch_instance_cpu(job):
+    """One instance of the batched workload through the oracle port (worker of
+    cpu_baseline_batch): rebuilt from its seed, assembled, solved with the
+    sweep-preconditioned GMRES(50) to rtol."""
+    seed, rtol = job
+    from rtg import workloads as W
+    from oracle import rt_oracle as O
+    mesh, spec = W.batch_instance(seed)
+    o = O.assemble(mesh, spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    _, its, info = O.solve_sweep_gmres(o, o["layout"], rtol=rtol)
+    return its, info
+
+
+def cpu_baseline_batch(seeds, rtol, n_total, workers=None):
+    """The batched workload's CPU baseline on all host cores: a bounded sample
+    of its instances (seeds) through the oracle port in a spawn process pool,
+    wall time scaled to n_total instances."""
+    import multiprocessing as mp
+    workers = workers or max(1, min(len(seeds), os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_batch_instance_cpu, [(s, rtol) for s in seeds])
+    wall = time.perf_counter() - t0
+    return {"value": wall * n_total / len(seeds), "unit": "s", "cores": workers, "kind": "port",
+            "sample": "{} of {} instances (seeds {}..{}), oracle assembly + scipy sweep-preconditioned GMRES(50) "
+                      "to rtol {:g} in a {}-process pool, wall {:.1f} s (pool start-up included) scaled by {:.0f}"
+                      .format(len(seeds), n_total, seeds[0], seeds[-1], rtol, workers, wall, n_total / len(seeds)),
+            "iterations_max": max(r[0] for r in res), "all_converged": all(r[1] == 0 for r in res)}
+
+
 def _events(stream):
     import torch
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -582,7 +612,7 @@ def run_batched(args):
         return None
     value = statistics.median(times)
     ndof = int(bc.N)
-    return {"metric": METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+    out = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32-inner/f64-outer", "data": "synthetic (256 seeded instances)",
             "config": {"workload": "256 independent instances (batch_instance seeds 1000..1255)", "ndof": ndof,
@@ -593,6 +623,10 @@ def run_batched(args):
                     "note": "inputs resident; the batched entry point takes device vectors"},
             "gpu_launches": int(n_launch),
             "clocks": clk.summary()}
+    if not args.no_cpu:
+        # all host cores, a bounded sample of 32 of the 256 instances
+        out["cpu_baseline"] = cpu_baseline_batch(list(range(1000, 1032)), rtol, nb)
+    return out
 
 
 def run_large(args):
