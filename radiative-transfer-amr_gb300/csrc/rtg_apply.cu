@@ -1,15 +1,20 @@
 // Matrix-free application of the RT DG operator and the small vector kernels
-// around it.  One CTA per spatial column: the column's DOFs are contiguous
-// (cell-major, then i, j, a), the scattering block is dense over the column's
-// angular nodes and diagonal in the spatial node (i, j), and the streaming
-// terms stay inside one element, so a column is the natural unit of work.
+// around it.  A spatial column is the unit of work: the column's DOFs are
+// contiguous (cell-major, then i, j, a), the scattering block is dense over
+// the column's angular nodes and diagonal in the spatial node (i, j), and the
+// streaming terms stay inside one element.
 //
-// Fast path (apply_col_kernel): the column's input is staged in shared memory
-// transposed to [angular row R][spatial node ij] (and, when it fits, the
-// column's angular scattering matrix W), then every output DOF is computed
-// from shared memory and written in global order (coalesced).  Columns too
-// large for shared memory use apply_global_kernel, which reads its operands
-// from global memory.
+// Main path (apply_tiled_kernel): one CTA per column (or per work item of a
+// column) stages the column's input in shared memory transposed to
+// [angular row R][spatial node ij] and walks the column's items: scattering
+// product from shared memory in 4 x 4 register tiles, factorised inflow face
+// fluxes, then every output DOF written in global order.  FP32 plans may hand
+// the scattering product to scat_tc_kernel (tcgen05 tensor cores, TF32 hi/lo
+// split).  The plan shape (rows per item, items per CTA, launches per
+// shared-memory class, tensor cores or not) is autotuned per handle
+// (tune_plan).  Columns too large for the tiled path use apply_col_kernel
+// (per-output chunks from shared memory) or apply_global_kernel (operands
+// read from global memory).
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
