@@ -576,7 +576,10 @@ def boundary_conditions_vector(mesh, bcs_dirac, L=None):
             nth = cell.ndofs[0]
             tb, _ = lg_nodes(nth)
             thf = push(cell.pos[0], cell.pos[1], tb)
-            if any(d is not None for d in dirac):
+            # the reference branches on any(dirac), i.e. on truthiness: a
+            # Dirac coordinate of 0.0 alone does not select the point-source
+            # branch (rt/boundary_conditions_vector.py:142)
+            if any(dirac):
                 lims = [(x0, x1, tx, xx), (y0, y1, ty, yy), (cell.pos[0], cell.pos[1], tb, thf)]
                 inside = [True, True, True]
                 fac, crd = [], []

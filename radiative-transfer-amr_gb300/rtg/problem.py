@@ -137,7 +137,10 @@ class DeviceContext:
     def inflow(self, bcs_dirac):
         """Inflow data at every node (rt/boundary_conditions_vector.py:101-207)."""
         bcs, dirac = bcs_dirac
-        if not any(d is not None for d in dirac):
+        # any(dirac), as the reference tests it: truthiness, so a lone Dirac
+        # coordinate of 0.0 keeps the sampled branch
+        # (rt/boundary_conditions_vector.py:142)
+        if not any(dirac):
             return self.to_device(self.node_values(bcs))
         return self.to_device(_dirac_inflow(self.layout, bcs, dirac))
 

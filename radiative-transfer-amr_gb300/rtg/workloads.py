@@ -117,6 +117,18 @@ def smooth_variable_problem(Lx=1., Ly=1., g=0.6):
                          meta={"g": g})
 
 
+def point_inflow_problem(Lx=3., Ly=2., g=0.6, dirac=(0.0, None, 0.3)):
+    """The smooth variable coefficients with a point-source inflow: ``dirac``
+    gives the Dirac position in x, y and/or th (None where the data are
+    sampled), the reference's ``bcs_dirac = [bcs, dirac]`` form
+    (rt/boundary_conditions_vector.py:142-196).  The default puts the source
+    at x = 0 in th = 0.3; a coordinate of 0.0 is a real position inside the
+    branch even though the reference's any(dirac) test alone would skip it."""
+    base = smooth_variable_problem(Lx, Ly, g)
+    return RTProblemSpec("point_inflow", base.kappa, base.sigma, base.Phi, base.f,
+                         [base.bcs_dirac[0], list(dirac)], meta={"g": g, "dirac": list(dirac)})
+
+
 def gaussian_bump_problem(Lx=3., Ly=2., amp=0.9, width=0.15, xc=1.5, yc=1.0, g=0.9):
     """Single adaptive problem: sigma_s = amp exp(-r^2 / (2 width^2)) centred at
     (xc, yc), sigma_t = sigma_s + 0.01, isotropic inflow 1 on x = 0 for
@@ -349,13 +361,33 @@ def disc_edge_mesh(mesh_cls=Mesh, seed=0, rounds=3, n0=4, nth0=4, n_max=9, nref_
 
 
 def config5_mesh(mesh_cls=Mesh, seed=0, scale=1.0):
-    """Large two-strong-scatterer mesh on [0,2]^2: refinement concentrated at
-    the disc edges, up to 9 nodes per dimension (degree 8), about 1e7 DOF at
-    scale 1 (``scale`` < 1 gives the same recipe with fewer refinement rounds
-    for tests)."""
-    rounds = 5 if scale >= 1.0 else max(1, int(round(5 * scale)))
+    """Large two-strong-scatterer mesh on [0,2]^2: 16x16 columns of 5x5 nodes
+    and 32 angular cells of 5 nodes to start, then four rounds of seeded
+    refinement concentrated at the disc edges (h or p in space up to 9 nodes
+    per dimension, h up to 64 cells or p up to 9 nodes in angle), about 8e6 DOF
+    at scale 1 (``scale`` < 1 gives the same recipe with fewer rounds).
+
+    The angular start is set by the phase function, not by cost: with HG
+    g = 0.95 the discrete kernel (dth/2 w) Phi of a coarse angular mesh is far
+    from conservative (largest eigenvalue of D^1/2 Phi D^1/2, D = diag(dth/2 w):
+    2.18 on 8 cells of 5 nodes, 1.20 on 16, 1.01 on 32), so inside the discs
+    (sigma_s / sigma_t = 0.998) a coarse mesh makes kappa - sigma lambda
+    strongly negative: a multiplying medium whose linear system GMRES cannot
+    solve in any reasonable number of iterations.  On 32 cells the system is
+    within 0.4 of that limit and sweep-preconditioned GMRES converges in about
+    40-50 iterations."""
+    rounds = 4 if scale >= 1.0 else max(0, int(round(4 * scale)))
     return disc_edge_mesh(mesh_cls=mesh_cls, seed=seed, rounds=rounds, n0=5, nth0=5, n_max=9,
-                          nref_ang=3, nref_spt=4, ang_prob=0.42)
+                          nref_ang=5, nref_spt=4, ang_prob=0.1, max_ang_lv=6)
+
+
+def config5_small_mesh(mesh_cls=Mesh, seed=0, rounds=1):
+    """The two-strong-scatterer recipe at a size the CPU oracle assembles in
+    seconds: 8x8 columns of 2x2 nodes, the same 32 angular cells of 5 nodes,
+    ``rounds`` rounds of disc-edge refinement up to 4 nodes per dimension
+    (about 6.7e4 DOF at one round)."""
+    return disc_edge_mesh(mesh_cls=mesh_cls, seed=seed, rounds=rounds, n0=2, nth0=5, n_max=4,
+                          nref_ang=5, nref_spt=3, ang_prob=0.1, max_ang_lv=6)
 
 
 def batch_instance(seed, mesh_cls=Mesh, max_cols=64, max_cells=16, n_range=(2, 8)):

@@ -2,7 +2,9 @@
 
 Run in a container where the reference source tree is present:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout> [--only CASE]
+
+(``--ref`` may also come from the environment variable RT_REFERENCE.)
 
 The reference's ``src/rt`` modules import petsc4py and mpi4py at module level.
 Neither is installed here, so two stub modules stand in (identity ``bcast``,
@@ -18,7 +20,13 @@ rt/solve.py:81-101 is solved directly with ``scipy.sparse.linalg.spsolve``.
 
 Each case writes ``tests/golden/<case>.npz`` holding the reference mesh (JSON
 of dg/mesh/to_file.py), the blocks M (diagonal), S, MS, IC, BC (CSR), the
-vectors f, g, the interior mask and the direct solution u.
+vectors f, g, the interior mask and the direct solution u.  The ``dirac`` case
+takes its inflow data through the reference's point-source branch
+(rt/boundary_conditions_vector.py:142-196).
+
+``projection_file.npz`` holds what the reference's ``Projection.to_file``
+writes (dg/projection/to_file.py:10-19) for a sampled function on the
+``small_random`` mesh: the mesh JSON text and the raw float64 bytes.
 """
 
 import argparse
@@ -173,14 +181,42 @@ def cases():
         "quad_none": (W.quadrant_free_mesh, lambda: W.smooth_variable_problem(1., 1., g=0.3)),
         "periodic": (W.periodic_mesh, lambda: W.smooth_variable_problem(1., 1., g=0.5)),
         "small_random": (W.small_random_mesh, lambda: W.gaussian_bump_problem()),
+        "dirac": (W.small_random_mesh, lambda: W.point_inflow_problem()),
     }
+
+
+def projection_func(x, y, th):
+    """The function sampled for the projection-file fixture."""
+    return np.sin(1.3 * x + 0.4) * np.cos(0.7 * y) * (1. + 0.25 * np.sin(2. * th)) + 0.1 * th
+
+
+def write_projection_fixture(RefMesh):
+    from rtg import workloads as W
+    from dg.projection import Projection as RefProjection
+    mesh = W.small_random_mesh(mesh_cls=RefMesh)
+    proj = RefProjection(mesh, projection_func)
+    pf = os.path.join(HERE, "_proj_tmp.npy")
+    mf = os.path.join(HERE, "_proj_mesh_tmp.json")
+    proj.to_file(pf, write_mesh=True, mesh_file_path=mf)
+    with open(pf, "rb") as fh:
+        raw = fh.read()
+    with open(mf) as fh:
+        mesh_json = fh.read()
+    os.remove(pf)
+    os.remove(mf)
+    np.savez_compressed(os.path.join(HERE, "projection_file.npz"), mesh_json=np.array(mesh_json),
+                        proj_bytes=np.frombuffer(raw, dtype=np.uint8))
+    print("projection_file  {} bytes of float64".format(len(raw)))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("RT_REFERENCE"),
+                    help="root of the reference checkout (its src/ is imported)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("--ref (or RT_REFERENCE) must name the reference checkout")
     install_stubs()
     sys.path.insert(0, os.path.join(args.ref, "src"))
     from dg.mesh import Mesh as RefMesh
@@ -194,7 +230,10 @@ def main():
         q["lgl_w_%d" % n] = np.asarray(wx, dtype=np.float64)
         q["lg_x_%d" % n] = np.asarray(tb, dtype=np.float64)
         q["lg_w_%d" % n] = np.asarray(wt, dtype=np.float64)
-    np.savez_compressed(os.path.join(HERE, "quadrature.npz"), **q)
+    if args.only is None:
+        np.savez_compressed(os.path.join(HERE, "quadrature.npz"), **q)
+    if args.only in (None, "projection_file"):
+        write_projection_fixture(RefMesh)
 
     for name, (mesh_fn, prob_fn) in cases().items():
         if args.only and name != args.only:

@@ -2,7 +2,9 @@
 
 Run in a container where the reference source tree is present:
 
-    python tests/golden/make_golden_amr.py [--ref /root/reference]
+    python tests/golden/make_golden_amr.py --ref <reference checkout>
+
+(``--ref`` may also come from the environment variable RT_REFERENCE.)
 
 For every golden case of make_golden.py (which must have been run first: its
 ``<case>.npz`` holds the reference mesh and the reference direct solution u),
@@ -89,8 +91,11 @@ def record(ind, prefix, cells_too):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("RT_REFERENCE"),
+                    help="root of the reference checkout (its src/ is imported)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("--ref (or RT_REFERENCE) must name the reference checkout")
     MG.install_stubs()
     src = os.path.join(args.ref, "src")
     sys.path.insert(0, src)

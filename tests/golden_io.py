@@ -6,7 +6,7 @@ import numpy as np
 import scipy.sparse as sp
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["cfg1", "hp_hanging", "quad_none", "periodic", "small_random"]
+CASES = ["cfg1", "hp_hanging", "quad_none", "periodic", "small_random", "dirac"]
 
 
 def load(case):
@@ -30,4 +30,5 @@ def problem(case):
         "quad_none": (W.quadrant_free_mesh, lambda: W.smooth_variable_problem(1., 1., g=0.3)),
         "periodic": (W.periodic_mesh, lambda: W.smooth_variable_problem(1., 1., g=0.5)),
         "small_random": (W.small_random_mesh, lambda: W.gaussian_bump_problem()),
+        "dirac": (W.small_random_mesh, lambda: W.point_inflow_problem()),
     }[case]

@@ -30,7 +30,7 @@ def _rel(a, b):
     return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
 
 
-@pytest.mark.parametrize("name", ["adaptive_2e5", "two_disc_9e6"])
+@pytest.mark.parametrize("name", ["adaptive_2e5", "two_disc_8e6"])
 def test_apply_linearity_and_precisions(name):
     import torch
     from rtg import _lib
