@@ -250,6 +250,17 @@ int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u,
               const rtg_solve_opts* opts, rtg_solve_info* info,
               double* hist, int hist_cap, void* stream);
 
+/* The triangular factor R of the last Arnoldi cycle of the handle's last
+ * rtg_solve (its Hessenberg after the Givens rotations), written column-major
+ * into R (host, n*n doubles, zeros below the diagonal); *n = the cycle's
+ * steps (0: no cycle ran; R untouched).  R may be NULL to query n.  The
+ * singular values of R are those of the cycle's (n+1) x n Hessenberg: the
+ * estimates of the preconditioned operator's extreme singular values that the
+ * reference reads after its solve (rt/solve.py:110-115,
+ * ksp.computeExtremeSingularValues(), which PETSc's GMRES computes from the
+ * same factor).  For method 1 the cycle is the last FP32 inner cycle. */
+int rtg_solve_hessenberg(rtg_handle* h, double* R, int cap, int32_t* n, void* stream);
+
 /* Batched solve of independent problems held by one handle.  The handle's mesh
  * is the concatenation of nbatch instances' meshes (no couplings between
  * them; each instance with its own coefficients), instance b owning DOFs

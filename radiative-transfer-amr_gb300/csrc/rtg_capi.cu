@@ -513,4 +513,13 @@ int rtg_solve(rtg_handle* h, const double* f, const double* g, double* u, const 
     return rc != RTG_OK ? rc : inner;
 }
 
+int rtg_solve_hessenberg(rtg_handle* h, double* R, int cap, int32_t* n, void* stream) {
+    return guard("rtg_solve_hessenberg", [&] {
+        if (!h || !n) throw RtgError{RTG_ERR_ARG, "null argument"};
+        int nn = 0;
+        last_hessenberg(h, R, cap, &nn, (cudaStream_t)stream);
+        *n = nn;
+    });
+}
+
 }  // extern "C"

@@ -296,6 +296,7 @@ void apply_coarse(rtg_handle* h, const T* v, T* z, cudaStream_t s);
 int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_solve_opts* o,
           rtg_solve_info* info, double* hist, int hist_cap, cudaStream_t s);
 void free_workspace(rtg_handle* h);
+int last_hessenberg(rtg_handle* h, double* R, int cap, int* n, cudaStream_t s);
 
 // Batched solve (rtg_batch.cu)
 int solve_batched(rtg_handle* h, int nb, const int64_t* inst_off, const double* f, const double* g, double* u,

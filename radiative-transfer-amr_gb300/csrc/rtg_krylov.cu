@@ -352,6 +352,12 @@ struct Workspace {
     bool warm[2] = {false, false};    // a cycle ran uncaptured (plans and launch shapes exist), per precision
     double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
+    // the last Arnoldi cycle with at least one step: its j x j triangular
+    // factor R (Givens-reduced Hessenberg, columns m + 1 apart) is in dH
+    // (device loop) or in hlast (host loop)
+    int last_j = 0;
+    bool last_on_device = false;
+    std::vector<double> hlast;
     std::vector<void*> allocs;
 };
 
@@ -654,6 +660,8 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             total += j;
             res.res = ws->hslot[2 * (j - 1)];
             res.converged = res.res <= tol_abs;
+            ws->last_j = j;
+            ws->last_on_device = true;
             // y = H^{-1} g on the device (into hdev, where the combine reads it)
             ysolve_kernel<<<1, 1, 0, s>>>(ws->dH, m + 1, ws->dg, j, ws->hdev), count_launch();
         } else {
@@ -694,6 +702,11 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 }
             }
         }
+        if (!lagged && j > 0) {
+            ws->last_j = j;
+            ws->last_on_device = false;
+            ws->hlast.assign(H.begin(), H.begin() + (size_t)j * (m + 1));
+        }
         if (!lagged) {
             // y = H^{-1} g (upper triangular j x j)
             for (int q = j - 1; q >= 0; --q) {
@@ -721,6 +734,26 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
 }
 
 }  // namespace
+
+int last_hessenberg(rtg_handle* h, double* R, int cap, int* n, cudaStream_t s) {
+    Workspace* ws = h->ws;
+    const int j = ws ? ws->last_j : 0;
+    *n = j;
+    if (!R || j == 0) return RTG_OK;
+    if (cap < j * j) throw RtgError{RTG_ERR_SIZE, "R needs n*n doubles"};
+    const int ld = ws->m + 1;
+    std::vector<double> raw((size_t)j * ld);
+    if (ws->last_on_device) {
+        RTG_CUDA(cudaMemcpyAsync(raw.data(), ws->dH, sizeof(double) * raw.size(), cudaMemcpyDeviceToHost, s));
+        RTG_CUDA(cudaStreamSynchronize(s));
+    } else {
+        std::copy(ws->hlast.begin(), ws->hlast.begin() + raw.size(), raw.begin());
+    }
+    // column-major j x j, the rows below the diagonal zero
+    for (int c = 0; c < j; ++c)
+        for (int q = 0; q < j; ++q) R[(size_t)c * j + q] = q <= c ? raw[(size_t)c * ld + q] : 0.;
+    return RTG_OK;
+}
 
 void free_workspace(rtg_handle* h) {
     if (!h->ws) return;

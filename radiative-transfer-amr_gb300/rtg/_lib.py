@@ -91,6 +91,7 @@ SIGNATURES = {
     "rtg_weight_forcing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtg_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(SolveOpts),
                             C.POINTER(SolveInfo), f64p, C.c_int, C.c_void_p]),
+    "rtg_solve_hessenberg": (C.c_int, [C.c_void_p, f64p, C.c_int, i32p, C.c_void_p]),
     "rtg_solve_batched": (C.c_int, [C.c_void_p, C.c_int, i64p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.c_void_p]),
     "rtg_dots_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,

@@ -161,6 +161,21 @@ class DeviceContext:
         out["history"] = hist[:info.hist_len].copy()
         return u, out
 
+    def extreme_singular_values(self, stream=None):
+        """[emax, emin] of the last solve's last Arnoldi cycle: the singular
+        values of its Givens-reduced Hessenberg factor, the estimate the
+        reference reads with ksp.computeExtremeSingularValues()
+        (rt/solve.py:110-115).  [1, 1] when no cycle ran, as PETSc returns."""
+        n = C.c_int32()
+        _lib.check(self.lib.rtg_solve_hessenberg(self.h, None, 0, C.byref(n), _stream_ptr(stream)))
+        if n.value == 0:
+            return [1.0, 1.0]
+        R = np.zeros(n.value * n.value)
+        _lib.check(self.lib.rtg_solve_hessenberg(self.h, _lib.ptr(R, C.c_double), R.size, C.byref(n),
+                                                 _stream_ptr(stream)))
+        sv = np.linalg.svd(R.reshape(n.value, n.value).T, compute_uv=False)
+        return [float(sv[0]), float(sv[-1])]
+
 
 def _dirac_inflow(lay, bcs, dirac):
     """Point-source inflow data (rt/boundary_conditions_vector.py:142-196),
@@ -293,6 +308,11 @@ class DeviceOperator:
         return sp.csr_matrix(D)
 
 
+# pc_type names (the reference's PETSc names and this library's own) -> the
+# preconditioner rtg_solve applies (Problem.solve documents the mapping)
+PC_TYPES = {"none": 0, "sweep": 1, "bjacobi": 1, "kaczmarz": 1, "dsa": 2, "learned": 3}
+
+
 class Problem:
     """rt.Problem with the GPU behind it (rt/class_Problem.py:11-32)."""
 
@@ -341,10 +361,24 @@ class Problem:
     def solve(self, mesh, **kwargs):
         """Solve the split system (rt/solve.py:21-181).
 
-        kwargs: ksp_type "gmres" (FP64 GMRES, the plain method) or "mixed"
-        (FP32 GMRES inside FP64 iterative refinement); restart (50), max_it
-        (5000), rtol (1e-12; the reference asks PETSc for 1e-15), atol (0),
-        x0 ("forcing" = start from f_I as the reference does, or "zero")."""
+        kwargs: ksp_type "gmres" or "fgmres" (FP64 GMRES, the plain method;
+        with a fixed preconditioner right-preconditioned GMRES and FGMRES build
+        the same iterates) or "mixed" (FP32 GMRES inside FP64 iterative
+        refinement); pc_type (below); restart (50), max_it (5000), rtol (1e-12;
+        the reference asks PETSc for 1e-15), atol (0), x0 ("forcing" = start
+        from f_I as the reference does, or "zero").
+
+        pc_type: the reference hands its string to PETSc (rt/solve.py:93-95);
+        here every name maps to a GPU preconditioner.  "bjacobi" (PETSc's
+        default, block Jacobi over ranks) and "kaczmarz" (row projections in
+        row order, the two-scatterer inputs' choice,
+        experiments/two-strong-scatterers/input.json:4-7) both map to the
+        upwind transport sweep: for the upwind DG operator the sweep is the
+        block Gauss-Seidel pass in flow order, the transport form of a
+        row-action sweep, and the algebraic methods themselves (a dense
+        row-by-row pass) have no GPU form worth shipping.  "none", "sweep",
+        "dsa" (with the column diffusion correction) and "learned" (with the
+        learned correction) name the others."""
         opts = {"verbose": False, "ksp_type": "gmres", "pc_type": "sweep", "restart": 50,
                 "max_it": 5000, "rtol": 1e-12, "atol": 0., "x0": "forcing",
                 "inner_rtol": 1e-6}
@@ -359,7 +393,7 @@ class Problem:
         # PETSc's "bjacobi" default maps to the sweep, the GPU preconditioner;
         # "dsa" adds the column diffusion correction, "learned" the learned
         # correction (a network set with rtg.learned.set_params)
-        precond = {"none": 0, "sweep": 1, "bjacobi": 1, "dsa": 2, "learned": 3}.get(opts["pc_type"])
+        precond = PC_TYPES.get(opts["pc_type"])
         if precond is None:
             raise ValueError("unsupported pc_type {}".format(opts["pc_type"]))
         x0 = f_dev if opts["x0"] == "forcing" else None
@@ -381,7 +415,7 @@ class Problem:
                             "max_it": int(opts["max_it"])}
         matrix_info = {"ndof": ctx.N, "ndof_interior": int(ctx.info["ndof_interior"]),
                        "ncoupling": int(ctx.info["ncoupling"]),
-                       "extreme_singular_values": [None, None],
+                       "extreme_singular_values": ctx.extreme_singular_values(),
                        "solve_seconds": time.perf_counter() - t0,
                        "fp64_applies": int(info["fp64_applies"]),
                        "fp32_applies": int(info["fp32_applies"])}

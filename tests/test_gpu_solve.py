@@ -125,3 +125,48 @@ def test_indefinite_case_reports_nonconvergence():
     assert conv["converged_reason"] < 0
     assert conv["iteration_number"] <= 500
     assert np.all(np.isfinite(uh.to_vector()))
+
+
+def test_reference_solver_parameters(case):
+    """The two-scatterer inputs' solver choice (ksp_type fgmres, pc_type
+    kaczmarz: experiments/two-strong-scatterers/input.json:4-7) goes through,
+    and matrix_info carries the extreme singular values (rt/solve.py:110-115)."""
+    name, g, mesh, prob, _ = case
+    uh, conv, minfo = prob.solve(mesh, ksp_type="fgmres", pc_type="kaczmarz", rtol=1e-13, max_it=20000)
+    assert conv["converged_reason"] > 0
+    assert _rel(uh.to_vector(), g["u"]) < 1e-10
+    emax, emin = minfo["extreme_singular_values"]
+    assert np.isfinite(emax) and np.isfinite(emin) and emax >= emin > 0.
+
+
+def test_extreme_singular_values_match_arnoldi():
+    """Unpreconditioned FP64 GMRES stopped after one 20-step cycle: the
+    singular values of the cycle's Hessenberg from the library equal those of
+    a numpy Arnoldi (CGS2) on the reference-assembled A_II from r0 = b."""
+    from rtg import Problem
+    g = golden_io.load("cfg1")
+    mesh_fn, prob_fn = golden_io.problem("cfg1")
+    spec = prob_fn()
+    mesh = mesh_fn()
+    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    _, conv, minfo = prob.solve(mesh, pc_type="none", restart=30, max_it=20, rtol=1e-30, x0="zero")
+    assert conv["iteration_number"] == 20
+    mask = g["mask"]
+    I, B = np.nonzero(mask)[0], np.nonzero(~mask)[0]
+    A = g["A"].tocsr()
+    AII = A[I][:, I]
+    b = g["f"][I] - A[I][:, B] @ g["g"][B]
+    V = [b / np.linalg.norm(b)]
+    H = np.zeros((21, 20))
+    for j in range(20):
+        w = AII @ V[j]
+        for _ in range(2):
+            h = np.array([v @ w for v in V])
+            w = w - sum(hq * v for hq, v in zip(h, V))
+            H[:j + 1, j] += h
+        H[j + 1, j] = np.linalg.norm(w)
+        V.append(w / H[j + 1, j])
+    sv = np.linalg.svd(H, compute_uv=False)
+    emax, emin = minfo["extreme_singular_values"]
+    assert abs(emax - sv[0]) < 1e-10 * sv[0], (emax, sv[0])
+    assert abs(emin - sv[-1]) < 1e-8 * sv[0], (emin, sv[-1])
