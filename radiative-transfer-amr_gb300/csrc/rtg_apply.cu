@@ -16,6 +16,7 @@
 // (per-output chunks from shared memory) or apply_global_kernel (operands
 // read from global memory).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -318,15 +319,24 @@ constexpr int kMaxItemCpl = 96;
 static_assert(sizeof(TileCpl) == 64, "coupling records are copied in 16-byte pieces");
 
 // Host-built tables of the FP64 tiled path.
+// Scattering classes of a spatial node (the reference keeps an off-diagonal
+// term of the (M - S) block iff |value| > 1e-14):
+//   0 no term kept, 1 every term kept, 2 the terms with |W| >= the node's
+//   threshold kept (cross-cell terms included), 3 own-cell terms only
+//   (|wx wy sigma| <= 1e-14), each tested on its own.
+// Classes 1 and 2 read the product; its tiles mask W by the threshold.
 template <typename T>
 struct TileParity {
-    const uint8_t* scls = nullptr;   // per spatial node: 0 no, 1 every, 2 some off-diagonal scattering term kept
+    const uint8_t* scls = nullptr;   // per spatial node: class 0..3
     const T* mortc = nullptr;        // cleaned dcoeff*Es and Et per coupling
     const float* mortf = nullptr;    // FP32 copy of the mortars (tested couplings)
-    const float* Wf = nullptr;       // FP32 copy of W (mixed nodes without a mask)
-    const uint64_t* colfull = nullptr;   // per column: bit ij set when node ij is of class 1 (ij < 64)
-    const int64_t* kbase = nullptr;      // per spatial node of class 2: first keep mask, or -1
-    const uint64_t* kmask = nullptr;     // per (class-2 node, row R): bit c set when term (R, c) is kept
+    const float* Wf = nullptr;       // FP32 copy of W (class-3 nodes)
+    const uint64_t* colfull = nullptr;   // per column: bit ij set when node ij reads the product (ij < 64)
+    // per spatial node: bits of the smallest |W| whose term is kept (class 1:
+    // 0, every term; classes 0 and 3: +inf bits, none).  For w >= 0 the order
+    // of the IEEE bit patterns is the order of the values, so the test is an
+    // integer compare.
+    const uint64_t* thr = nullptr;
 };
 
 // f-th node on the boundary of an nx x ny node grid, going around (j = 0 row,
@@ -543,15 +553,37 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+                if constexpr (kParity) {
+                    // the drop rule per (row, node): keep w iff bits(|w|) >= thr(node)
+                    // (integer compares: no work for the slow FP64 pipe)
+                    unsigned long long tb[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        tb[j] = j0 + j < nij ? par.thr[C.node_off + j0 + j] : 0x7FF0000000000000ull;
+#pragma unroll 2
+                    for (int c = 0; c < Nth; ++c) {
+                        T wv[4], xa[4];
+                        load4(WsT + c * Mp + m0, wv);
+                        load4(Xs + c * nijp + j0, xa);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const unsigned long long wb =
+                                (unsigned long long)__double_as_longlong((double)wv[i]) & 0x7FFFFFFFFFFFFFFFull;
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(wb >= tb[j] ? wv[i] : T(0), xa[j], acc[i][j]);
+                        }
+                    }
+                } else {
 #pragma unroll 4
-                for (int c = 0; c < Nth; ++c) {
-                    T wv[4], xa[4];
-                    load4(WsT + c * Mp + m0, wv);
-                    load4(Xs + c * nijp + j0, xa);
+                    for (int c = 0; c < Nth; ++c) {
+                        T wv[4], xa[4];
+                        load4(WsT + c * Mp + m0, wv);
+                        load4(Xs + c * nijp + j0, xa);
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                        for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
+                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
+                    }
                 }
 #pragma unroll
                 for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
@@ -669,19 +701,10 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                     const T cw = dxdy8 * swv;
                     const int cls = par.scls[node];
                     T s = T(0);
-                    if (cls == 1) {
+                    if (cls == 1 || cls == 2) {
                         s = Ys[m * nijp + ij];
-                    } else if (cls == 2 && par.kbase[node] >= 0) {
-                        // some terms kept, some dropped: the host's keep mask of row R
-                        uint64_t mk = par.kmask[par.kbase[node] + R];
-                        const T* wr = Wg + (int64_t)R * Nth;
-                        while (mk) {
-                            const int c = __ffsll((long long)mk) - 1;
-                            mk &= mk - 1;
-                            s = fma(wr[c], Xs[c * nijp + ij], s);
-                        }
-                    } else if (cls == 2) {
-                        // some terms kept, some dropped: test each one
+                    } else if (cls == 3) {
+                        // own-cell terms only, some kept: test each one
                         const bool skip_cross = !(tabs(swv) > small);
                         const int c0 = skip_cross ? crow[k] : 0;
                         const int c1 = skip_cross ? crow[k] + nth : Nth;
@@ -1163,11 +1186,10 @@ struct ParityTables {
     uint8_t* d_scls = nullptr;
     double* d_mortc = nullptr;
     uint64_t* d_colfull = nullptr;
-    int64_t* d_kbase = nullptr;
-    uint64_t* d_kmask = nullptr;
+    uint64_t* d_thr = nullptr;
     std::vector<int> esc, etc;     // per coupling: offsets of dcoeff*Es and Et in the cleaned table
     std::vector<char> tested;      // per coupling: summed term by term
-    int64_t nodes[3] = {0, 0, 0};  // nodes per scattering class
+    int64_t nodes[4] = {0, 0, 0, 0};   // nodes per scattering class
     int64_t ntested = 0;
 };
 
@@ -1198,8 +1220,7 @@ static void free_parity(const ParityTables* pt) {
     cudaFree(pt->d_scls);
     cudaFree(pt->d_mortc);
     cudaFree(pt->d_colfull);
-    cudaFree(pt->d_kbase);
-    cudaFree(pt->d_kmask);
+    cudaFree(pt->d_thr);
     delete pt;
 }
 
@@ -1208,7 +1229,9 @@ static void free_parity(const ParityTables* pt) {
 //  * node class: |fl(cw w)| grows with |w|, so the smallest and largest
 //    nonzero off-diagonal |W| entries decide whether every, no or some
 //    scattering term of the node is kept (cross-cell terms only where
-//    |wx wy sigma| > 1e-14, rt/preconditioner_matrix.py:450-495);
+//    |wx wy sigma| > 1e-14, rt/preconditioner_matrix.py:450-495); for "some"
+//    the kept terms are exactly those with |w| >= t, t the smallest double
+//    with |fl(cw t)| > 1e-14, found by stepping from 1e-14 / |cw|;
 //  * coupling: the terms dropped by |dcoeff Es Et| <= 1e-15 must be exactly
 //    the products with a set of Es entries or a set of Et entries; then those
 //    entries are zeroed in copies of dcoeff*Es and Et
@@ -1217,8 +1240,9 @@ static ParityTables* build_parity(const rtg_handle* h) {
     const HostTables& t = h->host;
     ParityTables* pt = new ParityTables();
     std::vector<uint8_t> scls((size_t)std::max(t.nnodes, 1), 0);
-    std::vector<uint64_t> colfull(t.cols.size(), 0), kmask;
-    std::vector<int64_t> kbase((size_t)std::max(t.nnodes, 1), -1);
+    constexpr uint64_t kInfBits = 0x7FF0000000000000ull;
+    std::vector<uint64_t> colfull(t.cols.size(), 0);
+    std::vector<uint64_t> thr((size_t)std::max(t.nnodes, 1), kInfBits);
     for (int ci = 0; ci < (int)t.cols.size(); ++ci) {
         const ColDev& C = t.cols[ci];
         const int Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
@@ -1247,7 +1271,7 @@ static ParityTables* build_parity(const rtg_handle* h) {
                 // cross-cell terms left out: the per-term loop when any own-cell term is kept
                 bool any = false;
                 for (int k = 0; k < ncell; ++k) any |= std::fabs(cw * cmax[k]) > kSmall;
-                cls = any ? 2 : 0;
+                cls = any ? 3 : 0;
             } else if (wmax == 0.) {
                 cls = 0;
             } else if (std::fabs(cw * wmin) > kSmall) {
@@ -1259,19 +1283,21 @@ static ParityTables* build_parity(const rtg_handle* h) {
             }
             scls[C.node_off + ij] = cls;
             ++pt->nodes[cls];
-            if (cls == 1 && ij < 64) colfull[ci] |= 1ull << ij;
-            if (cls == 2 && Nth <= 64) {
-                // the exact FP64 test of every term of every row of the node
-                const bool cross = std::fabs(swv) > kSmall;
-                kbase[C.node_off + ij] = (int64_t)kmask.size();
-                for (int R = 0; R < Nth; ++R) {
-                    uint64_t mk = 0;
-                    for (int c = 0; c < Nth; ++c) {
-                        if (c == R || (!cross && rcell[c] != rcell[R])) continue;
-                        if (std::fabs(cw * W[(int64_t)R * Nth + c]) > kSmall) mk |= 1ull << c;
-                    }
-                    kmask.push_back(mk);
-                }
+            if ((cls == 1 || cls == 2) && ij < 64) colfull[ci] |= 1ull << ij;
+            if (cls == 1) {
+                thr[C.node_off + ij] = 0;
+            } else if (cls == 2) {
+                // smallest t >= 0 with |fl(cw t)| > 1e-14 (fl(|cw| t) is monotone in t)
+                const double acw = std::fabs(cw);
+                double tt = kSmall / acw;
+                auto kept = [&](double w) { return std::fabs(cw * w) > kSmall; };
+                for (int it = 0; it < 64 && kept(tt); ++it) tt = std::nextafter(tt, 0.);
+                for (int it = 0; it < 64 && !kept(tt); ++it) tt = std::nextafter(tt, HUGE_VAL);
+                if (!kept(tt) || kept(std::nextafter(tt, 0.)))
+                    throw RtgError{RTG_ERR_ARG, "drop-rule threshold not found"};
+                uint64_t bits;
+                std::memcpy(&bits, &tt, sizeof(bits));
+                thr[C.node_off + ij] = bits;
             }
         }
     }
@@ -1345,11 +1371,8 @@ static ParityTables* build_parity(const rtg_handle* h) {
         if (!colfull.empty())
             RTG_CUDA(cudaMemcpy(pt->d_colfull, colfull.data(), sizeof(uint64_t) * colfull.size(),
                                 cudaMemcpyHostToDevice));
-        RTG_CUDA(cudaMalloc(&pt->d_kbase, sizeof(int64_t) * kbase.size()));
-        RTG_CUDA(cudaMemcpy(pt->d_kbase, kbase.data(), sizeof(int64_t) * kbase.size(), cudaMemcpyHostToDevice));
-        RTG_CUDA(cudaMalloc(&pt->d_kmask, sizeof(uint64_t) * std::max<size_t>(kmask.size(), 1)));
-        if (!kmask.empty())
-            RTG_CUDA(cudaMemcpy(pt->d_kmask, kmask.data(), sizeof(uint64_t) * kmask.size(), cudaMemcpyHostToDevice));
+        RTG_CUDA(cudaMalloc(&pt->d_thr, sizeof(uint64_t) * thr.size()));
+        RTG_CUDA(cudaMemcpy(pt->d_thr, thr.data(), sizeof(uint64_t) * thr.size(), cudaMemcpyHostToDevice));
         RTG_CUDA(cudaMalloc(&pt->d_mortc, sizeof(double) * std::max<size_t>(mortc.size(), 1)));
         if (!mortc.empty())
             RTG_CUDA(cudaMemcpy(pt->d_mortc, mortc.data(), sizeof(double) * mortc.size(), cudaMemcpyHostToDevice));
@@ -1429,73 +1452,81 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         const int nij = C.nx * C.ny;
         const int rows_cap = cap ? (*cap)[ci] : kTileRows;
         if ((!parity || par) && ncell <= kMaxCellsStaged) {
-            // split the column into items of whole cells
+            // split the column into items of whole cells; halve the rows per
+            // item (down to 4) until every item fits next to the staged column
             std::vector<TileItem> its;
             std::vector<size_t> ibytes;
             std::vector<int64_t> icost;
-            bool fits = true;
-            int k = 0;
             std::vector<std::vector<TileCpl>> ents;
-            while (k < ncell && fits) {
-                TileItem ti{ci, k, k, t.elems[C.elem_begin + k].row, 0, 0, 0, 0, 0, 0, 0,
-                            t.elems[C.elem_begin + k].cpl_begin};
-                int M = 0, ncp = 0;
-                while (k < ncell) {
-                    const ElemDev& E = t.elems[C.elem_begin + k];
-                    const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
-                    if (M > 0 && (M + nth > rows_cap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl))
-                        break;
-                    M += nth;
-                    ncp += nc;
-                    ++k;
-                }
-                ti.cell_end = k;
-                ti.M = M;
-                if (ncp > kMaxItemCpl) fits = false;
-                std::vector<TileCpl> en;
-                int tsz = 0;
-                for (int q = ti.cell_begin; q < ti.cell_end; ++q) {
-                    const ElemDev& E = t.elems[C.elem_begin + q];
-                    for (int kk = E.cpl_begin; kk < E.cpl_end; ++kk) {
-                        const CplGeo& g = t.cgeo[kk];
-                        const CplDev& cp = t.cpls[kk];
-                        TileCpl tc{};
-                        tc.base = g.base;
-                        tc.nth = E.nth;
-                        tc.toff = tsz;
-                        tc.m1 = g.m1;
-                        tc.nt1 = g.nth1;
-                        tc.face = cp.face;
-                        tc.n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
-                        tc.stride = g.stride;
-                        tc.es = parity ? par->esc[kk] : cp.es;
-                        tc.et = parity ? par->etc[kk] : cp.et;
-                        tc.dc = (float)t.cplc[kk];
-                        tc.k = kk;
-                        tc.tested = parity ? par->tested[kk] : 0;
-                        en.push_back(tc);
-                        tsz += g.m1 * E.nth;
-                    }
-                }
-                ti.ttot = tsz;
-                ti.ctot = boundary_nodes(C.nx, C.ny) * M;
-                const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
-                // Fy and Ys are read and written four values at a time: keep
-                // every region a multiple of 4 values from the aligned base
-                ti.tsz = (tsz + 3) & ~3;
-                // without the scattering product (tensor-core path) the region holds T and Fy only
-                ti.wcap = tc ? ti.tsz + Mp * nijp : std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
-                if ((ti.wcap & 3) || (ti.tsz & 3) || (nijp & 3))
-                    throw RtgError{RTG_ERR_ARG, "tiled apply: unaligned shared-memory region"};
-                ibytes.push_back(tile_item_bytes(sizeof(T), C.nx, C.ny, ti.wcap, M));
-                icost.push_back((int64_t)M * nij * (C.nth_col + C.nx + C.ny) + C.ndof);
-                ents.push_back(std::move(en));
-                its.push_back(ti);
-            }
             const size_t cb = tile_col_bytes(sizeof(T), C.nth_col, C.nx, C.ny, ncell);
-            for (size_t q = 0; q < its.size() && fits; ++q)
-                if (cb + ibytes[q] > kSmemBudget) fits = false;
-            if (tc && tc_smem_bytes(nij, C.nth_col) > kSmemBudget) fits = false;
+            bool fits = false;
+            for (int rcap = rows_cap; rcap > 0 && !fits; rcap = rcap > 4 ? rcap / 2 : 0) {
+                its.clear();
+                ibytes.clear();
+                icost.clear();
+                ents.clear();
+                fits = true;
+                int k = 0;
+                while (k < ncell && fits) {
+                    TileItem ti{ci, k, k, t.elems[C.elem_begin + k].row, 0, 0, 0, 0, 0, 0, 0,
+                                t.elems[C.elem_begin + k].cpl_begin};
+                    int M = 0, ncp = 0;
+                    while (k < ncell) {
+                        const ElemDev& E = t.elems[C.elem_begin + k];
+                        const int nth = E.nth, nc = E.cpl_end - E.cpl_begin;
+                        if (M > 0 && (M + nth > rcap || (M + nth) * nij > kTileOut || ncp + nc > kMaxItemCpl))
+                            break;
+                        M += nth;
+                        ncp += nc;
+                        ++k;
+                    }
+                    ti.cell_end = k;
+                    ti.M = M;
+                    if (ncp > kMaxItemCpl) fits = false;
+                    std::vector<TileCpl> en;
+                    int tsz = 0;
+                    for (int q = ti.cell_begin; q < ti.cell_end; ++q) {
+                        const ElemDev& E = t.elems[C.elem_begin + q];
+                        for (int kk = E.cpl_begin; kk < E.cpl_end; ++kk) {
+                            const CplGeo& g = t.cgeo[kk];
+                            const CplDev& cp = t.cpls[kk];
+                            TileCpl tc{};
+                            tc.base = g.base;
+                            tc.nth = E.nth;
+                            tc.toff = tsz;
+                            tc.m1 = g.m1;
+                            tc.nt1 = g.nth1;
+                            tc.face = cp.face;
+                            tc.n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+                            tc.stride = g.stride;
+                            tc.es = parity ? par->esc[kk] : cp.es;
+                            tc.et = parity ? par->etc[kk] : cp.et;
+                            tc.dc = (float)t.cplc[kk];
+                            tc.k = kk;
+                            tc.tested = parity ? par->tested[kk] : 0;
+                            en.push_back(tc);
+                            tsz += g.m1 * E.nth;
+                        }
+                    }
+                    ti.ttot = tsz;
+                    ti.ctot = boundary_nodes(C.nx, C.ny) * M;
+                    const int Mp = (M + 3) & ~3, nijp = (nij + 3) & ~3;
+                    // Fy and Ys are read and written four values at a time: keep
+                    // every region a multiple of 4 values from the aligned base
+                    ti.tsz = (tsz + 3) & ~3;
+                    // without the scattering product (tensor-core path) the region holds T and Fy only
+                    ti.wcap = tc ? ti.tsz + Mp * nijp : std::max(C.nth_col * Mp, ti.tsz + Mp * nijp);
+                    if ((ti.wcap & 3) || (ti.tsz & 3) || (nijp & 3))
+                        throw RtgError{RTG_ERR_ARG, "tiled apply: unaligned shared-memory region"};
+                    ibytes.push_back(tile_item_bytes(sizeof(T), C.nx, C.ny, ti.wcap, M));
+                    icost.push_back((int64_t)M * nij * (C.nth_col + C.nx + C.ny) + C.ndof);
+                    ents.push_back(std::move(en));
+                    its.push_back(ti);
+                }
+                for (size_t q = 0; q < its.size() && fits; ++q)
+                    if (cb + ibytes[q] > kSmemBudget) fits = false;
+                if (tc && tc_smem_bytes(nij, C.nth_col) > kSmemBudget) fits = false;
+            }
             if (fits) {
                 if (tc) {
                     auto its_ = sig_tile.find(C.sig);
@@ -1662,8 +1693,7 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
             tp.mortf = v32.mort;
             tp.Wf = v32.W;
             tp.colfull = plan->par->d_colfull;
-            tp.kbase = plan->par->d_kbase;
-            tp.kmask = plan->par->d_kmask;
+            tp.thr = plan->par->d_thr;
         }
         for (int q = 0; q < kSmemClasses; ++q) {
             const int n = plan->tg_begin[q + 1] - plan->tg_begin[q];
