@@ -540,53 +540,71 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
         cp_async_wait_all();
         __syncthreads();
         if (scat) {
-            const int tm = Mp / 4, tn = nijp / 4;
+            const int tm = Mp / 4, tn = nijp / 4, ntile = tm * tn;
             const float rtn = __frcp_rn((float)tn);
-            // FP64: only nodes of class 1 read the product
+            // FP64: nodes of classes 1 and 2 read the product
             const uint64_t fullm = kParity ? (nij <= 64 ? par.colfull[ci] : ~0ull) : ~0ull;
-            for (int tile = threadIdx.x; tile < tm * tn; tile += blockDim.x) {
-                const int tq = small_div(tile, rtn);
+            // ks adjacent lanes share a 4 x 4 tile, each summing every ks-th
+            // angular node, so that items of a few rows still keep every warp
+            // busy; the partial sums meet through shuffles (ks = 1, 2, 4 or 8,
+            // the same for the whole CTA, so the loop below is uniform)
+            int ks = 1;
+            while (ks < 8 && ntile * ks * 2 <= (int)blockDim.x) ks *= 2;
+            const int slot = threadIdx.x & (ks - 1);
+            const int per = blockDim.x / ks;
+            for (int tb0 = 0; tb0 < ntile; tb0 += per) {
+                const int tile = tb0 + (int)threadIdx.x / ks;
+                const int tq = tile < ntile ? small_div(tile, rtn) : 0;
                 const int m0 = 4 * tq, j0 = 4 * (tile - tq * tn);
-                if (kParity && j0 < 64 && !((fullm >> j0) & 0xFull)) continue;
+                const bool act = tile < ntile && !(kParity && j0 < 64 && !((fullm >> j0) & 0xFull));
                 T acc[4][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
-                if constexpr (kParity) {
-                    // the drop rule per (row, node): keep w iff bits(|w|) >= thr(node)
-                    // (integer compares: no work for the slow FP64 pipe)
-                    unsigned long long tb[4];
+                if (act) {
+                    if constexpr (kParity) {
+                        // the drop rule per (row, node): keep w iff bits(|w|) >= thr(node)
+                        // (integer compares: no work for the slow FP64 pipe)
+                        unsigned long long tb[4];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        tb[j] = j0 + j < nij ? par.thr[C.node_off + j0 + j] : 0x7FF0000000000000ull;
+                        for (int j = 0; j < 4; ++j)
+                            tb[j] = j0 + j < nij ? par.thr[C.node_off + j0 + j] : 0x7FF0000000000000ull;
 #pragma unroll 2
-                    for (int c = 0; c < Nth; ++c) {
-                        T wv[4], xa[4];
-                        load4(WsT + c * Mp + m0, wv);
-                        load4(Xs + c * nijp + j0, xa);
+                        for (int c = slot; c < Nth; c += ks) {
+                            T wv[4], xa[4];
+                            load4(WsT + c * Mp + m0, wv);
+                            load4(Xs + c * nijp + j0, xa);
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const unsigned long long wb =
-                                (unsigned long long)__double_as_longlong((double)wv[i]) & 0x7FFFFFFFFFFFFFFFull;
+                            for (int i = 0; i < 4; ++i) {
+                                const unsigned long long wb =
+                                    (unsigned long long)__double_as_longlong((double)wv[i]) & 0x7FFFFFFFFFFFFFFFull;
 #pragma unroll
-                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(wb >= tb[j] ? wv[i] : T(0), xa[j], acc[i][j]);
+                                for (int j = 0; j < 4; ++j)
+                                    acc[i][j] = fma(wb >= tb[j] ? wv[i] : T(0), xa[j], acc[i][j]);
+                            }
+                        }
+                    } else {
+#pragma unroll 4
+                        for (int c = slot; c < Nth; c += ks) {
+                            T wv[4], xa[4];
+                            load4(WsT + c * Mp + m0, wv);
+                            load4(Xs + c * nijp + j0, xa);
+#pragma unroll
+                            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                                for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
                         }
                     }
-                } else {
-#pragma unroll 4
-                    for (int c = 0; c < Nth; ++c) {
-                        T wv[4], xa[4];
-                        load4(WsT + c * Mp + m0, wv);
-                        load4(Xs + c * nijp + j0, xa);
-#pragma unroll
-                        for (int i = 0; i < 4; ++i)
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) acc[i][j] = fma(wv[i], xa[j], acc[i][j]);
-                    }
                 }
+                for (int o = 1; o < ks; o <<= 1)
 #pragma unroll
-                for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] += __shfl_xor_sync(0xffffffffu, acc[i][j], o);
+                if (act && slot == 0)
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
             }
         }
         __syncthreads();
