@@ -1,13 +1,16 @@
 """Benchmark: time to 1e-8 relative L2 error of the steady RT solve on one GB300.
 
-Workload (default, --workload cfg2): the single adaptive problem -- domain
-[0,3]x[0,2], sigma_s a Gaussian bump (amplitude 0.9, width 0.15) at (1.5, 1.0),
-sigma_t = sigma_s + 0.01, HG g = 0.9, inflow 1 on x = 0 for th in
-(-pi/4, pi/4), hp mesh from seeded random refinement (seed 0, six rounds, 3..7
-nodes per dimension), about 2.2e5 DOF.  Synthetic and seeded; no dataset.
+Workload (default, --workload cfg5): the large two-strong-scatterer problem --
+domain [0,2]^2, discs of radius 0.2 at (0.6, 0.6) and (1.4, 1.4) with
+sigma_s = 50, sigma_t = 50.1, background sigma_t = 0.1, sigma_s = 0.01,
+HG g = 0.95, beam inflow on y = 0; hp mesh from seeded refinement at the disc
+edges (seed 0: 16x16 columns of 5x5 nodes and 32 angular cells of 5 nodes to
+start, four rounds, up to 9 nodes per dimension), 7.95e6 DOF.  Synthetic and
+seeded; no dataset.
 
 A step is one solve from a zero initial guess to the error target.  The
-reference solution is a tight plain FP64 GPU solve (rtol 1e-14) computed before timing;
+reference solution is a tight plain FP64 GPU solve computed before timing
+(its agreement with the CPU oracle is tested on the same recipe at 6.7e4 DOF);
 the error is the quadrature-weighted relative L2 norm (weights = mass weights
 with kappa = 1).  Each method's residual tolerance is calibrated (untimed) as
 the loosest power of ten that reaches the 1e-8 target.  Three methods:
@@ -19,13 +22,17 @@ the loosest power of ten that reaches the 1e-8 target.  Three methods:
 value   : seconds per learned+mixed solve, device-resident inputs.
 e2e     : the same solve through the C ABI with host buffers: H2D of the
           sampled forcing and inflow node values, weighting kernel, solve, D2H
-          of u.
-roofline: the persistent sweep kernel (FP32), the kernel that dominates the
-          solve; apply_roofline: the FP32 system apply.
+          of u.  e2e_with_setup adds the handle's set-up (mesh flattening,
+          coefficient sampling, tables, block inverses, autotuners, network).
+roofline: the kernel that dominates the learned+mixed solve (the FP32 sweep);
+          apply_roofline: the FP32 system apply, with and without the angular
+          scattering matrices it streams.
+adaptive_2e5: the single adaptive problem (2.2e5 DOF) with the same three
+          methods, each error also stated against the CPU oracle's solution.
 
---workload cfg3: 256 independent instances in one batched solve vs the same
-instances solved one by one.  --workload cfg5: the ~9.4e6-DOF two-scatterer
-problem: apply and sweep throughput and a bounded solve.
+--workload cfg2 makes the adaptive problem the headline; --workload cfg3: 256
+independent instances in one batched solve vs the same instances solved one
+by one.
 """
 import argparse
 import ctypes as C
@@ -54,7 +61,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
+    ap.add_argument("--workload", default="cfg5", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu: two solves per method (learned+mixed, mixed, plain), "
@@ -134,8 +141,9 @@ def workload(name, seed=0):
     if name == "cfg1":
         return ("manufactured 4x4x4 cells n=4 (4096 DOF)", W.config1_mesh(), W.manufactured_problem())
     if name == "cfg5":
-        return ("two strong scatterers on [0,2]^2, disc-edge hp refinement seed %d, 5..9 nodes/dim "
-                "(~9.4e6 DOF)" % seed, W.config5_mesh(seed=seed), W.two_disc_problem())
+        return ("two strong scatterers on [0,2]^2 (sigma_s 50, sigma_t 50.1, HG g 0.95), disc-edge hp "
+                "refinement seed %d: 16x16 columns x 32 angular cells to start, 5..9 nodes/dim (~7.9e6 DOF)"
+                % seed, W.config5_mesh(seed=seed), W.two_disc_problem())
     return ("gaussian-bump adaptive hp, seed %d (~2.2e5 DOF)" % seed, W.config2_mesh(seed=seed),
             W.gaussian_bump_problem())
 
@@ -203,24 +211,67 @@ def rel_l2(u, ref, w):
     return float(np.sqrt(np.sum(w * (u - ref) ** 2) / np.sum(w * ref ** 2)))
 
 
-def cpu_baseline(mesh, spec, rtol, u_ref=None, w=None):
-    """The oracle port of the path on the host (single thread): assemble the
+def oracle_solve(mesh, spec, rtol, u_ref=None, w=None, o=None):
+    """The oracle port of the path on the host (one thread): assemble the
     reference's split system with scipy (rt/solve.py:81-101) and solve it with
-    scipy GMRES(50) preconditioned by the same upwind sweep the GPU uses, to the
-    residual tolerance that reaches the error target.  The whole solve is
-    timed (about 10 s for the 2.2e5-DOF workload)."""
+    scipy GMRES(50) preconditioned by the oracle's upwind sweep (this build's
+    preconditioner restated on the CPU; the reference itself hands PETSc
+    bjacobi or kaczmarz), to relative residual rtol.  Returns timings, the
+    solution and its error against u_ref."""
     from oracle import rt_oracle as O
     t0 = time.perf_counter()
-    o = O.assemble(mesh, spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    if o is None:
+        o = O.assemble(mesh, spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
     t_asm = time.perf_counter() - t0
     t1 = time.perf_counter()
-    u, its, info = O.solve_sweep_gmres(o, o["layout"], rtol=rtol)
+    u, its, info = O.solve_sweep_gmres(o, o["layout"], rtol=rtol, maxiter=400)
     t_solve = time.perf_counter() - t1
     err = rel_l2(u, u_ref, w) if u_ref is not None else None
-    return {"value": t_asm + t_solve, "unit": "s", "cores": 1, "kind": "port",
-            "sample": "whole workload: oracle assembly {:.1f} s + scipy sweep-preconditioned GMRES(50) "
-                      "{:.1f} s ({} iterations, rtol {:g})".format(t_asm, t_solve, its, rtol),
-            "rel_l2_err": err}
+    return {"assembly_s": t_asm, "solve_s": t_solve, "iterations": its, "rtol": rtol, "rel_l2_err": err,
+            "u": u, "o": o}
+
+
+def calibrated_cpu_rtol(mesh, spec, o, u_tight, w):
+    """The loosest power of ten (1e-7 .. 1e-13) at which the oracle's solve
+    reaches the error target against its own tight solve (untimed), the same
+    rule the GPU methods use (which start at 1e-6; on these problems 1e-6
+    never reaches 1e-8, and each oracle solve costs seconds)."""
+    for k in range(7, 14):
+        r = oracle_solve(mesh, spec, 10.0 ** (-k), u_tight, w, o=o)
+        if r["rel_l2_err"] <= ERR_TARGET:
+            return 10.0 ** (-k)
+    return 1e-13
+
+
+def cpu_baseline(mesh, spec, rtol, u_ref=None, w=None, scale=1.0, sample_desc="whole workload"):
+    """Timed oracle solve (assembly + sweep-GMRES) scaled by `scale` to the
+    full workload."""
+    r = oracle_solve(mesh, spec, rtol, u_ref, w)
+    t = r["assembly_s"] + r["solve_s"]
+    return {"value": t * scale, "unit": "s", "cores": 1, "kind": "port",
+            "solver": "oracle port: scipy GMRES(50) with this build's upwind sweep restated on the CPU "
+                      "(not the reference's PETSc bjacobi/kaczmarz, which cannot run here)",
+            "sample": "{}: oracle assembly {:.1f} s + sweep-preconditioned GMRES(50) {:.1f} s ({} iterations, "
+                      "rtol {:g} calibrated to the 1e-8 error target), scaled by {:.1f}".format(
+                          sample_desc, r["assembly_s"], r["solve_s"], r["iterations"], rtol, scale),
+            "rel_l2_err": r["rel_l2_err"]}
+
+
+def cpu_sample_cfg5(n_full):
+    """Bounded sample of the two-scatterer workload for the CPU arms: the
+    same recipe at 6.7e4 DOF (8x8 columns of 2x2 nodes, the same 32 angular
+    cells of 5 nodes, one disc-edge refinement round), oracle solve at the
+    rtol calibrated on the sample, wall time scaled by the DOF ratio (the
+    per-DOF work of assembly and of one iteration is set by the angular mesh,
+    which the sample shares)."""
+    from oracle import rt_oracle as O
+    from rtg import workloads as W
+    mesh, spec = W.config5_small_mesh(rounds=1), W.two_disc_problem()
+    o = O.assemble(mesh, spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    w = O.l2_weights(mesh, o["layout"])
+    tight = oracle_solve(mesh, spec, 1e-13, o=o)["u"]
+    rtol = calibrated_cpu_rtol(mesh, spec, o, tight, w)
+    return mesh, spec, rtol, tight, w, n_full / o["N"], o["N"]
 
 
 def _batch_instance_cpu(job):
@@ -355,13 +406,127 @@ def sweep_bytes(ctx, prec_bytes):
     return int(total), int(lev.value), int(lag.value)
 
 
+def l2_weights_dev(ctx, spec):
+    """Quadrature weights (dx dy dth / 8) wx wy wth (mass weights with kappa = 1)."""
+    import torch
+    from rtg import _lib
+    X, Y, _ = ctx.layout.node_coords()
+    ones = ctx.apply(_lib.RTG_MASS, torch.ones(ctx.N, dtype=torch.float64, device=ctx.device))
+    kap = ctx.to_device(np.asarray(np.broadcast_to(spec.kappa(X, Y), (ctx.N,)), dtype=np.float64))
+    return (ones / kap).cpu().numpy()
+
+
+def setup_context(mesh, spec, params):
+    """Handle creation and every first-use set-up, timed: mesh flattening and
+    coefficient sampling with the table upload, forcing and inflow vectors,
+    the sweep's block inverses in both precisions, the apply autotuners in
+    both precisions, the network's coefficients."""
+    import torch
+    from rtg import Problem, _lib, learned as LN
+    out = {}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+    ctx = prob.context(mesh)
+    torch.cuda.synchronize()
+    out["context_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f_dev = ctx.forcing(spec.f)
+    g_dev = ctx.inflow(spec.bcs_dirac)
+    torch.cuda.synchronize()
+    out["vectors_s"] = time.perf_counter() - t0
+    z64 = torch.zeros(ctx.N, dtype=torch.float64, device=ctx.device)
+    t0 = time.perf_counter()
+    ctx.precondition(z64)
+    ctx.precondition(z64.float(), prec=_lib.RTG_FP32)
+    torch.cuda.synchronize()
+    out["sweep_setup_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z64)
+    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z64.float(), prec=_lib.RTG_FP32)
+    torch.cuda.synchronize()
+    out["apply_tuning_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    LN.set_params(ctx, params)
+    torch.cuda.synchronize()
+    out["network_s"] = time.perf_counter() - t0
+    out["total_s"] = sum(out.values())
+    return ctx, f_dev, g_dev, out
+
+
+ARMS = {"plain_fp64": (0, 1), "mixed": (1, 1), "learned_mixed": (1, 3)}
+
+
+def solve_arm(ctx, f_dev, g_dev, arm, rtol):
+    method, pc = ARMS[arm]
+    return ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=3000, precond=pc, restart=30,
+                     inner_rtol=1e-5)
+
+
+def measure_arms(ctx, f_dev, g_dev, u_ref_h, w, steps, warmup, flush, stream, clk=None, u_oracle=None):
+    """Calibrate each method's rtol against the reference solution, then time
+    it (learned+mixed: steps after warmup; the others: up to 3 after 1)."""
+    import torch
+    rtols, first = {}, {}
+    for arm in ARMS:
+        for k in range(6, 15):
+            t0 = time.perf_counter()
+            u, info = solve_arm(ctx, f_dev, g_dev, arm, 10.0 ** (-k))
+            torch.cuda.synchronize()
+            first.setdefault(arm, time.perf_counter() - t0)
+            if rel_l2(u.cpu().numpy(), u_ref_h, w) <= ERR_TARGET:
+                rtols[arm] = 10.0 ** (-k)
+                break
+        else:
+            raise RuntimeError("{} did not reach the error target".format(arm))
+    launch_count = ctx.lib.rtg_launch_count
+    res = {}
+    for arm in ("learned_mixed", "mixed", "plain_fp64"):
+        n_steps, n_warm = (steps, warmup) if arm == "learned_mixed" else (max(1, min(steps, 3)), 1)
+        for _ in range(n_warm):
+            solve_arm(ctx, f_dev, g_dev, arm, rtols[arm])
+        times, errs, infos, launched = [], [], [], 0
+        if clk is not None and arm == "learned_mixed":
+            clk.__enter__()
+        for _ in range(n_steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = _events(stream)
+            n0 = launch_count()
+            e0.record(stream)
+            u, info = solve_arm(ctx, f_dev, g_dev, arm, rtols[arm])
+            e1.record(stream)
+            launched += launch_count() - n0
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            uh = u.cpu().numpy()
+            errs.append(rel_l2(uh, u_ref_h, w))
+            infos.append(info)
+        if clk is not None and arm == "learned_mixed":
+            clk.__exit__()
+        i = infos[-1]
+        res[arm] = {"rtol": rtols[arm], "rel_l2_err": max(errs), "median_s": statistics.median(times),
+                    "seconds": times, "iterations": i["iterations"], "outer": i["outer"],
+                    "fp64_applies": i["fp64_applies"], "fp32_applies": i["fp32_applies"],
+                    "learned": i["learned"], "fallbacks": i["fallbacks"], "first_solve_s": first[arm],
+                    "launches_per_solve": launched // max(1, n_steps)}
+        if u_oracle is not None:
+            res[arm]["rel_l2_err_vs_oracle"] = rel_l2(uh, u_oracle, w)
+    return res
+
+
+def w_bytes_fp32(ctx):
+    """Bytes of the FP32 angular scattering matrices an FP32 apply streams
+    (one Nth_col x Nth_col matrix per distinct column angular mesh)."""
+    so = ctx.sampled.sig_off
+    return int(4 * (so[-1] - so[0]))
+
+
 def run_ours(args):
     if args.workload == "cfg3":
         return run_batched(args)
-    if args.workload == "cfg5":
-        return run_large(args)
     import torch
-    from rtg import Problem, _lib, learned as LN
+    from rtg import _lib, learned as LN
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -372,74 +537,23 @@ def run_ours(args):
         torch.cuda.set_device(local)
     else:
         torch.cuda.set_device(0)
+    t0 = time.perf_counter()
     desc, mesh, spec = workload(args.workload, seed=rank)
-    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
-    ctx = prob.context(mesh)
-    N = ctx.N
-    f_dev = ctx.forcing(spec.f)
-    g_dev = ctx.inflow(spec.bcs_dirac)
+    mesh_s = time.perf_counter() - t0
     params, net_meta = LN.load(LN.DEFAULT_NET)
-    LN.set_params(ctx, params)
-    # L2 weights (dx dy dth/8) wx wy wth = mass weights with kappa = 1
-    lay = ctx.layout
-    X, Y, T = lay.node_coords()
-    ones = ctx.apply(_lib.RTG_MASS, torch.ones(N, dtype=torch.float64, device=ctx.device))
-    kap = ctx.to_device(np.asarray(np.broadcast_to(spec.kappa(X, Y), (N,)), dtype=np.float64))
-    w = (ones / kap).cpu().numpy()
-
+    ctx, f_dev, g_dev, setup = setup_context(mesh, spec, params)
+    N = ctx.N
+    w = l2_weights_dev(ctx, spec)
     # reference solution: tight plain FP64 solve
-    u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=20000, precond=1)
+    u_ref, info_ref = ctx.solve(f_dev, g_dev, method=0, rtol=1e-13, max_it=3000, precond=1)
     u_ref_h = u_ref.cpu().numpy()
-    arms = {"plain_fp64": (0, 1), "mixed": (1, 1), "learned_mixed": (1, 3)}
-
-    def solve(arm, rtol):
-        method, pc = arms[arm]
-        return ctx.solve(f_dev, g_dev, method=method, rtol=rtol, max_it=20000, precond=pc, restart=30,
-                         inner_rtol=1e-5)
-
-    def calibrate(arm):
-        for k in range(6, 15):
-            rtol = 10.0 ** (-k)
-            u, info = solve(arm, rtol)
-            err = rel_l2(u.cpu().numpy(), u_ref_h, w)
-            if err <= ERR_TARGET:
-                return rtol
-        raise RuntimeError("{} did not reach the error target".format(arm))
-
-    rtols = {arm: calibrate(arm) for arm in arms}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=ctx.device)
     stream = torch.cuda.current_stream()
-
-    launch_count = ctx.lib.rtg_launch_count
-    launched = {}
-
-    def timed(arm, steps, warm):
-        for _ in range(warm):
-            solve(arm, rtols[arm])
-        times, errs, infos = [], [], []
-        launched[arm] = 0
-        for _ in range(steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            e0, e1 = _events(stream)
-            n0 = launch_count()
-            e0.record(stream)
-            u, info = solve(arm, rtols[arm])
-            e1.record(stream)
-            launched[arm] += launch_count() - n0
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
-            errs.append(rel_l2(u.cpu().numpy(), u_ref_h, w))
-            infos.append(info)
-        return times, errs, infos
-
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        res = {"learned_mixed": timed("learned_mixed", args.steps, args.warmup)}
-    res["mixed"] = timed("mixed", max(1, min(args.steps, 3)), 1)
-    res["plain_fp64"] = timed("plain_fp64", max(1, min(args.steps, 3)), 1)
+    clk = ClockSampler(torch.cuda.current_device())
+    res = measure_arms(ctx, f_dev, g_dev, u_ref_h, w, args.steps, args.warmup, flush, stream, clk=clk)
     if world > 1:
         torch.distributed.barrier()
 
@@ -452,8 +566,8 @@ def run_ours(args):
     fw = torch.empty_like(fd)
     gd = torch.empty_like(fd)
     ud = torch.zeros_like(fd)
-    opts = _lib.SolveOpts(method=1, restart=30, max_it=20000, rtol=rtols["learned_mixed"], atol=0., precond=3,
-                          nonzero_guess=0, inner_rtol=1e-5, max_outer=20, verbose=0)
+    opts = _lib.SolveOpts(method=1, restart=30, max_it=3000, rtol=res["learned_mixed"]["rtol"], atol=0.,
+                          precond=3, nonzero_guess=0, inner_rtol=1e-5, max_outer=20, verbose=0)
     sinfo = _lib.SolveInfo()
     sp = C.c_void_p(stream.cuda_stream)
     e2e_times = []
@@ -474,7 +588,7 @@ def run_ours(args):
             e2e_times.append(e0.elapsed_time(e1) / 1e3)
     e2e_err = rel_l2(u_host.numpy(), u_ref_h, w)
 
-    # rooflines: the FP32 sweep (dominant kernel of the solve) and the FP32 apply
+    # rooflines: the FP32 sweep (dominant kernel of the learned+mixed solve) and the FP32 apply
     peak, peak_kind = peaks()
     r32 = torch.randn(N, dtype=torch.float32, device=ctx.device)
     z32 = torch.empty_like(r32)
@@ -483,13 +597,14 @@ def run_ours(args):
     t_apply = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, r32, z32, prec=_lib.RTG_FP32),
                           stream, flush)
     bytes_apply = int(ctx.info["bytes_per_apply_fp32"])
+    wb = w_bytes_fp32(ctx)
     x64 = torch.randn(N, dtype=torch.float64, device=ctx.device)
     y64 = torch.empty_like(x64)
     t_apply64 = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x64, y64, prec=_lib.RTG_FP64),
-                            stream, flush)
-    t_sweep64 = kernel_time(lambda: ctx.precondition(x64, y64, prec=_lib.RTG_FP64), stream, flush)
+                            stream, flush, 5)
+    t_sweep64 = kernel_time(lambda: ctx.precondition(x64, y64, prec=_lib.RTG_FP64), stream, flush, 5)
 
-    t_l, e_l, i_l = res["learned_mixed"]
+    t_l = res["learned_mixed"]["seconds"]
     value = statistics.median(t_l)
     if world > 1:
         tt = torch.tensor([max(t_l)], device=ctx.device)
@@ -497,18 +612,9 @@ def run_ours(args):
         value = float(tt.item())
     if rank != 0:
         return None
-    inf = i_l[-1]
-    # librtg kernels launched inside the timed solves (the library's own count)
-    launches = int(launched["learned_mixed"])
-
-    def arm_summary(arm):
-        t, e, i = res[arm]
-        return {"rtol": rtols[arm], "rel_l2_err": max(e), "median_s": statistics.median(t), "seconds": t,
-                "iterations": i[-1]["iterations"], "outer": i[-1]["outer"], "fp64_applies": i[-1]["fp64_applies"],
-                "fp32_applies": i[-1]["fp32_applies"], "learned": i[-1]["learned"],
-                "fallbacks": i[-1]["fallbacks"]}
-
-    t_plain = statistics.median(res["plain_fp64"][0])
+    t_plain = res["plain_fp64"]["median_s"]
+    tag = "cfg5" if args.workload == "cfg5" else "cfg2"
+    e2e = statistics.median(e2e_times)
     out = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * value, "higher_is_better": False,
@@ -516,36 +622,77 @@ def run_ours(args):
         "data": "synthetic (seeded hp mesh and coefficients)",
         "config": {"workload": desc, "ndof": N, "ndof_interior": int(ctx.info["ndof_interior"]),
                    "error_target": ERR_TARGET, "l2_flush": "256 MB write before every timed solve and kernel",
-                   "learned_mixed": arm_summary("learned_mixed"), "mixed": arm_summary("mixed"),
-                   "plain_fp64": arm_summary("plain_fp64"),
+                   "learned_mixed": res["learned_mixed"], "mixed": res["mixed"], "plain_fp64": res["plain_fp64"],
                    "speedup_learned_mixed_vs_plain_fp64": t_plain / value,
-                   "speedup_mixed_vs_plain_fp64": t_plain / statistics.median(res["mixed"][0]),
+                   "speedup_mixed_vs_plain_fp64": t_plain / res["mixed"]["median_s"],
                    "network": {"file": "rtg/nets/sweep_correction.npz", **net_meta},
-                   "reference_solution": {"rtol": 1e-14, "iterations": info_ref["iterations"], "res_f": info_ref["res_f"]},
+                   "reference_solution": {"method": "plain FP64 GPU solve", "rtol": 1e-13,
+                                          "iterations": info_ref["iterations"],
+                                          "rel_residual": info_ref["res_f"] / max(info_ref["rhs_norm"], 1e-300)},
+                   "setup": {"mesh_s": mesh_s, **setup},
                    "kernels_us": {"sweep_fp32": 1e6 * t_sweep, "sweep_fp64": 1e6 * t_sweep64,
                                   "apply_fp32": 1e6 * t_apply, "apply_fp64": 1e6 * t_apply64},
+                   "apply_fp64": {"flops": int(ctx.info["flops_per_apply"]),
+                                  "note": "FP64-pipe bound (GB300 FP64 rate is 1/64 of FP32)"},
                    "sweep": {"levels": nlev, "lagged_couplings": nlag},
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": statistics.median(e2e_times), "unit": "s", "h2d_bytes_per_step": 2 * 8 * N,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 2 * 8 * N,
                 "d2h_bytes_per_step": 8 * N, "rel_l2_err": e2e_err},
-        "gpu_launches": launches,
+        "e2e_with_setup": {"value": e2e + setup["total_s"] + mesh_s, "unit": "s",
+                           "note": "e2e plus the handle's set-up (a new mesh in an AMR loop pays it per solve)"},
+        "gpu_launches": int(res["learned_mixed"]["launches_per_solve"]) * args.steps,
         "roofline": {"bound": "hbm", "achieved": sb / t_sweep / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": sb / t_sweep / 1e9 / peak,
-                     "traffic": profiled_traffic("sweep_persistent_kernel_fp32_cfg2") if args.workload == "cfg2"
-                     else None,
+                     "traffic": profiled_traffic("sweep_persistent_kernel_fp32_" + tag),
                      "kernel": "sweep_persistent_kernel<float>", "bytes_per_launch": sb, "launch_s": t_sweep,
                      "peak_kind": peak_kind,
                      "note": "latency bound: {} wavefront levels, {:.2f} us per level".format(
                          nlev, 1e6 * t_sweep / max(nlev, 1))},
         "apply_roofline": {"bound": "hbm", "achieved": bytes_apply / t_apply / 1e9, "peak": peak, "unit": "GB/s",
                            "frac": bytes_apply / t_apply / 1e9 / peak, "kernel": "apply_tiled_kernel (FP32 system)",
-                           "bytes_per_launch": bytes_apply, "launch_s": t_apply, "peak_kind": peak_kind,
-                           "dof_applies_per_s": N / t_apply},
+                           "bytes_per_launch": bytes_apply, "w_bytes_per_launch": wb,
+                           "frac_with_w": (bytes_apply + wb) / t_apply / 1e9 / peak,
+                           "traffic": profiled_traffic("apply_tiled_kernel_fp32_" + tag),
+                           "launch_s": t_apply, "peak_kind": peak_kind, "dof_applies_per_s": N / t_apply,
+                           "tflops": ctx.info["flops_per_apply"] / t_apply / 1e12},
         "clocks": clk.summary(),
     }
+    if args.workload == "cfg5":
+        if not args.no_cpu:
+            smesh, sspec, srtol, stight, sw, scale, sN = cpu_sample_cfg5(N)
+            out["cpu_baseline"] = cpu_baseline(smesh, sspec, srtol, stight, sw, scale=scale,
+                                               sample_desc="the same recipe at {} DOF (one refinement round, "
+                                                           "8x8 columns of 2x2 nodes)".format(sN))
+        out["adaptive_2e5"] = secondary_adaptive(args, flush, stream)
+    else:
+        out["amr_indicators"] = amr_indicators(ctx, mesh, u_ref_h, stream, flush, not args.no_cpu)
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(mesh, spec, res["plain_fp64"]["rtol"], u_ref_h, w)
+    ctx.close()
+    return out
+
+
+def secondary_adaptive(args, flush, stream):
+    """The single adaptive problem (2.2e5 DOF): the three methods timed the same
+    way, each error also against the CPU oracle's solution; the AMR indicator
+    kernels; the oracle's solve timed as its CPU baseline."""
+    from rtg import learned as LN
+    desc, mesh, spec = workload("cfg2")
+    params, _ = LN.load(LN.DEFAULT_NET)
+    ctx, f_dev, g_dev, setup = setup_context(mesh, spec, params)
+    w = l2_weights_dev(ctx, spec)
+    u_ref, _ = ctx.solve(f_dev, g_dev, method=0, rtol=1e-14, max_it=3000, precond=1)
+    u_ref_h = u_ref.cpu().numpy()
+    orc = oracle_solve(mesh, spec, 1e-13, u_ref_h, w)
+    res = measure_arms(ctx, f_dev, g_dev, u_ref_h, w, min(args.steps, 3), 1, flush, stream, u_oracle=orc["u"])
+    out = {"workload": desc, "ndof": ctx.N, "setup": setup, **res,
+           "speedup_learned_mixed_vs_plain_fp64": res["plain_fp64"]["median_s"] / res["learned_mixed"]["median_s"],
+           "gpu_reference_vs_oracle_rel_l2": orc["rel_l2_err"],
+           "oracle_solution": {"rtol": 1e-13, "iterations": orc["iterations"]}}
     out["amr_indicators"] = amr_indicators(ctx, mesh, u_ref_h, stream, flush, not args.no_cpu)
     if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(mesh, spec, rtols["plain_fp64"], u_ref_h, w)
+        out["cpu_baseline"] = cpu_baseline(mesh, spec, res["plain_fp64"]["rtol"], u_ref_h, w)
+    ctx.close()
     return out
 
 
@@ -629,66 +776,32 @@ def run_batched(args):
     return out
 
 
-def run_large(args):
-    """cfg5 (~9.4e6 DOF): apply and sweep throughput in FP32 and FP64, and a
-    bounded learned+mixed solve (the strongly forward-peaked thick discs make
-    sweep-preconditioned GMRES stagnate; the residual reached is reported)."""
-    import torch
-    from rtg import Problem, _lib, learned as LN
-    torch.cuda.set_device(0)
-    desc, mesh, spec = workload("cfg5")
-    prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
-    ctx = prob.context(mesh)
-    N = ctx.N
-    stream = torch.cuda.current_stream()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=ctx.device)
-    peak, peak_kind = peaks()
-    out = {}
-    for nm, dt, prec, key in (("fp32", torch.float32, _lib.RTG_FP32, "bytes_per_apply_fp32"),
-                              ("fp64", torch.float64, _lib.RTG_FP64, "bytes_per_apply_fp64")):
-        x = torch.randn(N, dtype=dt, device=ctx.device)
-        y = torch.empty_like(x)
-        ta = kernel_time(lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec), stream, flush, 10)
-        ts = kernel_time(lambda: ctx.precondition(x, y, prec=prec), stream, flush, 5)
-        out[nm] = {"apply_s": ta, "apply_gbs": ctx.info[key] / ta / 1e9, "apply_frac": ctx.info[key] / ta / 1e9 / peak,
-                   "dof_applies_per_s": N / ta, "apply_tflops": ctx.info["flops_per_apply"] / ta / 1e12,
-                   "sweep_s": ts}
-    params, _ = LN.load(LN.DEFAULT_NET)
-    LN.set_params(ctx, params)
-    f_dev = ctx.forcing(spec.f)
-    g_dev = ctx.inflow(spec.bcs_dirac)
-    with ClockSampler(0) as clk:
-        torch.cuda.synchronize()
-        e0, e1 = _events(stream)
-        n0 = ctx.lib.rtg_launch_count()
-        e0.record(stream)
-        u, info = ctx.solve(f_dev, g_dev, method=1, precond=3, rtol=1e-8, max_it=300, restart=30, inner_rtol=1e-5)
-        e1.record(stream)
-        n_launch = ctx.lib.rtg_launch_count() - n0
-        torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
-    return {"metric": METRIC, "value": t, "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 0,
-            "ms_per_step": 1e3 * t, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32-inner/f64-outer", "data": "synthetic (seeded disc-edge hp mesh)",
-            "config": {"workload": desc, "ndof": N, "bounded_solve": {
-                "max_it": 300, "iterations": info["iterations"], "converged": info["converged"],
-                "rel_residual": info["res_f"] / max(info["rhs_norm"], 1e-300), "fallbacks": info["fallbacks"]},
-                "kernels": out},
-            "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "roofline": {"bound": "hbm", "achieved": out["fp32"]["apply_gbs"], "peak": peak, "unit": "GB/s",
-                         "frac": out["fp32"]["apply_frac"], "traffic": None, "kernel": "apply_tiled_kernel (FP32)",
-                         "peak_kind": peak_kind},
-            "gpu_launches": int(n_launch), "clocks": clk.summary()}
-
-
 def run_reference(args):
+    """The CPU arm: the oracle port timed on the host.  Two-scatterer workload:
+    each step times the bounded sample of cpu_sample_cfg5 (the rtol calibrated
+    on it, untimed) and scales it to the full DOF count; the adaptive problem
+    is timed whole."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
     desc, mesh, spec = workload(args.workload)
+    if args.workload == "cfg5":
+        from rtg.layout import MeshLayout
+        n_full = MeshLayout(mesh).N
+        smesh, sspec, rtol, tight, w, scale, sN = cpu_sample_cfg5(n_full)
+        run = lambda: cpu_baseline(smesh, sspec, rtol, tight, w, scale=scale,
+                                   sample_desc="the same recipe at {} DOF (one refinement round, "
+                                               "8x8 columns of 2x2 nodes)".format(sN))
+    else:
+        from oracle import rt_oracle as O
+        o = O.assemble(mesh, spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
+        w = O.l2_weights(mesh, o["layout"])
+        tight = oracle_solve(mesh, spec, 1e-13, o=o)["u"]
+        rtol = calibrated_cpu_rtol(mesh, spec, o, tight, w)
+        run = lambda: cpu_baseline(mesh, spec, rtol, tight, w)
     vals = []
     for it in range(args.warmup + args.steps):
-        cb = cpu_baseline(mesh, spec, 1e-9)
+        cb = run()
         if it >= args.warmup:
             vals.append(cb["value"])
     v = statistics.median(vals)

@@ -154,13 +154,15 @@ def gaussian_bump_problem(Lx=3., Ly=2., amp=0.9, width=0.15, xc=1.5, yc=1.0, g=0
                          meta={"g": g})
 
 
-def two_disc_problem(Lx=2., Ly=2., g=0.95):
+def two_disc_problem(Lx=2., Ly=2., g=0.95, discs=((0.6, 0.6), (1.4, 1.4)), rad=0.2, sigma_s=50.):
     """Two strong scatterers: discs of radius 0.2 at (0.6, 0.6) and (1.4, 1.4)
     with sigma_s = 50, sigma_t = 50.1 inside; background sigma_t = 0.1,
-    sigma_s = 0.01; beam inflow on y = 0 for |x - 1| < 0.25, |th - pi/2| < pi/8."""
+    sigma_s = 0.01; beam inflow on y = 0 for |x - 1| < 0.25, |th - pi/2| < pi/8.
+    (discs, rad and sigma_s vary it for the learned correction's training
+    family; sigma_t = sigma_s + 0.1 inside.)"""
     Phi = hg_phase(g)
-    discs = ((0.6, 0.6), (1.4, 1.4))
-    rad = 0.2
+    discs = tuple(tuple(d) for d in discs)
+    sig_in, kap_in = float(sigma_s), float(sigma_s) + 0.1
 
     def inside(x, y):
         x = np.asarray(x, dtype=float)
@@ -171,10 +173,10 @@ def two_disc_problem(Lx=2., Ly=2., g=0.95):
         return m
 
     def kappa(x, y):
-        return np.where(inside(x, y), 50.1, 0.1)
+        return np.where(inside(x, y), kap_in, 0.1)
 
     def sigma(x, y):
-        return np.where(inside(x, y), 50., 0.01)
+        return np.where(inside(x, y), sig_in, 0.01)
 
     def f(x, y, th):
         return 0. * (x + y + th)
@@ -430,6 +432,27 @@ def batch_instance(seed, mesh_cls=Mesh, max_cols=64, max_cells=16, n_range=(2, 8
     g = float(rng.uniform(0., 0.95))
     xs, ys = (float(v) for v in rng.uniform(0.3, 0.7, size=2))
     return mesh, gaussian_source_problem(sigma_t, ratio, g, xs=xs, ys=ys)
+
+
+def disc_family_instance(seed, mesh_cls=Mesh):
+    """One problem of the learned correction's two-scatterer family: one or
+    two discs (centres U([0.4, 1.6]^2), radius U(0.1, 0.3)), sigma_s
+    log-uniform in [2, 50] inside (sigma_t = sigma_s + 0.1), HG g in
+    U(0.7, 0.95), the two-scatterer beam inflow, on the resolved-angle
+    disc-edge recipe at one refinement round (8x8 columns of 2x2 or 3x3 nodes,
+    32 angular cells of 5 nodes; about 7e4 to 1.5e5 DOF)."""
+    rng = np.random.default_rng(104729 + seed)
+    nd = int(rng.integers(1, 3))
+    discs = tuple((float(a), float(b)) for a, b in rng.uniform(0.4, 1.6, size=(nd, 2)))
+    rad = float(rng.uniform(0.1, 0.3))
+    sig = float(np.exp(rng.uniform(np.log(2.), np.log(50.))))
+    g = float(rng.uniform(0.7, 0.95))
+    n0 = int(rng.integers(2, 4))
+    mesh = disc_edge_mesh(mesh_cls=mesh_cls, seed=seed, rounds=1, n0=n0, nth0=5, n_max=n0 + 2, nref_ang=5,
+                          nref_spt=3, ang_prob=0.1, max_ang_lv=6, discs=discs, radius=rad)
+    spec = two_disc_problem(g=g, discs=discs, rad=rad, sigma_s=sig)
+    spec.meta.update({"seed": seed, "sigma_s": sig})
+    return mesh, spec
 
 
 def config2_mesh(mesh_cls=Mesh, seed=0):
