@@ -509,6 +509,7 @@ def measure_arms(ctx, f_dev, g_dev, u_ref_h, w, steps, warmup, flush, stream, cl
                     "seconds": times, "iterations": i["iterations"], "outer": i["outer"],
                     "fp64_applies": i["fp64_applies"], "fp32_applies": i["fp32_applies"],
                     "learned": i["learned"], "fallbacks": i["fallbacks"], "first_solve_s": first[arm],
+                    "learned_kept": i["learned_kept"],
                     "launches_per_solve": launched // max(1, n_steps)}
         if u_oracle is not None:
             res[arm]["rel_l2_err_vs_oracle"] = rel_l2(uh, u_oracle, w)

@@ -136,8 +136,11 @@ typedef struct rtg_solve_opts {
     int32_t precond;       /* 0 none, 1 upwind transport sweep (right precond.),
                               2 sweep + column diffusion correction (two-level,
                               FGMRES), 3 sweep + learned correction (FGMRES;
-                              needs rtg_nn_set_params), falling back to 1 on a
-                              stall */
+                              needs rtg_nn_set_params): once per handle and
+                              inner precision, two timed 8-step cycles from
+                              the first residual (sweep alone, then with the
+                              correction) decide whether the correction stays;
+                              it also falls back to 1 on a stall */
     int32_t nonzero_guess; /* 1: start from x (reference: x0 = f_I)             */
     double  inner_rtol;    /* method 1: inner FP32 reduction per outer step     */
     int32_t max_outer;     /* method 1: cap on refinement steps                 */
@@ -159,6 +162,10 @@ typedef struct rtg_solve_info {
     int32_t learned;       /* applications of the learned correction           */
     int32_t fallbacks;     /* precond 3: switches to the sweep alone (stalls)  */
     int32_t coarse;        /* applications of the diffusion correction         */
+    int32_t trial_its;     /* precond 3: iterations of the learned-correction
+                              trial run by this solve (0: decided earlier)    */
+    int32_t learned_kept;  /* precond 3: 1 the trial kept the learned
+                              correction, 0 the sweep alone was faster        */
 } rtg_solve_info;
 
 /* library / quadrature ------------------------------------------------------ */

@@ -212,6 +212,10 @@ struct rtg_handle {
     rtg::ApplyPlan* plan32 = nullptr;
     rtg::BatchWs* bws = nullptr;
     rtg::NNWs* nn = nullptr;
+    // precond 3: outcome of the trial that decides whether the learned
+    // correction stays in the solve, per inner precision (0 FP64, 1 FP32):
+    // 0 not run yet, 1 kept, 2 the sweep alone reduced the residual faster
+    int nn_trial[2] = {0, 0};
     rtg::Coarse* coarse = nullptr;
     rtg::AmrTables* amr = nullptr;
 };

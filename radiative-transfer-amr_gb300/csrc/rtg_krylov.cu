@@ -733,6 +733,47 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
     return res;
 }
 
+// Precond 3 trial: from the same right-hand side, one timed cycle of
+// kTrialSteps steps with the sweep alone and one with the learned correction;
+// the correction stays when its log residual reduction per second is larger.
+// Runs once per handle and inner precision (h->nn_trial), the first time
+// precond 3 meets a residual; adds its work to pc and applies.
+constexpr int kTrialSteps = 8;
+
+template <typename T>
+void learned_trial(rtg_handle* h, Workspace* ws, const T* rhs, double beta, T* xT, T* wbuf, T* V, int* applies,
+                   PcState& pc, int* trial_its, cudaStream_t s) {
+    const int pi = sizeof(T) == 8 ? 0 : 1;
+    cudaEvent_t e0, e1;
+    RTG_CUDA(cudaEventCreate(&e0));
+    RTG_CUDA(cudaEventCreate(&e1));
+    double rate[2] = {0., 0.};   // log reduction per second: sweep alone, with the correction
+    try {
+        for (int q = 0; q < 2; ++q) {
+            PcState t;
+            t.mode = q == 0 ? 1 : 3;
+            RTG_CUDA(cudaEventRecord(e0, s));
+            GmresResult gr = gmres<T>(h, ws, rhs, xT, wbuf, V, kTrialSteps, 0., kTrialSteps, nullptr, applies, t, s);
+            RTG_CUDA(cudaEventRecord(e1, s));
+            RTG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            const double ratio = std::max(gr.res / beta, 1e-30);
+            rate[q] = -std::log(ratio) / std::max(1e-3 * (double)ms, 1e-9);
+            pc.sweeps += t.sweeps;
+            pc.learned += t.learned;
+            *trial_its += gr.iters;
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->nn_trial[pi] = rate[1] > rate[0] ? 1 : 2;
+}
+
 }  // namespace
 
 int last_hessenberg(rtg_handle* h, double* R, int cap, int* n, cudaStream_t s) {
@@ -810,11 +851,24 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
         throw RtgError{RTG_ERR_ARG, "preconditioner 3 needs a network (rtg_nn_set_params)"};
     if (pc.mode >= 1) get_sweep(h, s);
     if (pc.mode == 2 && !h->coarse) build_coarse(h, s);
+    const int tpi = o->method == 0 ? 0 : 1;
+    // precond 3 after a lost trial: the sweep alone
+    auto trial_verdict = [&]() {
+        if (pc.mode == 3 && h->nn_trial[tpi] == 2) {
+            pc.mode = 1;
+            ++pc.fallbacks;
+        }
+    };
+    trial_verdict();
 
     if (o->method == 0) {
         // GMRES on the correction: A d = r, x += d, repeated until converged.
         int used = 0;
         while (res > tol && used < o->max_it) {
+            if (pc.mode == 3 && h->nn_trial[0] == 0) {
+                learned_trial<double>(h, ws, ws->r, res, ws->w64, ws->t, ws->V64, &applies64, pc, &inf.trial_its, s);
+                trial_verdict();
+            }
             GmresResult gr = gmres<double>(h, ws, ws->r, ws->w64, ws->t, ws->V64, m, tol,
                                            o->max_it - used, &hv, &applies64, pc, s);
             used += std::max(gr.iters, 1);
@@ -837,6 +891,10 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
         while (res > tol && used < o->max_it && outer < max_outer) {
             // r32 = r / ||r||
             axpby_kernel<double, float><<<grid_for(N), 256, 0, s>>>(1. / res, ws->r, 0., ws->w32, N), count_launch();
+            if (pc.mode == 3 && h->nn_trial[1] == 0) {
+                learned_trial<float>(h, ws, ws->w32, 1., ws->d32, ws->s32, ws->V32, &applies32, pc, &inf.trial_its, s);
+                trial_verdict();
+            }
             // one FP32 solve per refinement step, capped at 20 restart cycles
             const int inner_cap = std::min(o->max_it - used, 20 * m);
             GmresResult gr = gmres<float>(h, ws, ws->w32, ws->d32, ws->s32, ws->V32, m,
@@ -863,6 +921,7 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.learned = pc.learned;
     inf.coarse = pc.coarse;
     inf.fallbacks = pc.fallbacks;
+    inf.learned_kept = (o->precond == 3 && h->nn_trial[tpi] == 1) ? 1 : 0;
     if (o->precond >= 1 && sweep_status(h, s) != RTG_OK)
         throw RtgError{RTG_ERR_TIMEOUT, "a sweep wait gave up; the solution is not valid"};
     inf.res_f = res;

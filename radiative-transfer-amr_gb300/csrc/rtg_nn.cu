@@ -828,6 +828,7 @@ void nn_set_params(rtg_handle* h, const float* params, cudaStream_t s) {
     }
     RTG_CUDA(cudaFree(P));
     w->has_params = true;
+    h->nn_trial[0] = h->nn_trial[1] = 0;   // a new network gets a new trial
 }
 
 bool nn_has_params(rtg_handle* h) { return h->nn && h->nn->has_params; }

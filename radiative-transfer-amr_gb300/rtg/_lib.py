@@ -70,7 +70,8 @@ class SolveInfo(C.Structure):
                 ("fp64_applies", C.c_int32), ("fp32_applies", C.c_int32), ("res0", C.c_double),
                 ("res_f", C.c_double), ("rhs_norm", C.c_double), ("seconds", C.c_double),
                 ("hist_len", C.c_int32), ("sweeps", C.c_int32), ("learned", C.c_int32),
-                ("fallbacks", C.c_int32), ("coarse", C.c_int32)]
+                ("fallbacks", C.c_int32), ("coarse", C.c_int32), ("trial_its", C.c_int32),
+                ("learned_kept", C.c_int32)]
 
 
 # exported symbol -> (restype, argtypes)
