@@ -29,7 +29,7 @@ namespace rtg {
 
 namespace {
 
-constexpr int kRedBlocks = 296;   // 2 x 148-ish; partial sums per reduction
+constexpr int kRedBlocks = 1216;  // 8 per SM on 152 SMs: enough loads in flight for HBM; partial sums per reduction
 constexpr int kRedThreads = 256;
 constexpr int kDotGroup = 8;      // vectors per pass in multi_dot
 
@@ -38,6 +38,25 @@ constexpr int kDotGroup = 8;      // vectors per pass in multi_dot
 // it), double from the per-warp sums on.
 template <typename T>
 using Acc = T;
+
+// Sum over the blocks' partials of output q for one lane: the lane's blocks
+// lane, lane + 32, ... loaded eight at a time (one L2 round trip per eight),
+// added in that fixed order.
+__device__ __forceinline__ double lane_partials(const double* __restrict__ partial, int nblocks, int stride, int q,
+                                                int lane) {
+    double sq = 0.;
+    for (int b0 = lane; b0 < nblocks; b0 += 32 * 8) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int b = b0 + 32 * u;
+            v[u] = b < nblocks ? __ldcg(partial + (int64_t)b * stride + q) : 0.;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) sq += v[u];
+    }
+    return sq;
+}
 
 // out[q] = <V_q, w> for q < k.  Each block writes its partial sums; the last
 // block to finish (atomic ticket) adds them in block order, so the result does
@@ -87,7 +106,7 @@ __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, co
     const int lane = threadIdx.x & 31;
     for (int q = threadIdx.x >> 5; q < k; q += blockDim.x >> 5) {
         double sq = 0.;
-        for (int b = lane; b < (int)gridDim.x; b += 32) sq += __ldcg(partial + (int64_t)b * k + q);
+        sq = lane_partials(partial, (int)gridDim.x, k, q, lane);
         for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
         if (lane == 0) {
             out[q] = sq;
@@ -172,7 +191,15 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
     for (int q = 0; q < K; ++q) acc[q] = Acc<T>(0);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         Acc<T> sv = w[i];
-        for (int q = 0; q < k; ++q) sv = fma(-hs[q], (Acc<T>)V[(int64_t)q * ldv + i], sv);
+        // eight loads in flight before their FMAs (a plain loop waits for each)
+        for (int q0 = 0; q0 < k; q0 += 8) {
+            T vv[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) vv[q] = q0 + q < k ? V[(int64_t)(q0 + q) * ldv + i] : T(0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q0 + q < k) sv = fma(-hs[q0 + q], (Acc<T>)vv[q], sv);
+        }
         w[i] = (T)sv;
         if (kNorm) {
             acc[0] = fma(sv, sv, acc[0]);
@@ -205,7 +232,7 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
     const int lane = threadIdx.x & 31;
     for (int q = threadIdx.x >> 5; q < nout; q += blockDim.x >> 5) {
         double sq = 0.;
-        for (int b = lane; b < (int)gridDim.x; b += 32) sq += __ldcg(partial + (int64_t)b * nout + q);
+        sq = lane_partials(partial, (int)gridDim.x, nout, q, lane);
         for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
         if (lane == 0) {
             out[q] = sq;
@@ -227,7 +254,14 @@ __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, in
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         Acc<T> sv = w[i];
-        for (int q = 0; q < k; ++q) sv = fma(-hs[q], Acc<T>(V[(int64_t)q * ldv + i]), sv);
+        for (int q0 = 0; q0 < k; q0 += 8) {
+            T vv[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) vv[q] = q0 + q < k ? V[(int64_t)(q0 + q) * ldv + i] : T(0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q0 + q < k) sv = fma(-hs[q0 + q], Acc<T>(vv[q]), sv);
+        }
         w[i] = (T)sv;
     }
 }
