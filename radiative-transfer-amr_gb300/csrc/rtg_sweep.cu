@@ -345,6 +345,16 @@ __device__ __forceinline__ T strided_dot(const T* col, int cs, const T* v, int v
     return (a0 + a1) + (a2 + a3);
 }
 
+// Stage n values of an element block (global start 16-byte aligned: element
+// offsets are padded to 4 values) with 16-byte copies and a scalar tail.
+template <typename T>
+__device__ __forceinline__ void stage_block(T* dst, const T* src, int n) {
+    constexpr int kVec = 16 / (int)sizeof(T);
+    const int nv = n / kVec;
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) cp_async16(dst + t * kVec, src + t * kVec);
+    for (int t = nv * kVec + (int)threadIdx.x; t < n; t += blockDim.x) cp_async_small<sizeof(T)>(dst + t, src + t);
+}
+
 template <typename T>
 struct UpwindMap {
     const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
@@ -420,7 +430,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             const T* Gg = um.G + um.goff[e];
             const int64_t* up = um.up + um.uoff[e];
             for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
-            for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bg + t, B + t);
+            stage_block(Bg, B, bsize);
             for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
                 const int ij = l / nth;
                 rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
@@ -485,7 +495,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         }
         const bool staged = bsize <= bcap;
         if (staged) {   // asynchronous copies: every load in flight at once
-            for (int t = threadIdx.x; t < bsize; t += blockDim.x) cp_async_small<sizeof(T)>(Bs + t, B + t);
+            stage_block(Bs, B, bsize);
         } else {
             // too large for shared memory: pull the block into L2 now (one
             // prefetch per 128-byte line, all in flight) for the products below
@@ -857,7 +867,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     // ---- element block inverses
     std::vector<int32_t> blk_elem, blk_r;
     std::vector<int64_t> blk_off, inv_off(ne);
-    int64_t off = 0;
+    int64_t off = 0, entries = 0;
     int max_nn = 1;
     for (int e = 0; e < ne; ++e) {
         const ElemDev& E = t.elems[e];
@@ -865,7 +875,11 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         const int nn = C.nx * C.ny;
         max_nn = std::max(max_nn, nn);
         s->max_nloc = std::max(s->max_nloc, nn * E.nth);
+        // each element's block starts on 4 values (16 bytes in FP32, 32 in
+        // FP64), so that the sweep stages it with 16-byte copies
+        off = (off + 3) & ~int64_t(3);
         inv_off[e] = off;
+        entries += (int64_t)E.nth * nn * nn;
         for (int r = 0; r < E.nth; ++r) {
             blk_elem.push_back(e);
             blk_r.push_back(r);
@@ -873,7 +887,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             off += (int64_t)nn * nn;
         }
     }
-    s->inv_entries = off;
+    s->inv_entries = entries;   // algorithmic entries (the padding excluded)
     s->d_lev_elems = sw_alloc<int32_t>(s, ne);
     s->d_active = sw_alloc<uint8_t>(s, active.size());
     s->d_inv_off = sw_alloc<int64_t>(s, ne);
