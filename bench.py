@@ -665,6 +665,7 @@ def run_ours(args):
                                                sample_desc="the same recipe at {} DOF (one refinement round, "
                                                            "8x8 columns of 2x2 nodes)".format(sN))
         out["adaptive_2e5"] = secondary_adaptive(args, flush, stream)
+        out["batched_256"] = batched_measure(2, 1, not args.no_cpu, cpu_instances=16)
     else:
         out["amr_indicators"] = amr_indicators(ctx, mesh, u_ref_h, stream, flush, not args.no_cpu)
         if not args.no_cpu:
@@ -697,7 +698,7 @@ def secondary_adaptive(args, flush, stream):
     return out
 
 
-def run_batched(args):
+def batched_measure(steps, warmup, with_cpu, cpu_instances=32):
     """cfg3: 256 independent instances (seeded degree, size, sigma_t, albedo,
     g) in one batched solve (method 1, one handle, graph-captured restart
     cycle), against solving the same instances one by one through rt.Problem-
@@ -706,13 +707,14 @@ def run_batched(args):
     import torch
     from rtg import DeviceContext, _lib, workloads as W
     from rtg.batch import BatchContext
-    rank = int(os.environ.get("RANK", "0"))
-    torch.cuda.set_device(0)
     nb = 256
     inst = [W.batch_instance(1000 + k) for k in range(nb)]
+    t0 = time.perf_counter()
     bc = BatchContext(inst)
     f = bc.forcing()
     g = bc.inflow()
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
     # reference solutions: tight individual FP64 solves
     ctxs = [DeviceContext(m, p.kappa, p.sigma, p.Phi) for m, p in inst]
@@ -731,13 +733,13 @@ def run_batched(args):
             break
     if rtol is None:
         raise RuntimeError("batched solve did not reach the error target")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         bc.solve(f, g, rtol=rtol, inner_rtol=1e-5)
     times = []
     launch_count = _lib.load().rtg_launch_count
     n_launch = 0
     with ClockSampler(0) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             torch.cuda.synchronize()
             e0, e1 = _events(stream)
             n0 = launch_count()
@@ -756,24 +758,39 @@ def run_batched(args):
             c.solve(fi, gi, method=1, precond=1, rtol=rtol, inner_rtol=1e-5, restart=30)
         torch.cuda.synchronize()
         seq.append(time.perf_counter() - t0)
+    for c in ctxs:
+        c.close()
+    value = statistics.median(times)
+    out = {"value": value, "unit": "s", "steps": steps, "warmup": warmup, "n_instances": nb,
+           "workload": "256 independent instances (batch_instance seeds 1000..1255)", "ndof": int(bc.N),
+           "rtol": rtol, "max_rel_err": max(errs), "error_target": ERR_TARGET, "setup_s": setup_s,
+           "sequential_one_by_one_s": min(seq), "speedup_batched_vs_sequential": min(seq) / value,
+           "iterations_max": max(i["iterations"] for i in infos), "gpu_launches": int(n_launch),
+           "clocks": clk.summary()}
+    if with_cpu:
+        # all host cores, a bounded sample of the 256 instances
+        out["cpu_baseline"] = cpu_baseline_batch(list(range(1000, 1000 + cpu_instances)), rtol, nb)
+    return out
+
+
+def run_batched(args):
+    rank = int(os.environ.get("RANK", "0"))
+    import torch
+    torch.cuda.set_device(0)
+    b = batched_measure(args.steps, args.warmup, not args.no_cpu)
     if rank != 0:
         return None
-    value = statistics.median(times)
-    ndof = int(bc.N)
-    out = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32-inner/f64-outer", "data": "synthetic (256 seeded instances)",
-            "config": {"workload": "256 independent instances (batch_instance seeds 1000..1255)", "ndof": ndof,
-                       "rtol": rtol, "max_rel_err": max(errs), "error_target": ERR_TARGET,
-                       "sequential_one_by_one_s": min(seq), "speedup_batched_vs_sequential": min(seq) / value,
-                       "iterations_max": max(i["iterations"] for i in infos)},
-            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
-                    "note": "inputs resident; the batched entry point takes device vectors"},
-            "gpu_launches": int(n_launch),
-            "clocks": clk.summary()}
-    if not args.no_cpu:
-        # all host cores, a bounded sample of 32 of the 256 instances
-        out["cpu_baseline"] = cpu_baseline_batch(list(range(1000, 1032)), rtol, nb)
+    out = {"metric": METRIC, "value": b["value"], "unit": "s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * b["value"], "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32-inner/f64-outer", "data": "synthetic (256 seeded instances)",
+           "config": {k: b[k] for k in ("workload", "ndof", "rtol", "max_rel_err", "error_target", "setup_s",
+                                        "sequential_one_by_one_s", "speedup_batched_vs_sequential",
+                                        "iterations_max")},
+           "e2e": {"value": b["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                   "note": "inputs resident; the batched entry point takes device vectors"},
+           "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
+    if "cpu_baseline" in b:
+        out["cpu_baseline"] = b["cpu_baseline"]
     return out
 
 

@@ -350,8 +350,9 @@ int rtg_error_spatial_jump(rtg_handle* h, const double* u, double* col_err2, voi
 int rtg_hp_steer(rtg_handle* h, const double* u, double* col_lp, double* cell_lp, void* stream);
 
 /* allocation-free inner products --------------------------------------------
- * No counterpart in the reference: this is the two-stage reduction rtg_solve
- * uses for its Arnoldi inner products and residual norms, offered to callers
+ * No counterpart in the reference: the kind of reduction rtg_solve uses for
+ * its Arnoldi inner products and residual norms (per-CTA partial sums added
+ * in a fixed order; its own grid, so the last bits can differ), offered to callers
  * that may not allocate device memory (a host whose memory manager owns every
  * device allocation, or a caller running its own Krylov loop around
  * rtg_apply where a cudaMalloc would stall or break the surrounding work).
@@ -364,7 +365,9 @@ int rtg_hp_steer(rtg_handle* h, const double* u, double* col_lp, double* cell_lp
  * looks up that array's device address (cudaGetSymbolAddress) with the device
  * current, so make the first call on each device before any stream capture.
  * All calls share the array: calls that overlap on the GPU race and must be
- * serialised by the caller; each call overwrites every partial sum it reads. */
+ * serialised by the caller; each call overwrites every partial sum it reads.
+ * The array's address is cached per device: do not use the library across a
+ * cudaDeviceReset. */
 int rtg_dots_noalloc(int k, const double* V, int64_t ldv, const double* w, int64_t n,
                      double* out, void* stream);
 

@@ -1798,7 +1798,10 @@ static float time_plan(rtg_handle* h, ApplyPlan* p, const T* x, T* y, cudaEvent_
     if (p->ntc) {
         int st = 0;
         RTG_CUDA(cudaMemcpy(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-        if (st) throw RtgError{RTG_ERR_TIMEOUT, "scat_tc_kernel: a wait for the tensor cores gave up"};
+        if (st) {
+            h->poisoned = true;
+            throw RtgError{RTG_ERR_TIMEOUT, "scat_tc_kernel: a wait for the tensor cores gave up"};
+        }
     }
     return tt;
 }
@@ -1931,6 +1934,17 @@ int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s) {
     return n;
 }
 
+int apply_status(rtg_handle* h, cudaStream_t s) {
+    const ApplyPlan* p = h->plan32;
+    if (h->poisoned) return RTG_ERR_TIMEOUT;
+    if (!p || !p->ntc) return RTG_OK;
+    int st = 0;
+    RTG_CUDA(cudaMemcpyAsync(&st, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RTG_CUDA(cudaStreamSynchronize(s));
+    if (st) h->poisoned = true;
+    return st ? RTG_ERR_TIMEOUT : RTG_OK;
+}
+
 void free_apply_plans(rtg_handle* h) {
     free_plan(h->plan64);
     free_plan(h->plan32);
@@ -1941,6 +1955,8 @@ template <typename T>
 void launch_apply(const rtg_handle* hc, const OpView<T>& v, uint32_t flags, const T* x, T* y,
                   cudaStream_t s) {
     rtg_handle* h = const_cast<rtg_handle*>(hc);
+    if (h->poisoned)
+        throw RtgError{RTG_ERR_TIMEOUT, "a tensor-core wait of this handle timed out earlier; destroy the handle"};
     constexpr bool f64 = sizeof(T) == 8;
     ApplyPlan*& plan = f64 ? h->plan64 : h->plan32;
     if (!plan) {

@@ -216,6 +216,11 @@ struct rtg_handle {
     // correction stays in the solve, per inner precision (0 FP64, 1 FP32):
     // 0 not run yet, 1 kept, 2 the sweep alone reduced the residual faster
     int nn_trial[2] = {0, 0};
+    // set when a bounded wait of the tensor-core scattering gave up: its
+    // copies or MMAs may still have been in flight when the CTA released its
+    // shared memory and tensor memory, so neither this handle nor the values it
+    // produced are trusted; every later apply or solve on it fails
+    bool poisoned = false;
     rtg::Coarse* coarse = nullptr;
     rtg::AmrTables* amr = nullptr;
 };
@@ -236,6 +241,9 @@ void launch_mask_vector(const rtg_handle* h, int part, const double* x, double* 
                         cudaStream_t s);
 void launch_weight_forcing(const rtg_handle* h, const double* f, double* out, cudaStream_t s);
 void free_apply_plans(rtg_handle* h);
+// RTG_ERR_TIMEOUT (and the handle poisoned) if a tensor-core wait of the FP32
+// apply gave up since the plan was built, else RTG_OK; one device read
+int apply_status(rtg_handle* h, cudaStream_t s);
 // FP32 apply autotuning table (tunes on first use): rows of [nx, ny, nth_b,
 // cap, ns per candidate cap]; returns the number of degree classes
 int apply_tuning(rtg_handle* h, int32_t* out, int cap_rows, cudaStream_t s);

@@ -958,6 +958,9 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     inf.learned_kept = (o->precond == 3 && h->nn_trial[tpi] == 1) ? 1 : 0;
     if (o->precond >= 1 && sweep_status(h, s) != RTG_OK)
         throw RtgError{RTG_ERR_TIMEOUT, "a sweep wait gave up; the solution is not valid"};
+    if (apply_status(h, s) != RTG_OK)
+        throw RtgError{RTG_ERR_TIMEOUT, "a tensor-core wait gave up; the solution is not valid and the handle "
+                                        "must be destroyed"};
     inf.res_f = res;
     inf.converged = res <= tol ? 1 : 0;
     // u = x on the unknowns, g on the inflow-boundary DOFs (rt/solve.py:163)

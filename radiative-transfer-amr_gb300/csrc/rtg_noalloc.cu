@@ -1,16 +1,18 @@
 // Allocation-free inner products: rtg_dots_noalloc.
 //
-// rtg_solve computes its Arnoldi inner products and residual norms with a
-// two-stage reduction whose first stage writes per-CTA partial sums to a
-// scratch buffer that the solver allocates on first use.  Some callers of
+// rtg_solve computes its Arnoldi inner products and residual norms from
+// per-CTA partial sums, added in a fixed order, in a scratch buffer that the
+// solver allocates on first use.  Some callers of
 // this library may not allocate device memory at all: a host application
 // whose memory manager owns every device allocation (a framework pool or a
 // fixed budget set at start-up), or a driver that wraps its own Krylov loop
 // around rtg_apply inside a region where cudaMalloc would stall or break the
 // surrounding work (a latency-critical loop, a capture of a larger pipeline).
-// For them this file provides the same reduction with its scratch in a
-// file-scope device array: the caller passes inputs and outputs, and nothing
-// is allocated.
+// For them this file provides the same kind of reduction (per-CTA partial
+// sums, then a second launch that adds them in a fixed order) with its scratch
+// in a file-scope device array: the caller passes inputs and outputs, and
+// nothing is allocated.  Its grid and summation order are its own, so results
+// can differ from the solver's in the last bits.
 //
 // Scratch: kNaBlocks x kNaMaxVectors doubles (296 x 64 x 8 B = 151,552 B) in
 // g_noalloc_partial.  Every GPU that loads the library holds it until the
@@ -18,6 +20,10 @@
 // streams, or two host threads) race on it and must be serialised by the
 // caller.  Each call overwrites every partial sum it later reads, so no state
 // from an earlier call survives into a result and nothing needs zeroing.
+// The array's device address is cached per device for the life of the
+// process: a cudaDeviceReset while the library is in use invalidates it (the
+// module is reloaded at a new address), so the library must not be used
+// across a reset.
 #include <mutex>
 
 #include "rtg_internal.h"

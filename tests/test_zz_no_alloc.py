@@ -3,7 +3,8 @@
 Callers that may not allocate device memory (a host whose memory manager owns
 every device allocation, or a caller running its own Krylov loop around
 rtg_apply where cudaMalloc would stall or break the surrounding work) get the
-solver's inner-product reduction with its scratch in a static device array.
+solver's kind of inner-product reduction with its scratch in a static device
+array.
 This test checks it against the norms the existing entry point rtg_solve
 reports for the same vectors (||b|| and the final true residual ||b - A x||),
 on two calls in a row.  The file is collected last so that a run stopping at
@@ -83,3 +84,25 @@ def test_noalloc_rejects_sizes_beyond_maximum():
                               C.c_void_p(out.data_ptr()), None)
     assert rc == _lib.RTG_ERR_SIZE
     assert b"[1, 64]" in lib.rtg_last_error()
+
+
+@pytest.mark.parametrize("k,pad", [(9, 0), (17, 5), (64, 3)])
+def test_noalloc_many_vectors(k, pad):
+    """Vector counts that exercise a last group of fewer than eight, several
+    groups, and the whole 64-wide scratch row, with rows ldv = n + pad apart;
+    two calls in a row against torch's V @ w."""
+    import torch
+    from rtg import _lib
+    lib = _lib.load()
+    n = 100003
+    gen = torch.Generator(device="cuda").manual_seed(k)
+    Vp = torch.randn(k, n + pad, dtype=torch.float64, device="cuda", generator=gen)
+    w = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
+    ref = (Vp[:, :n] @ w).cpu().numpy()
+    out = torch.empty(k, dtype=torch.float64, device="cuda")
+    for call in range(2):
+        out.fill_(float("nan"))
+        _lib.check(lib.rtg_dots_noalloc(k, C.c_void_p(Vp.data_ptr()), n + pad, C.c_void_p(w.data_ptr()), n,
+                                        C.c_void_p(out.data_ptr()), None))
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-12 * np.sqrt(n) * 4)
