@@ -64,75 +64,63 @@ def parse():
     ap.add_argument("--workload", default="cfg5", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
-                    help="short run for ncu: two solves per method (learned+mixed, mixed, plain), "
-                         "then 3 FP32 and 3 FP64 applies and sweeps")
+                    help="short run for ncu: each solve method, apply and sweep once in an NVTX range")
+    ap.add_argument("--scale", type=float, default=1.0, help="profile mode: two-scatterer recipe scale")
     ap.add_argument("--rtol", type=float, default=1e-9, help="profile mode: solver tolerance")
-    ap.add_argument("--max-it", type=int, default=20000, help="profile mode: iteration cap")
+    ap.add_argument("--max-it", type=int, default=3000, help="profile mode: iteration cap")
     return ap.parse_args()
 
 
 def run_profile(args):
-    """Minimal launch sequence for profiling: set-up, then per method one warm
-    and one measured solve, then three FP32 and three FP64 system applies."""
+    """Launch sequence for ncu: set-up and one warm-up of each piece, then each
+    piece once inside an NVTX range named after it -- solve_learned,
+    solve_mixed, solve_plain (one solve to --rtol each), apply_fp32,
+    sweep_fp32, apply_fp64, sweep_fp64 -- so that ncu --nvtx --nvtx-include
+    "<name>/" captures exactly one piece.  --scale < 1 takes the two-scatterer
+    recipe with fewer refinement rounds (a smaller case of the same kernels)."""
     import torch
-    from rtg import Problem, _lib
+    from rtg import Problem, _lib, learned as LN, workloads as W
     torch.cuda.set_device(0)
-    out = {}
-    t0 = time.perf_counter()
-    desc, mesh, spec = workload(args.workload)
-    out["mesh_s"] = time.perf_counter() - t0
+    if args.workload == "cfg5" and args.scale < 1.0:
+        mesh, spec = W.config5_mesh(scale=args.scale), W.two_disc_problem()
+    else:
+        _, mesh, spec = workload(args.workload)
     prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
-    t0 = time.perf_counter()
     ctx = prob.context(mesh)
-    torch.cuda.synchronize()
-    out["context_s"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
+    LN.set_params(ctx, LN.load(LN.DEFAULT_NET)[0])
     f_dev = ctx.forcing(spec.f)
     g_dev = ctx.inflow(spec.bcs_dirac)
+    fl = _lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS
+    x32 = torch.randn(ctx.N, dtype=torch.float32, device=ctx.device)
+    y32 = torch.empty_like(x32)
+    x64 = torch.randn(ctx.N, dtype=torch.float64, device=ctx.device)
+    y64 = torch.empty_like(x64)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=ctx.device)
+    pieces = [("solve_learned", lambda: ctx.solve(f_dev, g_dev, method=1, precond=3, rtol=args.rtol,
+                                                  max_it=args.max_it, restart=30, inner_rtol=1e-5)),
+              ("solve_mixed", lambda: ctx.solve(f_dev, g_dev, method=1, precond=1, rtol=args.rtol,
+                                                max_it=args.max_it, restart=30, inner_rtol=1e-5)),
+              ("solve_plain", lambda: ctx.solve(f_dev, g_dev, method=0, precond=1, rtol=args.rtol,
+                                                max_it=args.max_it, restart=30)),
+              ("apply_fp32", lambda: ctx.apply(fl, x32, y32, prec=_lib.RTG_FP32)),
+              ("sweep_fp32", lambda: ctx.precondition(x32, y32, prec=_lib.RTG_FP32)),
+              ("apply_fp64", lambda: ctx.apply(fl, x64, y64, prec=_lib.RTG_FP64)),
+              ("sweep_fp64", lambda: ctx.precondition(x64, y64, prec=_lib.RTG_FP64))]
+    out = {"ndof": ctx.N, "info": ctx.info}
+    for name, fn in pieces:
+        fn()
     torch.cuda.synchronize()
-    out["vectors_s"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    ctx.precondition(torch.zeros(ctx.N, dtype=torch.float64, device=ctx.device))
-    torch.cuda.synchronize()
-    out["sweep_setup_s"] = time.perf_counter() - t0
-    print(json.dumps({k: out[k] for k in out}), file=sys.stderr, flush=True)
-    from rtg import learned as LN
-    LN.set_params(ctx, LN.load(LN.DEFAULT_NET)[0])
-    # learned+mixed (the headline method), mixed, plain FP64
-    for name, method, pc in (("learned_mixed", 1, 3), ("mixed", 1, 1), ("plain_fp64", 0, 1)):
-        for rep in range(2):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            u, info = ctx.solve(f_dev, g_dev, method=method, rtol=args.rtol, max_it=args.max_it, precond=pc,
-                                restart=30, inner_rtol=1e-5)
-            torch.cuda.synchronize()
-            out["%s_rep%d" % (name, rep)] = {"s": time.perf_counter() - t0,
-                                             "iterations": info["iterations"],
-                                             "sweeps": info["sweeps"],
-                                             "res_f": info["res_f"], "rhs_norm": info["rhs_norm"],
-                                             "converged": info["converged"]}
-            print(json.dumps(out["%s_rep%d" % (name, rep)]), file=sys.stderr, flush=True)
-    stream = torch.cuda.current_stream()
-    for prec in (_lib.RTG_FP32, _lib.RTG_FP64):
-        dt = torch.float32 if prec == _lib.RTG_FP32 else torch.float64
-        nm = "fp32" if prec == _lib.RTG_FP32 else "fp64"
-        x = torch.randn(ctx.N, dtype=dt, device=ctx.device)
-        y = torch.empty_like(x)
-        for what, fn in (("apply", lambda: ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, x, y, prec=prec)),
-                         ("sweep", lambda: ctx.precondition(x, y, prec=prec))):
-            fn()
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(3):
-                fn()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            out["%s_%s_us" % (what, nm)] = 1e3 * e0.elapsed_time(e1) / 3
-    torch.cuda.synchronize()
-    out["ndof"] = ctx.N
-    out["info"] = ctx.info
+    for name, fn in pieces:
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push(name)
+        r = fn()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        out[name + "_s"] = time.perf_counter() - t0
+        if name.startswith("solve"):
+            out[name + "_iterations"] = r[1]["iterations"]
     print(json.dumps(out))
 
 
