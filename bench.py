@@ -109,6 +109,9 @@ def run_profile(args):
     out = {"ndof": ctx.N, "info": ctx.info}
     for name, fn in pieces:
         fn()
+    out["sweep_bytes_fp32"] = sweep_bytes(ctx, 4)[0]
+    out["sweep_bytes_fp64"] = sweep_bytes(ctx, 8)[0]
+    out["w_bytes_fp32"] = w_bytes_fp32(ctx)
     torch.cuda.synchronize()
     for name, fn in pieces:
         flush.fill_(1.0)
