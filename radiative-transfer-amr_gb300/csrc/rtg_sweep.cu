@@ -36,7 +36,9 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse (2 CTAs per SM)
-constexpr size_t kSweepSmemSmall = 72 * 1024;    // the alternative the first sweep also times (3 CTAs per SM)
+constexpr size_t kSweepSmemSmall = 72 * 1024;    // the alternatives the first sweep also times (3 CTAs per SM)
+constexpr size_t kSweepSmemTiny = 54 * 1024;     // ... and 4 CTAs per SM (the register limit): more copies in flight
+constexpr int kSweepShapes = 3;
 constexpr int kMaxCplStaged = 32;               // active couplings staged per element
 constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
@@ -750,15 +752,15 @@ struct Sweep {
     int64_t inv_entries = 0;
     int max_nloc = 0;
     int64_t max_b = 0, max_c = 0;
-    // launch shapes per precision (0 FP32, 1 FP64): two shared-memory budgets,
-    // the faster one chosen by timing the first sweep of the handle
+    // launch shapes per precision (0 FP32, 1 FP64): kSweepShapes shared-memory
+    // budgets, the fastest chosen by timing the first sweep of the handle
     struct Shape {
         size_t smem = 0;
         int bcap = 0, grid = 0, reg_cap = 0;
     };
-    Shape shape[2][2];
+    Shape shape[2][kSweepShapes];
     int pick[2] = {-1, -1};
-    float shape_ms[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    float shape_ms[2][kSweepShapes] = {};
     int32_t *d_greg32 = nullptr, *d_greg64 = nullptr;
     int n_lagged = 0;
     std::vector<void*> allocs;
@@ -1059,8 +1061,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         int dev = 0, nsm = 0;
         RTG_CUDA(cudaGetDevice(&dev));
         RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        const size_t budgets[2] = {kSweepSmemBudget, kSweepSmemSmall};
-        for (int q = 0; q < 2; ++q) {
+        const size_t budgets[kSweepShapes] = {kSweepSmemBudget, kSweepSmemSmall, kSweepSmemTiny};
+        for (int q = 0; q < kSweepShapes; ++q) {
             Sweep::Shape& sh = s->shape[pi][q];
             const size_t budget = budgets[q];
             const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
@@ -1075,11 +1077,11 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
                                                                    sh.smem));
             sh.grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
         }
-        // time both (after one warm-up each); the smaller budget must win by 3 %
+        // time each (after one warm-up); a smaller budget must win by 3 %
         cudaEvent_t e0, e1;
         RTG_CUDA(cudaEventCreate(&e0));
         RTG_CUDA(cudaEventCreate(&e1));
-        for (int q = 0; q < 2; ++q) {
+        for (int q = 0; q < kSweepShapes; ++q) {
             float best = 1e30f;
             for (int rep = 0; rep < 3; ++rep) {
                 sweep_fill_kernel<T><<<std::max(1, std::min((int)h->host.elems.size(), 152 * 8)), 256, 0, st>>>(
@@ -1096,7 +1098,10 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        s->pick[pi] = s->shape_ms[pi][1] < 0.97f * s->shape_ms[pi][0] ? 1 : 0;
+        int best_q = 0;
+        for (int q = 1; q < kSweepShapes; ++q)
+            if (s->shape_ms[pi][q] < 0.97f * s->shape_ms[pi][best_q]) best_q = q;
+        s->pick[pi] = best_q;
         // the real sweep below starts from a fresh fill
         sweep_fill_kernel<T><<<std::max(1, std::min((int)h->host.elems.size(), 152 * 8)), 256, 0, st>>>(
             v, (int)h->host.elems.size(), z, s->d_next), count_launch();
