@@ -38,7 +38,12 @@ constexpr int kSweepThreads = 256;
 constexpr size_t kSweepSmemBudget = 110 * 1024;  // rhs + prefetched block inverse (2 CTAs per SM)
 constexpr size_t kSweepSmemSmall = 72 * 1024;    // the alternatives the first sweep also times (3 CTAs per SM)
 constexpr size_t kSweepSmemTiny = 54 * 1024;     // ... and 4 CTAs per SM (the register limit): more copies in flight
-constexpr int kSweepShapes = 3;
+constexpr int kSweepShapes = 5;
+// the shapes the first sweep times: (threads per CTA, shared-memory budget);
+// the 128-thread CTAs fit 6 or 8 per SM, each staging one element
+constexpr int kShapeThreads[kSweepShapes] = {kSweepThreads, kSweepThreads, kSweepThreads, 128, 128};
+constexpr size_t kShapeBudget[kSweepShapes] = {kSweepSmemBudget, kSweepSmemSmall, kSweepSmemTiny, 36 * 1024,
+                                               27 * 1024};
 constexpr int kMaxCplStaged = 32;               // active couplings staged per element
 constexpr int kMaxBlock = 100;  // nx*ny supported by the element-block inverse
 
@@ -756,7 +761,7 @@ struct Sweep {
     // budgets, the fastest chosen by timing the first sweep of the handle
     struct Shape {
         size_t smem = 0;
-        int bcap = 0, grid = 0, reg_cap = 0;
+        int bcap = 0, grid = 0, reg_cap = 0, threads = kSweepThreads;
     };
     Shape shape[2][kSweepShapes];
     int pick[2] = {-1, -1};
@@ -1050,21 +1055,22 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
     auto launch = [&](const Sweep::Shape& sh) {
         um.reg_cap = sh.reg_cap;
-        sweep_persistent_kernel<T><<<sh.grid, kSweepThreads, sh.smem, st>>>(
+        sweep_persistent_kernel<T><<<sh.grid, sh.threads, sh.smem, st>>>(
             v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next,
             s->d_status, um, rhs_cap, sh.bcap, (int)s->max_c, trace), count_launch();
     };
     if (s->pick[pi] < 0) {
-        // the two launch shapes: larger per-CTA shared memory (more one-phase
-        // elements and staged blocks, 2 CTAs per SM) or smaller (3 CTAs per
-        // SM, for meshes whose levels hold many elements)
+        // the launch shapes: larger per-CTA shared memory (more one-phase
+        // elements and staged blocks, fewer CTAs per SM) or smaller (more
+        // CTAs per SM and so more element stagings in flight, for meshes whose
+        // levels hold many elements; the sweep is throughput bound there)
         int dev = 0, nsm = 0;
         RTG_CUDA(cudaGetDevice(&dev));
         RTG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        const size_t budgets[kSweepShapes] = {kSweepSmemBudget, kSweepSmemSmall, kSweepSmemTiny};
         for (int q = 0; q < kSweepShapes; ++q) {
             Sweep::Shape& sh = s->shape[pi][q];
-            const size_t budget = budgets[q];
+            const size_t budget = kShapeBudget[q];
+            sh.threads = kShapeThreads[q];
             const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
             const int64_t fit = (int64_t)((budget - std::min(rhs_bytes, budget)) / sizeof(T));
             sh.bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
@@ -1073,7 +1079,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
             sh.smem = sizeof(T) * (size_t)(2 * rhs_cap + std::max<int64_t>((int64_t)sh.bcap + s->max_c, gmax));
             raise_smem_limit((const void*)sweep_persistent_kernel<T>, sh.smem);
             int per_sm = 0;
-            RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, kSweepThreads,
+            RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent_kernel<T>, sh.threads,
                                                                    sh.smem));
             sh.grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
         }
