@@ -25,6 +25,8 @@
 // cross-cell scattering is left to the Krylov iteration.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <map>
 #include <queue>
 #include <vector>
 
@@ -871,22 +873,43 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     for (int e = 0; e < ne; ++e)
         for (int k = t.elems[e].cpl_begin; k < t.elems[e].cpl_end; ++k)
             active[k] = level[t.cpls[k].nbr] < level[e] ? 1 : 0;
-    // ---- element block inverses
+    // ---- element block inverses.  An element's blocks are a function of its
+    // node counts, face and boundary flags, extinction and streaming constants,
+    // angular table and the column's wx wy kappa values (what
+    // build_block_inverse_kernel reads); elements that agree on the bits of
+    // all of them share one copy (the sweep reaches blocks through
+    // inv_elem_off), so they are built and stored once.
     std::vector<int32_t> blk_elem, blk_r;
     std::vector<int64_t> blk_off, inv_off(ne);
     int64_t off = 0, entries = 0;
     int max_nn = 1;
+    std::map<std::vector<uint64_t>, int64_t> shared;
+    auto bits = [](double x) {
+        uint64_t u;
+        std::memcpy(&u, &x, sizeof(u));
+        return u;
+    };
     for (int e = 0; e < ne; ++e) {
         const ElemDev& E = t.elems[e];
         const ColDev& C = t.cols[E.col];
         const int nn = C.nx * C.ny;
         max_nn = std::max(max_nn, nn);
         s->max_nloc = std::max(s->max_nloc, nn * E.nth);
-        // each element's block starts on 4 values (16 bytes in FP32, 32 in
+        entries += (int64_t)E.nth * nn * nn;
+        std::vector<uint64_t> key = {(uint64_t)C.nx, (uint64_t)C.ny, (uint64_t)E.nth, (uint64_t)E.flags};
+        for (int q = 0; q < 3; ++q) key.push_back(bits(t.econst[4 * (size_t)e + q]));
+        for (int q = 0; q < 7 * E.nth; ++q) key.push_back(bits(t.ang[(size_t)E.ang + q]));
+        for (int q = 0; q < nn; ++q) key.push_back(bits(t.kw[(size_t)C.node_off + q]));
+        auto hit = shared.find(key);
+        if (hit != shared.end()) {
+            inv_off[e] = hit->second;
+            continue;
+        }
+        // each distinct block set starts on 4 values (16 bytes in FP32, 32 in
         // FP64), so that the sweep stages it with 16-byte copies
         off = (off + 3) & ~int64_t(3);
         inv_off[e] = off;
-        entries += (int64_t)E.nth * nn * nn;
+        shared.emplace(std::move(key), off);
         for (int r = 0; r < E.nth; ++r) {
             blk_elem.push_back(e);
             blk_r.push_back(r);
