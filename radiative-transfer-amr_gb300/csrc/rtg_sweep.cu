@@ -967,13 +967,17 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         max_c = std::max(max_c, c);
     }
     s->max_c = max_c;
-    // ---- upwind maps of the elements whose map fits in shared memory
+    // ---- upwind maps of the elements whose map fits in shared memory.  A map
+    // is a function of the element's (shared) block inverses and of its active
+    // couplings' faces, sizes, mortars and dcoeff; elements that agree on them
+    // share one stored map (built once, by the first of them).
     {
         const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
         std::vector<uint8_t> gok(ne, 0);
         std::vector<int32_t> gnup(ne, 0), gel, greg32(ne, 0), greg64(ne, 0);
         std::vector<int64_t> goff64(ne, 0), goff32(ne, 0), uoff(ne, 0), up;
         int64_t gtot64 = 0, gtot32 = 0;
+        std::map<std::vector<uint64_t>, std::pair<int64_t, int64_t>> gshared;
         for (int e = 0; e < ne; ++e) {
             const ElemDev& E = t.elems[e];
             const ColDev& C = t.cols[E.col];
@@ -994,11 +998,27 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             gnup[e] = (int32_t)nup;
             greg32[e] = (int32_t)region32;
             greg64[e] = (int32_t)region64;
-            goff64[e] = gtot64;
-            goff32[e] = gtot32;
             uoff[e] = (int64_t)up.size();
-            gtot64 += ld64 * nloc;
-            gtot32 += ld32 * nloc;
+            std::vector<uint64_t> gkey = {(uint64_t)inv_off[e], (uint64_t)E.nth, (uint64_t)E.flags};
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                if (!active[k]) continue;
+                const CplGeo& g = t.cgeo[k];
+                const CplDev& cp = t.cpls[k];
+                gkey.insert(gkey.end(), {(uint64_t)cp.face, (uint64_t)g.m1, (uint64_t)g.nth1, (uint64_t)cp.es,
+                                         (uint64_t)cp.et, bits(t.cplc[k])});
+            }
+            auto ghit = gshared.find(gkey);
+            const bool built = ghit == gshared.end();
+            if (built) {
+                goff64[e] = gtot64;
+                goff32[e] = gtot32;
+                gshared.emplace(std::move(gkey), std::make_pair(gtot64, gtot32));
+                gtot64 += ld64 * nloc;
+                gtot32 += ld32 * nloc;
+            } else {
+                goff64[e] = ghit->second.first;
+                goff32[e] = ghit->second.second;
+            }
             for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
                 if (!active[k]) continue;
                 const CplGeo& g = t.cgeo[k];
@@ -1012,7 +1032,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
                     s->g_read[p] += (p ? ld64 : ld32) * nloc;
                     s->up_read[p] += nup;
                 }
-            gel.push_back(e);
+            if (built) gel.push_back(e);
         }
         s->g_entries = gtot64 + gtot32;
         s->d_gok = sw_alloc<uint8_t>(s, ne);
