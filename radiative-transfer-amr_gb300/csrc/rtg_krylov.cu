@@ -391,6 +391,9 @@ struct Workspace {
     // (device loop) or in hlast (host loop)
     int last_j = 0;
     bool last_on_device = false;
+    // per column: 1 when its rows of A mask_B g are zero for every g (neither
+    // it nor a face neighbour holds an inflow-boundary node)
+    int32_t* rhs_skip = nullptr;
     std::vector<double> hlast;
     std::vector<void*> allocs;
 };
@@ -855,9 +858,35 @@ int solve(rtg_handle* h, const double* f, const double* g, double* u, const rtg_
     rtg_solve_info inf{};
     std::vector<double> hv;
 
-    // b = mask_I (f - A mask_B g)     (rt/solve.py:98-101)
+    // b = mask_I (f - A mask_B g)     (rt/solve.py:98-101).  mask_B g is zero
+    // outside the inflow-boundary nodes, so only their columns and the
+    // columns facing them get nonzero rows: the apply runs on those alone
+    // (the same kernels, the same bits) into a zeroed t.
+    if (!ws->rhs_skip) {
+        const HostTables& t = h->host;
+        const int nc = (int)t.cols.size();
+        std::vector<char> inflow(nc, 0);
+        for (const ElemDev& E : t.elems)
+            if (E.flags >> 4) inflow[E.col] = 1;
+        std::vector<int32_t> skip(nc, 1);
+        for (int c = 0; c < nc; ++c) {
+            bool need = inflow[c];
+            for (int q = 0; q < 8 && !need; ++q) {
+                const int nb = t.col_nbr8[(size_t)8 * c + q];
+                need = nb >= 0 && inflow[nb];
+            }
+            skip[c] = need ? 0 : 1;
+        }
+        ws->rhs_skip = dalloc<int32_t>(ws, nc);
+        RTG_CUDA(cudaMemcpy(ws->rhs_skip, skip.data(), sizeof(int32_t) * nc, cudaMemcpyHostToDevice));
+    }
     launch_mask_vector(h, 1, g, ws->gb, s);
-    launch_apply<double>(h, h->v64, RTG_SYSTEM | RTG_MASK_ROWS, ws->gb, ws->t, s);
+    RTG_CUDA(cudaMemsetAsync(ws->t, 0, sizeof(double) * N, s));
+    {
+        OpView<double> vb = h->v64;
+        vb.skip = ws->rhs_skip;
+        launch_apply<double>(h, vb, RTG_SYSTEM | RTG_MASK_ROWS, ws->gb, ws->t, s);
+    }
     inf.fp64_applies++;
     launch_mask_vector(h, 0, f, ws->b, s);
     axpby_kernel<double, double><<<grid_for(N), 256, 0, s>>>(-1., ws->t, 1., ws->b, N), count_launch();
