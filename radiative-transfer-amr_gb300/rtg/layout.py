@@ -152,21 +152,31 @@ class MeshLayout:
         return out
 
     def node_coords(self):
-        """(x, y, th) of every DOF in global order."""
-        X = np.empty(self.N)
-        Y = np.empty(self.N)
-        T = np.empty(self.N)
-        for e in range(self.nelem):
-            ci = int(self.elem_col[e])
-            xx, yy = self.col_nodes(ci)
-            th = self.cell_nodes(e)
-            nx, ny, nt = len(xx), len(yy), len(th)
-            o = int(self.elem_off[e])
-            sl = slice(o, o + nx * ny * nt)
-            X[sl] = np.repeat(xx, ny * nt)
-            Y[sl] = np.tile(np.repeat(yy, nt), nx)
-            T[sl] = np.tile(th, nx * ny)
-        return X, Y, T
+        """(x, y, th) of every DOF in global order (beta = nth ny i + nth j + a
+        within an element), computed once per layout: elements of equal
+        (nx, ny, nth) are pushed forward together."""
+        if getattr(self, "_coords", None) is None:
+            X = np.empty(self.N)
+            Y = np.empty(self.N)
+            T = np.empty(self.N)
+            cols = self.elem_col
+            shape = np.stack([self.col_ndofs[cols, 0], self.col_ndofs[cols, 1], self.cell_ndof], axis=1)
+            for nx, ny, nt in np.unique(shape, axis=0):
+                es = np.nonzero((shape[:, 0] == nx) & (shape[:, 1] == ny) & (shape[:, 2] == nt))[0]
+                ci = cols[es]
+                xx = push(self.col_pos[ci, 0][:, None], self.col_pos[ci, 2][:, None], quad(0, int(nx))[0][None, :])
+                yy = push(self.col_pos[ci, 1][:, None], self.col_pos[ci, 3][:, None], quad(0, int(ny))[0][None, :])
+                th = push(self.cell_pos[es, 0][:, None], self.cell_pos[es, 1][:, None], quad(1, int(nt))[0][None, :])
+                n = int(nx * ny * nt)
+                idx = self.elem_off[es][:, None] + np.arange(n)[None, :]
+                full = (len(es), int(nx), int(ny), int(nt))
+                X[idx] = np.broadcast_to(xx[:, :, None, None], full).reshape(len(es), n)
+                Y[idx] = np.broadcast_to(yy[:, None, :, None], full).reshape(len(es), n)
+                T[idx] = np.broadcast_to(th[:, None, None, :], full).reshape(len(es), n)
+            for a in (X, Y, T):
+                a.setflags(write=False)
+            self._coords = (X, Y, T)
+        return self._coords
 
     def signatures(self):
         """Distinct column angular meshes: col_sig[ci] and, per signature, the
