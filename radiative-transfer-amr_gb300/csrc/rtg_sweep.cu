@@ -26,8 +26,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <map>
 #include <queue>
+#include <unordered_map>
 #include <vector>
 
 #include "rtg_internal.h"
@@ -199,6 +199,18 @@ __global__ void build_block_inverse_kernel(OpView<float> v, const int32_t* __res
 constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
 constexpr int kMaxFaceNodes = 4 * kMaxNodes;
 constexpr int kTr = 8;   // trace entries per element
+
+// hash of a key of 64-bit words (the bits of an element's block inputs)
+struct WordsHash {
+    size_t operator()(const std::vector<uint64_t>& v) const {
+        uint64_t h = 1469598103934665603ull;
+        for (uint64_t w : v) {
+            h ^= w + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+            h *= 1099511628211ull;
+        }
+        return (size_t)h;
+    }
+};
 
 
 __device__ __forceinline__ float from_bits_f(unsigned int u) { return __uint_as_float(u); }
@@ -883,7 +895,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     std::vector<int64_t> blk_off, inv_off(ne);
     int64_t off = 0, entries = 0;
     int max_nn = 1;
-    std::map<std::vector<uint64_t>, int64_t> shared;
+    std::unordered_map<std::vector<uint64_t>, int64_t, WordsHash> shared;
+    shared.reserve((size_t)ne);
     auto bits = [](double x) {
         uint64_t u;
         std::memcpy(&u, &x, sizeof(u));
@@ -977,7 +990,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         std::vector<int32_t> gnup(ne, 0), gel, greg32(ne, 0), greg64(ne, 0);
         std::vector<int64_t> goff64(ne, 0), goff32(ne, 0), uoff(ne, 0), up;
         int64_t gtot64 = 0, gtot32 = 0;
-        std::map<std::vector<uint64_t>, std::pair<int64_t, int64_t>> gshared;
+        std::unordered_map<std::vector<uint64_t>, std::pair<int64_t, int64_t>, WordsHash> gshared;
+        gshared.reserve((size_t)ne);
         for (int e = 0; e < ne; ++e) {
             const ElemDev& E = t.elems[e];
             const ColDev& C = t.cols[E.col];
