@@ -530,41 +530,78 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             const int ij = l / nth;
             rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
         }
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            // warp 0: the active couplings in order, one lane each (their
+            // metadata loads in flight together), compacted by ballot with a
+            // prefix sum of their staging sizes; then the face nodes that have
+            // active couplings, in ascending order, 32 nodes at a time
+            const int lane = threadIdx.x;
             int nc = 0, off = 0, fm = 0;
-            for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
-                if (!active[k]) continue;
-                fm |= 1 << v.cpls[k].face;
-                if (nc >= kMaxCplStaged) {
-                    off = ccap + 1;   // too many: read from global memory
-                    continue;
+            bool over = false;
+            for (int k0 = E.cpl_begin; k0 < E.cpl_end; k0 += 32) {
+                const int k = k0 + lane;
+                const bool act = k < E.cpl_end && active[k];
+                int F = 0, n0 = 0, sz = 0;
+                CplGeo g{};
+                if (act) {
+                    F = v.cpls[k].face;
+                    g = v.cgeo[k];
+                    n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    sz = g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1 + g.m1 * nth;
                 }
-                const CplGeo g = v.cgeo[k];
-                const int F = v.cpls[k].face;
-                const int n0 = (F % 2 == 0) ? C.ny : C.nx;
-                s_k[nc] = k;
-                s_off[nc] = off;
-                s_F[nc] = F;
-                s_m1[nc] = g.m1;
-                s_nt1[nc] = g.nth1;
-                s_n0[nc] = n0;
-                s_str[nc] = g.stride;
-                s_base[nc] = g.base;
-                s_dc[nc] = v.cplc[k];
-                off += g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1 + g.m1 * nth;
-                ++nc;
+                const unsigned am = __ballot_sync(0xffffffffu, act);
+                int fbit = act ? 1 << F : 0;
+                for (int o = 16; o > 0; o >>= 1) fbit |= __shfl_xor_sync(0xffffffffu, fbit, o);
+                fm |= fbit;
+                int incl = sz;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const int pos = nc + __popc(am & ((1u << lane) - 1u));
+                if (act) {
+                    if (pos >= kMaxCplStaged) {
+                        over = true;   // too many: read from global memory
+                    } else {
+                        s_k[pos] = k;
+                        s_off[pos] = off + incl - sz;
+                        s_F[pos] = F;
+                        s_m1[pos] = g.m1;
+                        s_nt1[pos] = g.nth1;
+                        s_n0[pos] = n0;
+                        s_str[pos] = g.stride;
+                        s_base[pos] = g.base;
+                        s_dc[pos] = v.cplc[k];
+                    }
+                }
+                nc += __popc(am);
+                off += __shfl_sync(0xffffffffu, incl, 31);
             }
-            s_off[nc] = off;
-            s_nc = (off <= ccap) ? nc : -1;   // -1: read from global memory
+            over = __any_sync(0xffffffffu, over);
+            if (lane == 0) {
+                if (over) {
+                    s_off[kMaxCplStaged] = ccap + 1;
+                    s_nc = -1;
+                } else {
+                    s_off[nc] = off;
+                    s_nc = (off <= ccap) ? nc : -1;   // -1: read from global memory
+                }
+            }
             int nf = 0;
-            for (int ij = 0; ij < nn && nf < kMaxFaceNodes; ++ij) {
-                const int i = ij / C.ny, j = ij % C.ny;
-                if (bdry_node_s(bm, i, j, C.nx, C.ny)) continue;
+            for (int ij0 = 0; ij0 < nn; ij0 += 32) {
+                const int ij = ij0 + lane;
                 bool hit = false;
-                for (int F = 0; F < 4; ++F) hit |= ((fm >> F) & 1) && on_face(F, i, j, C.nx, C.ny);
-                if (hit) s_face[nf++] = ij;
+                if (ij < nn) {
+                    const int i = ij / C.ny, j = ij % C.ny;
+                    if (!bdry_node_s(bm, i, j, C.nx, C.ny))
+                        for (int F = 0; F < 4; ++F) hit |= ((fm >> F) & 1) && on_face(F, i, j, C.nx, C.ny);
+                }
+                const unsigned hm = __ballot_sync(0xffffffffu, hit);
+                const int p = nf + __popc(hm & ((1u << lane) - 1u));
+                if (hit && p < kMaxFaceNodes) s_face[p] = ij;
+                nf += __popc(hm);
             }
-            s_nf = nf;
+            if (lane == 0) s_nf = min(nf, kMaxFaceNodes);
         }
         __syncthreads();
         const int ncs = s_nc, nf = s_nf;
