@@ -412,6 +412,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     // metadata of the staged couplings (read on the critical path)
     __shared__ int s_F[kMaxCplStaged], s_m1[kMaxCplStaged], s_nt1[kMaxCplStaged], s_n0[kMaxCplStaged];
     __shared__ int s_str[kMaxCplStaged];
+    __shared__ int s_es[kMaxCplStaged], s_et[kMaxCplStaged];
     __shared__ long long s_base[kMaxCplStaged];
     __shared__ T s_dc[kMaxCplStaged];
     if (v.stop && *v.stop) return;
@@ -543,8 +544,10 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 const bool act = k < E.cpl_end && active[k];
                 int F = 0, n0 = 0, sz = 0;
                 CplGeo g{};
+                CplDev cp{};
                 if (act) {
-                    F = v.cpls[k].face;
+                    cp = v.cpls[k];
+                    F = cp.face;
                     g = v.cgeo[k];
                     n0 = (F % 2 == 0) ? C.ny : C.nx;
                     sz = g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1 + g.m1 * nth;
@@ -570,6 +573,8 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                         s_nt1[pos] = g.nth1;
                         s_n0[pos] = n0;
                         s_str[pos] = g.stride;
+                        s_es[pos] = cp.es;
+                        s_et[pos] = cp.et;
                         s_base[pos] = g.base;
                         s_dc[pos] = v.cplc[k];
                     }
@@ -605,14 +610,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         }
         __syncthreads();
         const int ncs = s_nc, nf = s_nf;
+        // the staged couplings' mortars, from the metadata warp 0 gathered
+        // (asynchronous copies, waited on with the block inverse's)
         for (int c = 0; c < ncs; ++c) {
-            const int k = s_k[c];
-            const CplDev cp = v.cpls[k];
-            const CplGeo g = v.cgeo[k];
-            const int n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+            const int m1 = s_m1[c], n0 = s_n0[c], nt1 = s_nt1[c];
             T* dst = cs + s_off[c];
-            for (int t = threadIdx.x; t < g.m1 * n0; t += blockDim.x) dst[t] = __ldg(v.mort + cp.es + t);
-            for (int t = threadIdx.x; t < g.nth1 * nth; t += blockDim.x) dst[g.m1 * n0 + t] = __ldg(v.mort + cp.et + t);
+            const T* es = v.mort + s_es[c];
+            const T* et = v.mort + s_et[c];
+            for (int t = threadIdx.x; t < m1 * n0; t += blockDim.x) cp_async_small<sizeof(T)>(dst + t, es + t);
+            for (int t = threadIdx.x; t < nt1 * nth; t += blockDim.x)
+                cp_async_small<sizeof(T)>(dst + m1 * n0 + t, et + t);
         }
         cp_async_wait_all();
         __syncthreads();
