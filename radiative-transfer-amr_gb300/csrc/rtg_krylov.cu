@@ -244,6 +244,194 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
     if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// Sixteen bytes of T: the unit of the vectorised Gram-Schmidt kernels (one
+// 128-bit load or store per basis vector and thread).
+template <typename T>
+struct alignas(16) Pack {
+    static constexpr int n = 16 / (int)sizeof(T);
+    T v[n];
+};
+
+template <typename T>
+__device__ __forceinline__ Pack<T> load_pack(const T* p) {
+    return *reinterpret_cast<const Pack<T>*>(p);
+}
+
+// Partial sums of one block (outputs q < nout, every thread's acc[q]) to
+// partial[block * nout + q], then the last block to finish adds the blocks'
+// partials in block order (the result does not depend on the schedule),
+// writes out (and out_sum = out + add when add is given), runs the Arnoldi
+// update after a norm pass that carries one, and resets the ticket.
+template <typename T, int NO>
+__device__ __forceinline__ void block_reduce_out(const T (&acc)[NO], int nout, double* __restrict__ partial,
+                                                 unsigned int* __restrict__ ticket, double* __restrict__ out,
+                                                 const double* __restrict__ add, double* __restrict__ out_sum,
+                                                 const ArnoldiState* ast) {
+    __shared__ double red[NO][kRedThreads / 32];
+    __shared__ int s_last;
+#pragma unroll
+    for (int q = 0; q < NO; ++q) {
+        if (q < nout) {
+            T sw = acc[q];
+            for (int o = 16; o > 0; o >>= 1) sw += __shfl_down_sync(0xffffffffu, sw, o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = (double)sw;
+        }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nout) {
+        double sb = 0.;
+        for (int wq = 0; wq < kRedThreads / 32; ++wq) sb += red[threadIdx.x][wq];
+        partial[(int64_t)blockIdx.x * nout + threadIdx.x] = sb;
+    }
+    __threadfence();   // every writer's partials before the ticket
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < nout; q += blockDim.x >> 5) {
+        double sq = lane_partials(partial, (int)gridDim.x, nout, q, lane);
+        for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
+        if (lane == 0) {
+            out[q] = sq;
+            if (add) out_sum[q] = sq + add[q];
+            if (ast && ast->H) arnoldi_update(*ast, ast->hcol, sqrt(sq));
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// Basis vectors whose packs a thread loads before their FMAs: all of them up
+// to 16 (64 registers in either precision), eight at a time beyond that, so
+// that two blocks of kRedThreads fit on an SM (128 registers a thread).
+template <int KMAX>
+__host__ __device__ constexpr int pack_group() { return KMAX <= 16 ? KMAX : 8; }
+
+// Blocks of kRedThreads per SM the register budget aims at: one where the
+// FP64 update-and-dot pass keeps 16 or more accumulators in doubles besides
+// its packs (the 128-register cap of two blocks would spill), two elsewhere.
+template <typename T, int KMAX, bool kNorm>
+__host__ __device__ constexpr int vec_min_blocks() { return !kNorm && sizeof(T) == 8 && KMAX >= 16 ? 1 : 2; }
+
+// multi_dot_kernel with 16-byte loads: out[q] = <V_q, w> for q < k <= KMAX.
+// Each thread takes Pack<T>::n consecutive entries per step, the loads of up
+// to 16 basis vectors issued before their FMAs; the last block also takes
+// the entries past the last whole pack.  V_q and w start on 16-byte
+// boundaries (the host checks).
+template <typename T, int KMAX>
+__global__ void __launch_bounds__(kRedThreads, 2) multi_dot_vec_kernel(
+    const T* __restrict__ V, int64_t ldv, int k, const T* __restrict__ w, int64_t n, double* __restrict__ partial,
+    unsigned int* __restrict__ ticket, double* __restrict__ out, const double* __restrict__ add,
+    double* __restrict__ out_sum, const int* __restrict__ stop) {
+    constexpr int P = Pack<T>::n;
+    constexpr int G = pack_group<KMAX>();
+    if (stop && *stop) return;   // every block: the ticket stays untouched
+    T acc[KMAX];
+#pragma unroll
+    for (int q = 0; q < KMAX; ++q) acc[q] = T(0);
+    const int64_t np = n / P;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < np; c += (int64_t)gridDim.x * blockDim.x) {
+        const Pack<T> wp = load_pack(w + c * P);
+#pragma unroll
+        for (int q0 = 0; q0 < KMAX; q0 += G) {
+            if (q0 >= k) break;
+            Pack<T> vp[G];
+#pragma unroll
+            for (int u = 0; u < G; ++u)
+                if (q0 + u < k) vp[u] = load_pack(V + (int64_t)(q0 + u) * ldv + c * P);
+#pragma unroll
+            for (int u = 0; u < G; ++u)
+                if (q0 + u < k) {
+#pragma unroll
+                    for (int e = 0; e < P; ++e) acc[q0 + u] = fma(vp[u].v[e], wp.v[e], acc[q0 + u]);
+                }
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1) {
+        const int64_t i = np * P + threadIdx.x;
+        if (i < n) {
+            const T wi = w[i];
+#pragma unroll
+            for (int q = 0; q < KMAX; ++q)
+                if (q < k) acc[q] = fma(V[(int64_t)q * ldv + i], wi, acc[q]);
+        }
+    }
+    block_reduce_out<T, KMAX>(acc, k, partial, ticket, out, add, out_sum, nullptr);
+}
+
+// axpy_dot_kernel with 16-byte loads: w -= sum_{q<k} h[q] V_q, then
+// out[q] = <V_q, w> (kNorm false) or out[0] = <w, w> (kNorm true).  With at
+// most 16 basis vectors a thread keeps the packs it loaded for the dot
+// products; with more, the second read of V_q hits the cache.  The update
+// subtracts the terms in q order, as the scalar kernel does.
+template <typename T, int KMAX, bool kNorm>
+__global__ void __launch_bounds__(kRedThreads, vec_min_blocks<T, KMAX, kNorm>()) axpy_dot_vec_kernel(
+    T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k, const double* __restrict__ h, int64_t n,
+    double* __restrict__ partial, unsigned int* __restrict__ ticket, double* __restrict__ out,
+    const double* __restrict__ add, double* __restrict__ out_sum, const int* __restrict__ stop, ArnoldiState ast) {
+    constexpr int P = Pack<T>::n;
+    constexpr int NO = kNorm ? 1 : KMAX;
+    constexpr int G = pack_group<KMAX>();
+    constexpr bool kKeep = KMAX == G;
+    if (stop && *stop) return;
+    __shared__ T hs[KMAX];
+    if ((int)threadIdx.x < k) hs[threadIdx.x] = (T)h[threadIdx.x];
+    __syncthreads();
+    T acc[NO];
+#pragma unroll
+    for (int q = 0; q < NO; ++q) acc[q] = T(0);
+    const int64_t np = n / P;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < np; c += (int64_t)gridDim.x * blockDim.x) {
+        Pack<T> sv = load_pack(w + c * P);
+        Pack<T> vp[G];
+#pragma unroll
+        for (int q0 = 0; q0 < KMAX; q0 += G) {
+            if (q0 >= k) break;
+#pragma unroll
+            for (int u = 0; u < G; ++u)
+                if (q0 + u < k) vp[u] = load_pack(V + (int64_t)(q0 + u) * ldv + c * P);
+#pragma unroll
+            for (int u = 0; u < G; ++u)
+                if (q0 + u < k) {
+#pragma unroll
+                    for (int e = 0; e < P; ++e) sv.v[e] = fma(-hs[q0 + u], vp[u].v[e], sv.v[e]);
+                }
+        }
+        *reinterpret_cast<Pack<T>*>(w + c * P) = sv;
+        if (kNorm) {
+#pragma unroll
+            for (int e = 0; e < P; ++e) acc[0] = fma(sv.v[e], sv.v[e], acc[0]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < NO; ++q)
+                if (q < k) {
+                    const Pack<T> vq = kKeep ? vp[q % G] : load_pack(V + (int64_t)q * ldv + c * P);
+#pragma unroll
+                    for (int e = 0; e < P; ++e) acc[q] = fma(vq.v[e], sv.v[e], acc[q]);
+                }
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1) {
+        const int64_t i = np * P + threadIdx.x;
+        if (i < n) {
+            T si = w[i];
+#pragma unroll
+            for (int q = 0; q < KMAX; ++q)
+                if (q < k) si = fma(-hs[q], V[(int64_t)q * ldv + i], si);
+            w[i] = si;
+            if (kNorm) {
+                acc[0] = fma(si, si, acc[0]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < NO; ++q)
+                    if (q < k) acc[q] = fma(V[(int64_t)q * ldv + i], si, acc[q]);
+            }
+        }
+    }
+    block_reduce_out<T, NO>(acc, kNorm ? 1 : k, partial, ticket, out, add, out_sum, kNorm ? &ast : nullptr);
+}
+
 // w -= sum_q h[q] V_q
 template <typename T>
 __global__ void multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
@@ -365,13 +553,18 @@ inline int grid_for(int64_t n) {
 struct Workspace {
     int m = 0;
     int64_t N = 0;
-    double* V64 = nullptr;   // (m+1) x N
-    float* V32 = nullptr;    // (m+1) x N
+    int64_t ld = 0;          // stride of the bases: N rounded up to 64 entries (16-byte aligned vectors)
+    double* V64 = nullptr;   // (m+1) x ld
+    float* V32 = nullptr;    // (m+1) x ld
     double *b = nullptr, *r = nullptr, *x = nullptr, *t = nullptr, *gb = nullptr;
     double *w64 = nullptr, *z64 = nullptr, *t64 = nullptr;
     float *w32 = nullptr, *d32 = nullptr, *z32 = nullptr, *t32 = nullptr, *s32 = nullptr;
-    double* Z64 = nullptr;      // m x N flexible basis (preconditioners 2 and 3)
+    double* Z64 = nullptr;      // m x ld flexible basis (every preconditioned mode)
     float* Z32 = nullptr;
+    // grids of the 16-byte Gram-Schmidt kernels (blocks resident on every SM,
+    // at most kRedBlocks): [FP64][KMAX 8, 16, 32] and [FP64][KMAX][norm pass]
+    int gdot[2][3] = {};
+    int gaxd[2][3][2] = {};
     double* partial = nullptr;  // kRedBlocks x (m+1)
     unsigned int* ticket = nullptr;   // last-block ticket of multi_dot_kernel (0 between launches)
     // device Arnoldi state of the lagged-check inner loop
@@ -408,6 +601,8 @@ T* dalloc(Workspace* ws, int64_t n) {
     return (T*)p;
 }
 
+void init_vec_grids(Workspace* ws);
+
 Workspace* get_ws(rtg_handle* h, int m) {
     Workspace* ws = h->ws;
     const int64_t N = h->host.ndof;
@@ -417,8 +612,10 @@ Workspace* get_ws(rtg_handle* h, int m) {
     h->ws = ws;
     ws->m = m;
     ws->N = N;
-    ws->V64 = dalloc<double>(ws, (int64_t)(m + 1) * N);
-    ws->V32 = dalloc<float>(ws, (int64_t)(m + 1) * N);
+    ws->ld = (N + 63) / 64 * 64;
+    ws->V64 = dalloc<double>(ws, (int64_t)(m + 1) * ws->ld);
+    ws->V32 = dalloc<float>(ws, (int64_t)(m + 1) * ws->ld);
+    init_vec_grids(ws);
     ws->b = dalloc<double>(ws, N);
     ws->r = dalloc<double>(ws, N);
     ws->x = dalloc<double>(ws, N);
@@ -451,11 +648,91 @@ Workspace* get_ws(rtg_handle* h, int m) {
     return ws;
 }
 
+// blocks of kernel fn resident on all SMs of the current device, at most kRedBlocks
+int resident_grid(const void* fn) {
+    int dev = 0, sms = 0, per_sm = 0;
+    RTG_CUDA(cudaGetDevice(&dev));
+    RTG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    RTG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRedThreads, 0));
+    return std::max(1, std::min(kRedBlocks, per_sm * sms));
+}
+
+// the grids of every 16-byte Gram-Schmidt kernel, found once per workspace
+// (outside any stream capture)
+void init_vec_grids(Workspace* ws) {
+    ws->gdot[0][0] = resident_grid((const void*)multi_dot_vec_kernel<float, 8>);
+    ws->gdot[0][1] = resident_grid((const void*)multi_dot_vec_kernel<float, 16>);
+    ws->gdot[0][2] = resident_grid((const void*)multi_dot_vec_kernel<float, 32>);
+    ws->gdot[1][0] = resident_grid((const void*)multi_dot_vec_kernel<double, 8>);
+    ws->gdot[1][1] = resident_grid((const void*)multi_dot_vec_kernel<double, 16>);
+    ws->gdot[1][2] = resident_grid((const void*)multi_dot_vec_kernel<double, 32>);
+    ws->gaxd[0][0][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 8, false>);
+    ws->gaxd[0][1][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 16, false>);
+    ws->gaxd[0][2][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 32, false>);
+    ws->gaxd[0][0][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 8, true>);
+    ws->gaxd[0][1][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 16, true>);
+    ws->gaxd[0][2][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 32, true>);
+    ws->gaxd[1][0][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 8, false>);
+    ws->gaxd[1][1][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 16, false>);
+    ws->gaxd[1][2][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 32, false>);
+    ws->gaxd[1][0][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 8, true>);
+    ws->gaxd[1][1][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 16, true>);
+    ws->gaxd[1][2][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 32, true>);
+}
+
+// the 16-byte kernels take vectors that start on 16-byte boundaries, ldv apart
+template <typename T>
+bool packed(const T* p, int64_t ldv) {
+    return ((uintptr_t)p & 15u) == 0 && (ldv * (int64_t)sizeof(T)) % 16 == 0;
+}
+
+inline int kmax_index(int k) { return k <= 8 ? 0 : (k <= 16 ? 1 : 2); }   // KMAX 8, 16, 32
+
+// out[q] = <V_q, w> for q < k (and out_sum = out + add when add is given)
 template <typename T>
 void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, double* out,
           const double* add, double* out_sum, cudaStream_t s, const int* stop = nullptr) {
-    multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
-                                                          out_sum, stop), count_launch();
+    if (k > 32 || !packed(V, ldv) || !packed(w, 0)) {
+        multi_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
+                                                              out_sum, stop), count_launch();
+        return;
+    }
+    const int ki = kmax_index(k);
+    const int g = ws->gdot[sizeof(T) == 8][ki];
+    if (ki == 0)
+        multi_dot_vec_kernel<T, 8><<<g, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
+                                                             out_sum, stop);
+    else if (ki == 1)
+        multi_dot_vec_kernel<T, 16><<<g, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
+                                                              out_sum, stop);
+    else
+        multi_dot_vec_kernel<T, 32><<<g, kRedThreads, 0, s>>>(V, ldv, k, w, n, ws->partial, ws->ticket, out, add,
+                                                              out_sum, stop);
+    count_launch();
+}
+
+// w -= V h over k <= 32 vectors fused with out = V^T w (kNorm false) or
+// out[0] = <w, w> and the Arnoldi update of ast (kNorm true)
+template <typename T, bool kNorm>
+void axpy_dot(Workspace* ws, T* w, const T* V, int64_t ldv, int k, const double* h, int64_t n, double* out,
+              const double* add, double* out_sum, const int* stop, ArnoldiState ast, cudaStream_t s) {
+    if (!packed(V, ldv) || !packed((const T*)w, 0)) {
+        axpy_dot_kernel<T, kNorm><<<kRedBlocks, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket,
+                                                                    out, add, out_sum, stop, ast), count_launch();
+        return;
+    }
+    const int ki = kmax_index(k);
+    const int g = ws->gaxd[sizeof(T) == 8][ki][kNorm ? 1 : 0];
+    if (ki == 0)
+        axpy_dot_vec_kernel<T, 8, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
+                                                                   add, out_sum, stop, ast);
+    else if (ki == 1)
+        axpy_dot_vec_kernel<T, 16, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
+                                                                    add, out_sum, stop, ast);
+    else
+        axpy_dot_vec_kernel<T, 32, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
+                                                                    add, out_sum, stop, ast);
+    count_launch();
 }
 
 template <typename T>
@@ -498,12 +775,12 @@ template <typename T>
 T* flex_basis(Workspace* ws, int m);
 template <>
 double* flex_basis<double>(Workspace* ws, int m) {
-    if (!ws->Z64) ws->Z64 = dalloc<double>(ws, (int64_t)m * ws->N);
+    if (!ws->Z64) ws->Z64 = dalloc<double>(ws, (int64_t)m * ws->ld);
     return ws->Z64;
 }
 template <>
 float* flex_basis<float>(Workspace* ws, int m) {
-    if (!ws->Z32) ws->Z32 = dalloc<float>(ws, (int64_t)m * ws->N);
+    if (!ws->Z32) ws->Z32 = dalloc<float>(ws, (int64_t)m * ws->ld);
     return ws->Z32;
 }
 
@@ -522,6 +799,7 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                   double tol_abs, int max_it, std::vector<double>* hist, int* applies,
                   PcState& pc, cudaStream_t s) {
     const int64_t N = ws->N;
+    const int64_t ld = ws->ld;
     GmresResult res;
     const OpView<T>& v = view<T>(h);
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
@@ -578,10 +856,10 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         // one Arnoldi step on stream s: w = A M(v_j), CGS2 against V, v_{j+1} = w / ||w||
         // (with a device Arnoldi state the norm pass ends with the Arnoldi update)
         auto step = [&](int j, cudaStream_t s, ArnoldiState ast) {
-            T* vj = V + (int64_t)j * N;
-            T* vn = V + (int64_t)(j + 1) * N;
+            T* vj = V + (int64_t)j * ld;
+            T* vn = V + (int64_t)(j + 1) * ld;
             if (flex) {
-                T* zj = Z + (int64_t)j * N;
+                T* zj = Z + (int64_t)j * ld;
                 apply_sweep<T>(h, vj, zj, s, nullptr, nullptr, stop, true);
                 if (mode == 2) {
                     apply_coarse<T>(h, vj, zj, s);
@@ -593,22 +871,18 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
                 launch_apply<T>(h, vs, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
             }
             // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
-            dots<T>(ws, V, N, j + 1, wbuf, N, h1, nullptr, nullptr, s, stop);
+            dots<T>(ws, V, ld, j + 1, wbuf, N, h1, nullptr, nullptr, s, stop);
             if (j + 1 <= kFuseMax) {
                 // w -= V h1 fused with h2 = V^T w; then w -= V h2 fused with ||w||^2
-                axpy_dot_kernel<T, false><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h1, N, ws->partial, ws->ticket, h2, h1, ho, stop, ArnoldiState{}),
-                    count_launch();
-                axpy_dot_kernel<T, true><<<kRedBlocks, kRedThreads, 0, s>>>(
-                    wbuf, V, N, j + 1, h2, N, ws->partial, ws->ticket, nr, nullptr, nullptr, stop, ast),
-                    count_launch();
+                axpy_dot<T, false>(ws, wbuf, V, ld, j + 1, h1, N, h2, h1, ho, stop, ArnoldiState{}, s);
+                axpy_dot<T, true>(ws, wbuf, V, ld, j + 1, h2, N, nr, nullptr, nullptr, stop, ast, s);
             } else {
-                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h1, N), count_launch();
-                dots<T>(ws, V, N, j + 1, wbuf, N, h2, h1, ho, s);
-                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, N, j + 1, h2, N), count_launch();
+                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ld, j + 1, h1, N), count_launch();
+                dots<T>(ws, V, ld, j + 1, wbuf, N, h2, h1, ho, s);
+                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ld, j + 1, h2, N), count_launch();
                 dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
             }
-            T* zn = (flex && j + 1 < m) ? Z + (int64_t)(j + 1) * N : nullptr;
+            T* zn = (flex && j + 1 < m) ? Z + (int64_t)(j + 1) * ld : nullptr;
             normalize_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, vn, nr, ho, j + 1, N, stop, zn, zn ? next : nullptr),
                 count_launch();
         };
@@ -755,9 +1029,9 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
         }
         if (flex) {
             // x += Z y
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, N, j, ws->hdev, 1., N), count_launch();
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, Z, ld, j, ws->hdev, 1., N), count_launch();
         } else {
-            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, N, j, ws->hdev, 1., N), count_launch();
+            combine_kernel<T, T><<<grid_for(N), 256, 0, s>>>(xT, V, ld, j, ws->hdev, 1., N), count_launch();
         }
         res.iters = total;
         if (res.converged) break;
