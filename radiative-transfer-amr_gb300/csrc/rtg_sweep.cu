@@ -200,6 +200,38 @@ constexpr long long kSpinLimitCycles = 2000000000LL;  // about one second
 constexpr int kMaxFaceNodes = 4 * kMaxNodes;
 constexpr int kTr = 8;   // trace entries per element
 
+// Element records.  Everything an element reads about itself before its data
+// (its scalars, the active couplings with their staging offsets, the face
+// nodes those couplings reach, the one-phase map fields) is resolved at set-up
+// and stored per claim index with a fixed stride, so that the claim is
+// followed by one coalesced load instead of a chain of dependent ones.
+// int32 words; 64-bit values take two words, low first.
+constexpr int kRecE = 0;        // element
+constexpr int kRecCol = 1;      // column
+constexpr int kRecDof = 2;      // first DOF (two words)
+constexpr int kRecNx = 4, kRecNy = 5, kRecNth = 6;
+constexpr int kRecFlags = 7;    // ElemDev::flags
+constexpr int kRecInv = 8;      // first block-inverse entry (two words)
+constexpr int kRecNcs = 10;     // staged active couplings; -1: read from global memory
+constexpr int kRecNf = 11;      // face nodes with active couplings
+constexpr int kRecCplB = 12, kRecCplE = 13;   // the element's couplings (all of them)
+constexpr int kRecOk = 14;      // one-phase path: bit 0 FP32, bit 1 FP64
+constexpr int kRecReg = 15;     // one-phase staged region in values, FP32 then FP64
+constexpr int kRecNup = 17;     // upwind values of the one-phase map
+constexpr int kRecGoff = 18;    // map offset, FP32 (two words) then FP64 (two words)
+constexpr int kRecUoff = 22;    // upwind index list offset (two words)
+constexpr int kRecHead = 24;
+// per staged coupling: face, m1, nth1, n0, stride, es, et, base (two words),
+// staging offset, coupling index, (unused); then the face nodes (ascending ij)
+constexpr int kRecCpl = 12;
+constexpr int kCplF = 0, kCplM1 = 1, kCplNt1 = 2, kCplN0 = 3, kCplStr = 4, kCplEs = 5, kCplEt = 6, kCplBase = 7,
+              kCplOff = 9, kCplK = 10;
+constexpr int kRecMax = kRecHead + kRecCpl * kMaxCplStaged + kMaxFaceNodes;
+
+__device__ __forceinline__ int64_t rec64(const int* w) {
+    return (int64_t)(((uint64_t)(uint32_t)w[1] << 32) | (uint64_t)(uint32_t)w[0]);
+}
+
 // hash of a key of 64-bit words (the bits of an element's block inputs)
 struct WordsHash {
     size_t operator()(const std::vector<uint64_t>& v) const {
@@ -378,23 +410,18 @@ __device__ __forceinline__ void stage_block(T* dst, const T* src, int n) {
 
 template <typename T>
 struct UpwindMap {
-    const uint8_t* ok = nullptr;     // per element: bit 0 FP32, bit 1 FP64 takes the one-phase path
-    const int32_t* reg = nullptr;    // per element: values of its staged region (this precision)
-    int reg_cap = 0;                 // ... and the largest region this launch's shared memory holds
-    const int32_t* nup = nullptr;    // per element: upwind values
-    const int64_t* goff = nullptr;   // per element: first entry of G_e (this precision's copy)
-    const int64_t* uoff = nullptr;   // per element: first entry of its upwind index list
+    int reg_cap = 0;                 // the largest one-phase region this launch's shared memory holds (values)
     const int64_t* up = nullptr;     // upwind value offsets into z
-    const T* G = nullptr;
+    const T* G = nullptr;            // maps (this precision's copy)
 };
 
 template <typename T>
 __global__ void __launch_bounds__(kSweepThreads, 4)
-sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, const uint8_t* __restrict__ active,
-                        const T* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
+sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstride, int ne,
+                        const uint8_t* __restrict__ active, const T* __restrict__ inv,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ next,
-                        int* __restrict__ status, UpwindMap<T> um,
-                        int rhs_cap, int bcap, int ccap, unsigned long long* __restrict__ trace) {
+                        int* __restrict__ status, UpwindMap<T> um, int rhs_cap, int bcap,
+                        unsigned long long* __restrict__ trace) {
     extern __shared__ __align__(16) unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);      // rin, then the couplings c (face nodes)
     T* zpre = rhs + rhs_cap;                  // B rin
@@ -402,60 +429,58 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
     T* cs = Bs + bcap;   // staged couplings: per active coupling Es | Et | upwind face line | T
     // one-phase path: the upwind values and G_e take the place of Bs and cs
     constexpr uint8_t kOkBit = sizeof(T) == 8 ? 2 : 1;
+    constexpr int kP = sizeof(T) == 8 ? 1 : 0;   // this precision's slot among the record's per-precision words
     __shared__ int s_idx;
     __shared__ int s_abort;
-    __shared__ int s_nc;
-    __shared__ int s_nf;
-    __shared__ int s_k[kMaxCplStaged];
-    __shared__ int s_off[kMaxCplStaged + 1];
-    __shared__ int s_face[kMaxFaceNodes];     // face nodes (ij) with active couplings
-    // metadata of the staged couplings (read on the critical path)
-    __shared__ int s_F[kMaxCplStaged], s_m1[kMaxCplStaged], s_nt1[kMaxCplStaged], s_n0[kMaxCplStaged];
-    __shared__ int s_str[kMaxCplStaged];
-    __shared__ int s_es[kMaxCplStaged], s_et[kMaxCplStaged];
-    __shared__ long long s_base[kMaxCplStaged];
+    __shared__ int s_rec[kRecMax];
     __shared__ T s_dc[kMaxCplStaged];
     if (v.stop && *v.stop) return;
     for (;;) {
+        unsigned long long t_claim = 0;
         if (threadIdx.x == 0) {
             s_idx = (int)atomicAdd(next, 1u);
             s_abort = 0;
+            if (trace) t_claim = globaltimer_ns();
         }
         __syncthreads();
         const int idx = s_idx;
         if (idx >= ne) break;
-        const int e = order[idx];
-        if (trace && threadIdx.x == 0) trace[kTr * e] = globaltimer_ns();
-        const ElemDev E = v.elems[e];
-        if (v.skip && v.skip[E.col]) {
+        // the element's record: one coalesced load after the claim
+        const int32_t* rp = rec + (int64_t)idx * rstride;
+        for (int w = threadIdx.x; w < rstride; w += blockDim.x) s_rec[w] = __ldg(rp + w);
+        __syncthreads();
+        const int e = s_rec[kRecE];
+        if (trace && threadIdx.x == 0) trace[kTr * e] = t_claim;
+        if (v.skip && v.skip[s_rec[kRecCol]]) {
             // left out (a converged instance of a batch): no work and no
             // values; only elements left out with it read them
             __syncthreads();
             continue;
         }
-        const ColDev C = v.cols[E.col];
-        const int nth = E.nth, nn = C.nx * C.ny, nloc = nn * nth;
-        const int bm = E.flags >> 4;
+        const int nx = s_rec[kRecNx], ny = s_rec[kRecNy], nth = s_rec[kRecNth];
+        const int nn = nx * ny, nloc = nn * nth;
+        const int bm = s_rec[kRecFlags] >> 4;
+        const int64_t dof_off = rec64(s_rec + kRecDof);
         // ---- independent of the sweep: block inverse, residual, mortars
-        const T* B = inv + inv_elem_off[e];
+        const T* B = inv + rec64(s_rec + kRecInv);
         const int bsize = nth * nn * nn;
-        if (um.ok && (um.ok[e] & kOkBit) && um.reg[e] <= um.reg_cap) {
+        if ((s_rec[kRecOk] & kOkBit) && s_rec[kRecReg + kP] <= um.reg_cap) {
             // ---- one-phase path: zpre = B rin and G_e staged before the wait,
             // then z = zpre + G_e z_upwind once the upwind values arrive
             constexpr int kVec = 16 / sizeof(T);   // values per 16-byte copy
-            const int nup = um.nup[e];
+            const int nup = s_rec[kRecNup];
             const int ld = map_ld<T>(nup);
             const int gsz = ld * nloc;             // a multiple of kVec
             T* zl = Bs;
             T* Gs = Bs + ld;
             T* Bg = Gs + gsz;
-            const T* Gg = um.G + um.goff[e];
-            const int64_t* up = um.up + um.uoff[e];
+            const T* Gg = um.G + rec64(s_rec + kRecGoff + 2 * kP);
+            const int64_t* up = um.up + rec64(s_rec + kRecUoff);
             for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
             stage_block(Bg, B, bsize);
             for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
                 const int ij = l / nth;
-                rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
+                rhs[l] = bdry_node_s(bm, ij / ny, ij % ny, nx, ny) ? T(0) : rin[dof_off + l];
             }
             int64_t my_up = threadIdx.x < nup ? __ldg(up + threadIdx.x) : 0;
             cp_async_wait_all();
@@ -496,12 +521,12 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                     const int q0 = half ? vh : 0, q1 = half ? nvec : vh;
                     part = map_row(Gs + (size_t)l2 * ld, zl, q0, q1, half ? T(0) : zpre[l2]);
                     if (half) rhs[l2] = part;
-                    else if (!split) st_relaxed(z + E.dof_off + l2, part);
+                    else if (!split) st_relaxed(z + dof_off + l2, part);
                 }
             }
             if (split) {
                 __syncthreads();
-                if (t < nloc) st_relaxed(z + E.dof_off + t, part + rhs[t]);
+                if (t < nloc) st_relaxed(z + dof_off + t, part + rhs[t]);
             }
             __syncthreads();
             if (trace && threadIdx.x == 0) {
@@ -529,98 +554,25 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
         const T* Bv = staged ? Bs : B;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
-            rhs[l] = bdry_node_s(bm, ij / C.ny, ij % C.ny, C.nx, C.ny) ? T(0) : rin[E.dof_off + l];
+            rhs[l] = bdry_node_s(bm, ij / ny, ij % ny, nx, ny) ? T(0) : rin[dof_off + l];
         }
-        if (threadIdx.x < 32) {
-            // warp 0: the active couplings in order, one lane each (their
-            // metadata loads in flight together), compacted by ballot with a
-            // prefix sum of their staging sizes; then the face nodes that have
-            // active couplings, in ascending order, 32 nodes at a time
-            const int lane = threadIdx.x;
-            int nc = 0, off = 0, fm = 0;
-            bool over = false;
-            for (int k0 = E.cpl_begin; k0 < E.cpl_end; k0 += 32) {
-                const int k = k0 + lane;
-                const bool act = k < E.cpl_end && active[k];
-                int F = 0, n0 = 0, sz = 0;
-                CplGeo g{};
-                CplDev cp{};
-                if (act) {
-                    cp = v.cpls[k];
-                    F = cp.face;
-                    g = v.cgeo[k];
-                    n0 = (F % 2 == 0) ? C.ny : C.nx;
-                    sz = g.m1 * n0 + g.nth1 * nth + g.m1 * g.nth1 + g.m1 * nth;
-                }
-                const unsigned am = __ballot_sync(0xffffffffu, act);
-                int fbit = act ? 1 << F : 0;
-                for (int o = 16; o > 0; o >>= 1) fbit |= __shfl_xor_sync(0xffffffffu, fbit, o);
-                fm |= fbit;
-                int incl = sz;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += t;
-                }
-                const int pos = nc + __popc(am & ((1u << lane) - 1u));
-                if (act) {
-                    if (pos >= kMaxCplStaged) {
-                        over = true;   // too many: read from global memory
-                    } else {
-                        s_k[pos] = k;
-                        s_off[pos] = off + incl - sz;
-                        s_F[pos] = F;
-                        s_m1[pos] = g.m1;
-                        s_nt1[pos] = g.nth1;
-                        s_n0[pos] = n0;
-                        s_str[pos] = g.stride;
-                        s_es[pos] = cp.es;
-                        s_et[pos] = cp.et;
-                        s_base[pos] = g.base;
-                        s_dc[pos] = v.cplc[k];
-                    }
-                }
-                nc += __popc(am);
-                off += __shfl_sync(0xffffffffu, incl, 31);
-            }
-            over = __any_sync(0xffffffffu, over);
-            if (lane == 0) {
-                if (over) {
-                    s_off[kMaxCplStaged] = ccap + 1;
-                    s_nc = -1;
-                } else {
-                    s_off[nc] = off;
-                    s_nc = (off <= ccap) ? nc : -1;   // -1: read from global memory
-                }
-            }
-            int nf = 0;
-            for (int ij0 = 0; ij0 < nn; ij0 += 32) {
-                const int ij = ij0 + lane;
-                bool hit = false;
-                if (ij < nn) {
-                    const int i = ij / C.ny, j = ij % C.ny;
-                    if (!bdry_node_s(bm, i, j, C.nx, C.ny))
-                        for (int F = 0; F < 4; ++F) hit |= ((fm >> F) & 1) && on_face(F, i, j, C.nx, C.ny);
-                }
-                const unsigned hm = __ballot_sync(0xffffffffu, hit);
-                const int p = nf + __popc(hm & ((1u << lane) - 1u));
-                if (hit && p < kMaxFaceNodes) s_face[p] = ij;
-                nf += __popc(hm);
-            }
-            if (lane == 0) s_nf = min(nf, kMaxFaceNodes);
-        }
-        __syncthreads();
-        const int ncs = s_nc, nf = s_nf;
-        // the staged couplings' mortars, from the metadata warp 0 gathered
-        // (asynchronous copies, waited on with the block inverse's)
+        // the active couplings (in coupling order) and the face nodes they
+        // reach, from the record; their mortars staged with asynchronous
+        // copies, waited on with the block inverse's
+        const int ncs = s_rec[kRecNcs], nf = s_rec[kRecNf];
+        const int* s_cpl = s_rec + kRecHead;
+        const int* s_face = s_cpl + kRecCpl * max(ncs, 0);
         for (int c = 0; c < ncs; ++c) {
-            const int m1 = s_m1[c], n0 = s_n0[c], nt1 = s_nt1[c];
-            T* dst = cs + s_off[c];
-            const T* es = v.mort + s_es[c];
-            const T* et = v.mort + s_et[c];
+            const int* cp = s_cpl + kRecCpl * c;
+            const int m1 = cp[kCplM1], n0 = cp[kCplN0], nt1 = cp[kCplNt1];
+            T* dst = cs + cp[kCplOff];
+            const T* es = v.mort + cp[kCplEs];
+            const T* et = v.mort + cp[kCplEt];
             for (int t = threadIdx.x; t < m1 * n0; t += blockDim.x) cp_async_small<sizeof(T)>(dst + t, es + t);
             for (int t = threadIdx.x; t < nt1 * nth; t += blockDim.x)
                 cp_async_small<sizeof(T)>(dst + m1 * n0 + t, et + t);
         }
+        if ((int)threadIdx.x < ncs) s_dc[threadIdx.x] = v.cplc[s_cpl[kRecCpl * threadIdx.x + kCplK]];
         cp_async_wait_all();
         __syncthreads();
         // zpre = B rin, block stored as [r][k][ij]
@@ -638,10 +590,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             // stage the upwind face lines as they are published (coalesced,
             // each value once; each thread waits on its own values)
             for (int c = 0; c < ncs; ++c) {
-                const int m1 = s_m1[c], nt1 = s_nt1[c];
-                T* dst = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth;
-                const T* src = z + s_base[c];
-                const int str = s_str[c];
+                const int* cp = s_cpl + kRecCpl * c;
+                const int m1 = cp[kCplM1], nt1 = cp[kCplNt1];
+                T* dst = cs + cp[kCplOff] + m1 * cp[kCplN0] + nt1 * nth;
+                const T* src = z + rec64(cp + kCplBase);
+                const int str = cp[kCplStr];
                 for (int t = threadIdx.x; t < m1 * nt1; t += blockDim.x) {
                     const int jj = t / nt1, a = t % nt1;
                     T val = T(0);
@@ -657,15 +610,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 int c = 0, base = 0;
                 for (int t = threadIdx.x;; t += blockDim.x) {
                     // advance to the coupling that holds item t
-                    while (c < ncs && t >= base + s_m1[c] * nth) {
-                        base += s_m1[c] * nth;
+                    while (c < ncs && t >= base + s_cpl[kRecCpl * c + kCplM1] * nth) {
+                        base += s_cpl[kRecCpl * c + kCplM1] * nth;
                         ++c;
                     }
                     if (c >= ncs) break;
-                    const int m1 = s_m1[c], nt1 = s_nt1[c];
-                    const T* Et = cs + s_off[c] + m1 * s_n0[c];
+                    const int* cp = s_cpl + kRecCpl * c;
+                    const int m1 = cp[kCplM1], nt1 = cp[kCplNt1];
+                    const T* Et = cs + cp[kCplOff] + m1 * cp[kCplN0];
                     const T* zl = Et + nt1 * nth;
-                    T* Tm = cs + s_off[c] + m1 * s_n0[c] + nt1 * nth + m1 * nt1;
+                    T* Tm = cs + cp[kCplOff] + m1 * cp[kCplN0] + nt1 * nth + m1 * nt1;
                     const int q = t - base, jj = q / nth, r = q % nth;
                     T acc = T(0);
                     for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
@@ -675,15 +629,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             __syncthreads();
             if (trace && threadIdx.x == 0) ck2 = clock64();
             for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
-                const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
+                const int ij = s_face[t / nth], r = t % nth, i = ij / ny, j = ij % ny;
                 T acc = T(0);
                 for (int c = 0; c < ncs; ++c) {
-                    const int F = s_F[c];
-                    if (!on_face(F, i, j, C.nx, C.ny)) continue;
-                    const int m1 = s_m1[c], n0 = s_n0[c];
+                    const int* cp = s_cpl + kRecCpl * c;
+                    const int F = cp[kCplF];
+                    if (!on_face(F, i, j, nx, ny)) continue;
+                    const int m1 = cp[kCplM1], n0 = cp[kCplN0];
                     const int qq = (F % 2 == 0) ? j : i;
-                    const T* Es = cs + s_off[c];
-                    const T* Tm = Es + m1 * n0 + s_nt1[c] * nth + m1 * s_nt1[c];
+                    const T* Es = cs + cp[kCplOff];
+                    const T* Tm = Es + m1 * n0 + cp[kCplNt1] * nth + m1 * cp[kCplNt1];
                     T sacc = T(0);
                     for (int jj = 0; jj < m1; ++jj) sacc += Es[jj * n0 + qq] * Tm[jj * nth + r];
                     acc += s_dc[c] * sacc;
@@ -692,16 +647,16 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
             }
         } else {
             for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
-                const int ij = s_face[t / nth], r = t % nth, i = ij / C.ny, j = ij % C.ny;
+                const int ij = s_face[t / nth], r = t % nth, i = ij / ny, j = ij % ny;
                 T acc = T(0);
-                for (int k = E.cpl_begin; k < E.cpl_end; ++k) {
+                for (int k = s_rec[kRecCplB]; k < s_rec[kRecCplE]; ++k) {
                     if (!active[k]) continue;
                     const CplDev cp = v.cpls[k];
                     const int F = cp.face;
-                    if (!on_face(F, i, j, C.nx, C.ny)) continue;
+                    if (!on_face(F, i, j, nx, ny)) continue;
                     const CplGeo g = v.cgeo[k];
                     const int qq = (F % 2 == 0) ? j : i;
-                    const int n0 = (F % 2 == 0) ? C.ny : C.nx;
+                    const int n0 = (F % 2 == 0) ? ny : nx;
                     const T* Es = v.mort + cp.es;
                     const T* Et = v.mort + cp.et;
                     const T dc = v.cplc[k];
@@ -736,7 +691,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ order, int ne, 
                 a3 -= col[s_face[f + 3] * nn] * rhs[s_face[f + 3] * nth + r];
             }
             for (; f < nf; ++f) a0 -= col[s_face[f] * nn] * rhs[s_face[f] * nth + r];
-            st_relaxed(z + E.dof_off + (int64_t)ij * nth + r, (a0 + a1) + (a2 + a3));
+            st_relaxed(z + dof_off + (int64_t)ij * nth + r, (a0 + a1) + (a2 + a3));
         }
         // the stored values are the publication (downstream elements wait on
         // the values themselves); the barrier ends this element's use of the
@@ -825,6 +780,8 @@ struct Sweep {
     int pick[2] = {-1, -1};
     float shape_ms[2][kSweepShapes] = {};
     int32_t *d_greg32 = nullptr, *d_greg64 = nullptr;
+    int32_t* d_rec = nullptr;            // element records in claim order
+    int rec_stride = 0;                  // words per record (a multiple of 32)
     int n_lagged = 0;
     std::vector<void*> allocs;
     unsigned int* d_next = nullptr;      // work counter
@@ -1122,6 +1079,94 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
                                                                     s->d_G32), count_launch();
             RTG_CUDA(cudaGetLastError());
         }
+        // ---- element records in claim order (the words are listed with kRecE)
+        auto bdry = [](int bm, int i, int j, int nx, int ny) {
+            return ((bm & 1) && i == nx - 1) || ((bm & 2) && j == ny - 1) || ((bm & 4) && i == 0) ||
+                   ((bm & 8) && j == 0);
+        };
+        auto onf = [](int F, int i, int j, int nx, int ny) {
+            return (F == 0 && i == nx - 1) || (F == 1 && j == ny - 1) || (F == 2 && i == 0) || (F == 3 && j == 0);
+        };
+        auto put64 = [](int32_t* w, int64_t x) {
+            w[0] = (int32_t)(uint32_t)((uint64_t)x & 0xFFFFFFFFu);
+            w[1] = (int32_t)(uint32_t)((uint64_t)x >> 32);
+        };
+        std::vector<std::vector<int32_t>> recs(ne);
+        size_t rmax = kRecHead;
+        for (int idx = 0; idx < ne; ++idx) {
+            const int e = lev_elems[idx];
+            const ElemDev& E = t.elems[e];
+            const ColDev& C = t.cols[E.col];
+            std::vector<int32_t>& R = recs[idx];
+            R.assign(kRecHead, 0);
+            R[kRecE] = e;
+            R[kRecCol] = E.col;
+            put64(&R[kRecDof], E.dof_off);
+            R[kRecNx] = C.nx;
+            R[kRecNy] = C.ny;
+            R[kRecNth] = E.nth;
+            R[kRecFlags] = E.flags;
+            put64(&R[kRecInv], inv_off[e]);
+            R[kRecCplB] = E.cpl_begin;
+            R[kRecCplE] = E.cpl_end;
+            R[kRecOk] = gok[e];
+            R[kRecReg] = greg32[e];
+            R[kRecReg + 1] = greg64[e];
+            R[kRecNup] = gnup[e];
+            put64(&R[kRecGoff], goff32[e]);
+            put64(&R[kRecGoff + 2], goff64[e]);
+            put64(&R[kRecUoff], uoff[e]);
+            std::vector<int> act;
+            int fm = 0;
+            for (int k = E.cpl_begin; k < E.cpl_end; ++k)
+                if (active[k]) {
+                    act.push_back(k);
+                    fm |= 1 << t.cpls[k].face;
+                }
+            const int ncs = (int)act.size() <= kMaxCplStaged ? (int)act.size() : -1;
+            R[kRecNcs] = ncs;
+            int soff = 0;
+            for (int c = 0; c < ncs; ++c) {
+                const int k = act[c];
+                const CplDev& cp = t.cpls[k];
+                const CplGeo& g = t.cgeo[k];
+                const int n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+                int32_t w[kRecCpl] = {};
+                w[kCplF] = cp.face;
+                w[kCplM1] = g.m1;
+                w[kCplNt1] = g.nth1;
+                w[kCplN0] = n0;
+                w[kCplStr] = g.stride;
+                w[kCplEs] = cp.es;
+                w[kCplEt] = cp.et;
+                put64(&w[kCplBase], g.base);
+                w[kCplOff] = soff;
+                w[kCplK] = k;
+                R.insert(R.end(), w, w + kRecCpl);
+                soff += g.m1 * n0 + g.nth1 * E.nth + g.m1 * g.nth1 + g.m1 * E.nth;
+            }
+            const int bm = E.flags >> 4;
+            int nf = 0;
+            for (int ij = 0; ij < C.nx * C.ny && nf < kMaxFaceNodes; ++ij) {
+                const int i = ij / C.ny, j = ij % C.ny;
+                bool hit = false;
+                if (!bdry(bm, i, j, C.nx, C.ny))
+                    for (int F = 0; F < 4; ++F) hit |= ((fm >> F) & 1) && onf(F, i, j, C.nx, C.ny);
+                if (hit) {
+                    R.push_back(ij);
+                    ++nf;
+                }
+            }
+            R[kRecNf] = nf;
+            rmax = std::max(rmax, R.size());
+        }
+        s->rec_stride = (int)((rmax + 31) / 32 * 32);
+        if (s->rec_stride > kRecMax) throw RtgError{RTG_ERR_SIZE, "sweep element record too long"};
+        std::vector<int32_t> flat((size_t)ne * s->rec_stride, 0);
+        for (int idx = 0; idx < ne; ++idx)
+            std::copy(recs[idx].begin(), recs[idx].end(), flat.begin() + (size_t)idx * s->rec_stride);
+        s->d_rec = sw_alloc<int32_t>(s, flat.size());
+        RTG_CUDA(cudaMemcpy(s->d_rec, flat.data(), sizeof(int32_t) * flat.size(), cudaMemcpyHostToDevice));
     }
     return s;
 }
@@ -1147,18 +1192,13 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     const int pi = f64 ? 1 : 0;
     const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
     UpwindMap<T> um;
-    um.ok = s->d_gok;
-    um.reg = f64 ? s->d_greg64 : s->d_greg32;
-    um.nup = s->d_gnup;
-    um.goff = f64 ? s->d_goff64 : s->d_goff32;
-    um.uoff = s->d_uoff;
     um.up = s->d_up;
     um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
     auto launch = [&](const Sweep::Shape& sh) {
         um.reg_cap = sh.reg_cap;
         sweep_persistent_kernel<T><<<sh.grid, sh.threads, sh.smem, st>>>(
-            v, s->d_lev_elems, (int)h->host.elems.size(), s->d_active, inv, s->d_inv_off, r, z, s->d_next,
-            s->d_status, um, rhs_cap, sh.bcap, (int)s->max_c, trace), count_launch();
+            v, s->d_rec, s->rec_stride, (int)h->host.elems.size(), s->d_active, inv, r, z, s->d_next, s->d_status,
+            um, rhs_cap, sh.bcap, trace), count_launch();
     };
     if (s->pick[pi] < 0) {
         // the launch shapes: larger per-CTA shared memory (more one-phase
