@@ -277,7 +277,9 @@ apply_col_kernel(OpView<T> v, const float* __restrict__ Wf32, const float* __res
 // copy is a cp.async, so a staging loop has all its loads in flight.
 // Shared memory: Xs[Nth][nijp] | column table | cell rows and flags | item
 // region: WsT[Nth][Mp] (later T | Fy[Mp][nijp]) | Ys[Mp][nijp] |
-// row table[Mp][kRowVals] | row -> cell.
+// row table[Mp][kRowVals] | row -> cell.  Without the product (the
+// tensor-core path takes it) a CTA may hold any run of items of its column,
+// down to one, and Xs holds only the current item's rows.
 //
 // FP64 (kParity) keeps the reference's drop rules without per-term tests on
 // the common path:
@@ -425,8 +427,12 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
     const bool scat = kProduct && fl.scat;
     const int nij = C.nx * C.ny, Nth = C.nth_col, ncell = C.elem_end - C.elem_begin;
     const int nijp = (nij + 3) & ~3, Nthp = (Nth + 3) & ~3;
-    T* Xs = smt;                                                  // [Nth][nijp]
-    T* colt = Xs + (size_t)Nth * nijp;                            // column table
+    // with the product every row of x is staged once per column; without it
+    // (tensor-core path) each item stages its own rows (grp.w: the most rows
+    // of an item of the group, a multiple of 4)
+    const int xrows = kProduct ? Nth : grp.w;
+    T* Xs = smt;                                                  // [xrows][nijp]
+    T* colt = Xs + (size_t)xrows * nijp;                          // column table
     T* rowt = colt + col_table_size(C.nx, C.ny);                  // [Nthp][kRowVals]
     int* crow = reinterpret_cast<int*>(rowt + (size_t)Nthp * kRowVals);   // [ncell+1] first row; crow[ncell] = Nth
     int* cflg = crow + ncell + 1;                                          // [ncell] element flags
@@ -473,7 +479,7 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
     const T* xc = x + C.dof_off;
     // stage x transposed: Xs[row][ij]; pad columns are zero (d grows per
     // thread, so the cell index k only moves forward)
-    {
+    if constexpr (kProduct) {
         int k = 0;
         for (int d = threadIdx.x; d < C.ndof; d += blockDim.x) {
             while (d >= nij * crow[k + 1]) ++k;
@@ -482,10 +488,10 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
             const int ij = small_div(l, s_rcp[nth]);
             cp_async_small<sizeof(T)>(Xs + (crow[k] + l - ij * nth) * nijp + ij, xc + d);
         }
+        if (nijp != nij)
+            for (int t = threadIdx.x; t < Nth * (nijp - nij); t += blockDim.x)
+                Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = T(0);
     }
-    if (nijp != nij)
-        for (int t = threadIdx.x; t < Nth * (nijp - nij); t += blockDim.x)
-            Xs[(t / (nijp - nij)) * nijp + nij + t % (nijp - nij)] = T(0);
     // the column's row table
     for (int R = threadIdx.x; R < Nth; R += blockDim.x) {
         const int k = rcell[R];
@@ -535,6 +541,19 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                     cp_async_small<sizeof(T)>(WsT + t, WTg + (int64_t)c * Nth + it.row0 + m);
                 else
                     WsT[t] = T(0);
+            }
+        }
+        if constexpr (!kProduct) {
+            // the item's rows of x (its DOFs are contiguous: whole cells),
+            // row R at Xs[R - row0]; the product does not run, so the pad
+            // columns are never read
+            int k = it.cell_begin;
+            for (int d = nij * it.row0 + threadIdx.x; d < nij * (it.row0 + M); d += blockDim.x) {
+                while (d >= nij * crow[k + 1]) ++k;
+                const int nth = crow[k + 1] - crow[k];
+                const int l = d - nij * crow[k];
+                const int ij = small_div(l, s_rcp[nth]);
+                cp_async_small<sizeof(T)>(Xs + (crow[k] - it.row0 + l - ij * nth) * nijp + ij, xc + d);
             }
         }
         cp_async_wait_all();
@@ -708,8 +727,9 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
             }
             const int R = crow[k] + r;
             const int m = R - it.row0;   // row within the item
+            const int xr0 = kProduct ? R : m;   // row of Xs
             const T* rw = rowt + R * kRowVals;
-            const T xself = Xs[R * nijp + ij];
+            const T xself = Xs[xr0 * nijp + ij];
             const T mterm = rw[0] * kwn[ij];
             T acc = T(0);
             if constexpr (kParity) {
@@ -746,7 +766,7 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                 if (fl.mass) acc += mterm * xself;
             }
             if (fl.ic) {
-                const T* xr = Xs + R * nijp;
+                const T* xr = Xs + xr0 * nijp;
                 T t1 = T(0), t2 = T(0);
                 const T* gy = Gys + j * C.ny;
                 for (int jj = 0; jj < C.ny; ++jj) t1 += gy[jj] * xr[i * C.ny + jj];
@@ -1406,9 +1426,11 @@ static ParityTables* build_parity(const rtg_handle* h) {
 // column (gcap items, 0: all of them) and stages the column's input once.
 // Shared memory of a group: the column part (input, column table, cell
 // rows and flags) and the largest item region of its items.
-static size_t tile_col_bytes(size_t vsize, int nth_col, int nx, int ny, int ncell) {
+// xrows: rows of x staged (the column's nth_col with the product, the most
+// rows of an item of the group without it)
+static size_t tile_col_bytes(size_t vsize, int nth_col, int nx, int ny, int ncell, int xrows) {
     const int nijp = (nx * ny + 3) & ~3, nthp = (nth_col + 3) & ~3;
-    return vsize * ((size_t)nth_col * nijp + (size_t)col_table_size(nx, ny) + (size_t)nthp * kRowVals) +
+    return vsize * ((size_t)xrows * nijp + (size_t)col_table_size(nx, ny) + (size_t)nthp * kRowVals) +
            sizeof(int) * col_int_words(ncell, nth_col) + 16;
 }
 static size_t tile_item_bytes(size_t vsize, int nx, int ny, int wcap, int M) {
@@ -1457,6 +1479,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         int64_t cost;
         size_t smem;
         int col;
+        int xrows;   // tensor-core path: x rows staged (the most rows of an item)
         std::vector<TileItem> its;
         std::vector<std::vector<TileCpl>> ents;
     };
@@ -1476,7 +1499,8 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
             std::vector<size_t> ibytes;
             std::vector<int64_t> icost;
             std::vector<std::vector<TileCpl>> ents;
-            const size_t cb = tile_col_bytes(sizeof(T), C.nth_col, C.nx, C.ny, ncell);
+            // column part of the shared memory with x rows xr
+            auto colb = [&](int xr) { return tile_col_bytes(sizeof(T), C.nth_col, C.nx, C.ny, ncell, xr); };
             bool fits = false;
             for (int rcap = rows_cap; rcap > 0 && !fits; rcap = rcap > 4 ? rcap / 2 : 0) {
                 its.clear();
@@ -1542,7 +1566,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                     its.push_back(ti);
                 }
                 for (size_t q = 0; q < its.size() && fits; ++q)
-                    if (cb + ibytes[q] > kSmemBudget) fits = false;
+                    if (colb(tc ? (its[q].M + 3) & ~3 : C.nth_col) + ibytes[q] > kSmemBudget) fits = false;
                 if (tc && tc_smem_bytes(nij, C.nth_col) > kSmemBudget) fits = false;
             }
             if (fits) {
@@ -1564,13 +1588,16 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                 }
                 const size_t per = gcap > 0 ? (size_t)gcap : its.size();
                 for (size_t q0 = 0; q0 < its.size(); q0 += per) {
-                    GroupRec g{0, 0, ci, {}, {}};
+                    GroupRec g{0, 0, ci, 0, {}, {}};
+                    size_t ib = 0;
                     for (size_t q = q0; q < std::min(its.size(), q0 + per); ++q) {
                         g.cost += icost[q];
-                        g.smem = std::max(g.smem, cb + ibytes[q]);
+                        ib = std::max(ib, ibytes[q]);
+                        if (tc) g.xrows = std::max(g.xrows, (its[q].M + 3) & ~3);
                         g.its.push_back(its[q]);
                         g.ents.push_back(std::move(ents[q]));
                     }
+                    g.smem = colb(tc ? g.xrows : C.nth_col) + ib;
                     groups.push_back(std::move(g));
                 }
                 continue;
@@ -1650,7 +1677,7 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
             ti.cpl_end = (int)ent.size();
             tv.push_back(ti);
         }
-        tg.push_back(make_int4(g.col, first, (int)tv.size(), 0));
+        tg.push_back(make_int4(g.col, first, (int)tv.size(), g.xrows));
         const int slot = kSmemClasses - 1 - c;   // launch index
         counts[slot]++;
         p->tg_smem[slot] = std::max(p->tg_smem[slot], g.smem);
@@ -1837,7 +1864,9 @@ static ApplyPlan* tune_plan(rtg_handle* h, cudaStream_t s) {
         for (int rows : {16, 32, 64})
             for (int gcap : {0, 1})
                 for (int split : {0, 1}) shapes.push_back(PlanShape{rows, gcap, split, 0});
-        // tensor-core scattering (FP32): one CTA per column, items of 32 or 64 rows
+        // tensor-core scattering (FP32): one CTA per column, items of 32 or 64
+        // rows (one CTA per item ties with these on the two-scatterer problem
+        // and is left out of the list; rtg_apply_shape can still pin it)
         if (!f64)
             for (int rows : {32, 64}) shapes.push_back(PlanShape{rows, 0, 0, 1});
         for (const PlanShape& sh : shapes) {
