@@ -596,11 +596,15 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                             load4(Xs + c * nijp + j0, xa);
 #pragma unroll
                             for (int i = 0; i < 4; ++i) {
-                                const unsigned long long wb =
-                                    (unsigned long long)__double_as_longlong((double)wv[i]) & 0x7FFFFFFFFFFFFFFFull;
+                                // the dropped terms' W zeroed by an integer mask of its bits
+                                // (no FP64 select)
+                                const unsigned long long wbits = (unsigned long long)__double_as_longlong((double)wv[i]);
+                                const unsigned long long wb = wbits & 0x7FFFFFFFFFFFFFFFull;
 #pragma unroll
-                                for (int j = 0; j < 4; ++j)
-                                    acc[i][j] = fma(wb >= tb[j] ? wv[i] : T(0), xa[j], acc[i][j]);
+                                for (int j = 0; j < 4; ++j) {
+                                    const unsigned long long keep = wb >= tb[j] ? ~0ull : 0ull;
+                                    acc[i][j] = fma(__longlong_as_double((long long)(wbits & keep)), xa[j], acc[i][j]);
+                                }
                             }
                         }
                     } else {
@@ -616,14 +620,49 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                         }
                     }
                 }
-                for (int o = 1; o < ks; o <<= 1)
+                // reduce-scatter over the ks lanes of the tile: each step
+                // halves the partial sums a lane holds (it keeps one half and
+                // adds its partner's copy of it), so lane s ends with 16/ks
+                // finished outputs from index base (row-major in the tile)
+                T a[16];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
+                for (int i = 0; i < 4; ++i)
 #pragma unroll
-                        for (int j = 0; j < 4; ++j) acc[i][j] += __shfl_xor_sync(0xffffffffu, acc[i][j], o);
-                if (act && slot == 0)
+                    for (int j = 0; j < 4; ++j) a[4 * i + j] = acc[i][j];
+                int base = 0;
+                if (ks >= 2) {
+                    const bool up = slot & 1;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) store4(Ys + (m0 + i) * nijp + j0, acc[i]);
+                    for (int q = 0; q < 8; ++q) {
+                        const T keep = up ? a[q + 8] : a[q], send = up ? a[q] : a[q + 8];
+                        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+                    }
+                    base += up ? 8 : 0;
+                }
+                if (ks >= 4) {
+                    const bool up = slot & 2;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const T keep = up ? a[q + 4] : a[q], send = up ? a[q] : a[q + 4];
+                        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+                    }
+                    base += up ? 4 : 0;
+                }
+                if (ks >= 8) {
+                    const bool up = slot & 4;
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const T keep = up ? a[q + 2] : a[q], send = up ? a[q] : a[q + 2];
+                        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+                    }
+                    base += up ? 2 : 0;
+                }
+                if (act) {
+                    const int cnt = 16 / ks;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q)
+                        if (q < cnt) Ys[(m0 + ((base + q) >> 2)) * nijp + j0 + ((base + q) & 3)] = a[q];
+                }
             }
         }
         __syncthreads();
