@@ -427,15 +427,20 @@ def setup_context(mesh, spec, params):
     g_dev = ctx.inflow(spec.bcs_dirac)
     torch.cuda.synchronize()
     out["vectors_s"] = time.perf_counter() - t0
+    # inputs and outputs of both precisions made before the clocks start: the
+    # timed regions hold the library's own first-use work only
     z64 = torch.zeros(ctx.N, dtype=torch.float64, device=ctx.device)
+    z32 = torch.zeros(ctx.N, dtype=torch.float32, device=ctx.device)
+    o64, o32 = torch.empty_like(z64), torch.empty_like(z32)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ctx.precondition(z64)
-    ctx.precondition(z64.float(), prec=_lib.RTG_FP32)
+    ctx.precondition(z64, o64)
+    ctx.precondition(z32, o32, prec=_lib.RTG_FP32)
     torch.cuda.synchronize()
     out["sweep_setup_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z64)
-    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z64.float(), prec=_lib.RTG_FP32)
+    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z64, o64)
+    ctx.apply(_lib.RTG_SYSTEM | _lib.RTG_MASK_ROWS, z32, o32, prec=_lib.RTG_FP32)
     torch.cuda.synchronize()
     out["apply_tuning_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
