@@ -761,7 +761,7 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
             const int i = small_div(ij, rny), j = ij - i * C.ny;
             const int flg = cflg[k];
             if (fl.mask_rows && bdry_node(flg >> 4, i, j, C.nx, C.ny)) {
-                yc[d] = T(0);
+                if constexpr (kProduct) yc[d] = T(0);   // tensor-core path: y was zeroed
                 continue;
             }
             const int R = crow[k] + r;
@@ -828,7 +828,13 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                     if (!kParity || tabs(val) > T(kBcTol)) acc += val * xself;
                 }
             }
-            yc[d] = acc;
+            // tensor-core path: the scattering kernel adds its part to the
+            // same zeroed y concurrently; two terms on zero sum the same in
+            // either order
+            if constexpr (kProduct)
+                yc[d] = acc;
+            else
+                atomicAdd(yc + d, acc);
         }
         // the next item overwrites the couplings and the item region
         __syncthreads();
@@ -838,8 +844,10 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
 // ------------------------------------------------- tensor-core scattering
 // FP32 scattering product on the 5th-generation tensor cores: one CTA per
 // (column, tile of 128 angular rows): D[m][ij] = sum_c W[R0+m][c] X[c][ij],
-// then y[R0+m, ij] += -(dx dy / 8) sw_ij D[m][ij] (the tiled kernel has
-// written the other terms; rows of inflow-boundary nodes stay masked).
+// then y[R0+m, ij] += -(dx dy / 8) sw_ij D[m][ij] by an atomic add: the
+// caller zeroes y and the tiled kernel adds the other terms concurrently on
+// another stream (exactly two terms on zero, so the sum does not depend on
+// their order); rows of inflow-boundary nodes stay zero.
 // Each value is split into TF32 hi + lo parts (hi = round-to-nearest TF32,
 // lo = value - hi, exact in FP32) and D accumulates A_lo B_hi + A_hi B_lo +
 // A_hi B_hi with tcgen05.mma (kind::tf32, M = 128, N = nij padded to 16,
@@ -1059,7 +1067,7 @@ scat_tc_kernel(OpView<float> v, uint32_t flags, const TcItem* __restrict__ items
                 const int i = ij / C.ny, j = ij % C.ny;
                 if (fl.mask_rows && bdry_node(s_cflg[kc] >> 4, i, j, C.nx, C.ny)) continue;
                 const int64_t dof = C.dof_off + (int64_t)nij * s_crow[kc] + (int64_t)ij * nth + r;
-                y[dof] += -dxdy8 * v.sw[C.node_off + ij] * __uint_as_float(d[jj]);
+                atomicAdd(y + dof, -dxdy8 * v.sw[C.node_off + ij] * __uint_as_float(d[jj]));
             }
         }
     }
@@ -1286,6 +1294,11 @@ struct ApplyPlan {
     int ntc = 0;
     size_t tc_smem = 0;
     int* d_status = nullptr;               // RTG_ERR_TIMEOUT if a wait of scat_tc_kernel gave up
+    // tensor-core plans: y is zeroed, then the tiled kernels (on the caller's
+    // stream) and scat_tc_kernel (on side) add their parts concurrently
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int64_t ndof = 0;
     const ParityTables* par = nullptr;   // FP64 tiled path
     bool own_par = false;
     std::vector<TuneRecord> tuning;
@@ -1737,6 +1750,12 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
         p->tc_smem = std::max(p->tc_smem, tc_smem_bytes(C.nx * C.ny, C.nth_col));
     }
     p->ntc = (int)tci.size();
+    p->ndof = t.ndof;
+    if (p->ntc) {
+        RTG_CUDA(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+        RTG_CUDA(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+        RTG_CUDA(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    }
     p->d_tc = (TcItem*)up(tci.data(), sizeof(TcItem) * tci.size());
     p->d_wtc = (float*)up(wtiles.data(), sizeof(float) * wtiles.size());
     p->d_status = (int*)up(nullptr, 0);
@@ -1746,6 +1765,9 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
 
 static void free_plan(ApplyPlan* p) {
     if (!p) return;
+    if (p->side) cudaStreamDestroy(p->side);
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
     for (void* d : p->allocs) cudaFree(d);
     if (p->own_par) free_parity(p->par);
     delete p;
@@ -1769,6 +1791,21 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
                      T* y, cudaStream_t s) {
     constexpr bool f64 = sizeof(T) == 8;
     RTG_LAUNCHED("a kernel before the apply");
+    // tensor-core plan: zero y; the scattering runs on the side stream while
+    // the tiled kernels run here (both add into y)
+    const bool tc_run = !f64 && plan->ntc && (flags & (RTG_SYSTEM | RTG_SCAT));
+    if (plan->ntc) RTG_CUDA(cudaMemsetAsync(y, 0, sizeof(T) * (size_t)plan->ndof, s));
+    if (tc_run) {
+        RTG_CUDA(cudaEventRecord(plan->ev_fork, s));
+        RTG_CUDA(cudaStreamWaitEvent(plan->side, plan->ev_fork, 0));
+        if constexpr (!f64) {
+            scat_tc_kernel<<<plan->ntc, kTcThreads, plan->tc_smem, plan->side>>>(v, flags, plan->d_tc, plan->d_wtc, x,
+                                                                                  y, plan->d_status),
+                count_launch();
+            RTG_LAUNCHED("scat_tc_kernel");
+        }
+        RTG_CUDA(cudaEventRecord(plan->ev_join, plan->side));
+    }
     if (plan->ntiles) {
         TileParity<T> tp{};
         if constexpr (f64) {
@@ -1813,14 +1850,7 @@ static void run_plan(const ApplyPlan* plan, const OpView<T>& v, const OpView<flo
         apply_global_kernel<T, T, f64><<<plan->nslow, kApplyThreads, 0, s>>>(v, v32.mort, flags, plan->d_slow, x, y), count_launch();
         RTG_LAUNCHED("apply_global_kernel");
     }
-    if constexpr (!f64) {
-        if (plan->ntc && (flags & (RTG_SYSTEM | RTG_SCAT))) {
-            scat_tc_kernel<<<plan->ntc, kTcThreads, plan->tc_smem, s>>>(v, flags, plan->d_tc, plan->d_wtc, x, y,
-                                                                         plan->d_status),
-                count_launch();
-            RTG_LAUNCHED("scat_tc_kernel");
-        }
-    }
+    if (tc_run) RTG_CUDA(cudaStreamWaitEvent(s, plan->ev_join, 0));
 }
 
 static int plan_launches(const ApplyPlan* p) {
