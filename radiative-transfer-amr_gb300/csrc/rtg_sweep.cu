@@ -880,6 +880,24 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     for (int L = 0; L < nlev; ++L) s->lev_start[L + 1] += s->lev_start[L];
     std::vector<int32_t> lev_elems(ne), fill(s->lev_start.begin(), s->lev_start.end() - 1);
     for (int e = 0; e < ne; ++e) lev_elems[fill[level[e]]++] = e;
+    // within a level, the elements with the longest chain of levels below
+    // them first (list scheduling by bottom level), then by index: the CTAs
+    // claim the critical chains early (any order within a level is a valid
+    // claim order, every predecessor sits on an earlier level)
+    {
+        std::vector<int32_t> blev(ne, 0);
+        for (int L = nlev - 1; L >= 0; --L)
+            for (int q = s->lev_start[L]; q < s->lev_start[L + 1]; ++q) {
+                const int e = lev_elems[q];
+                int b = 0;
+                for (int d : succ[e])
+                    if (level[d] > level[e]) b = std::max(b, blev[d] + 1);
+                blev[e] = b;
+            }
+        for (int L = 0; L < nlev; ++L)
+            std::stable_sort(lev_elems.begin() + s->lev_start[L], lev_elems.begin() + s->lev_start[L + 1],
+                             [&](int x, int y) { return blev[x] > blev[y]; });
+    }
     s->h_lev_elems = lev_elems;
     // a coupling is active when its upwind element sits on an earlier level
     std::vector<uint8_t> active(t.cpls.size(), 0);
