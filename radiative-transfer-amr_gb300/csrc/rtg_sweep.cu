@@ -220,7 +220,8 @@ constexpr int kRecReg = 15;     // one-phase staged region in values, FP32 then 
 constexpr int kRecNup = 17;     // upwind values of the one-phase map
 constexpr int kRecGoff = 18;    // map offset, FP32 (two words) then FP64 (two words)
 constexpr int kRecUoff = 22;    // upwind index list offset (two words)
-constexpr int kRecHead = 24;
+constexpr int kRecDirect = 24;  // 1: every staged coupling has diagonal mortars (Es and Et)
+constexpr int kRecHead = 25;
 // per staged coupling: face, m1, nth1, n0, stride, es, et, base (two words),
 // staging offset, coupling index, (unused); then the face nodes (ascending ij)
 constexpr int kRecCpl = 12;
@@ -586,7 +587,31 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             trace[kTr * e + 1] = globaltimer_ns();
             ck0 = clock64();
         }
-        if (ncs >= 0) {
+        if (ncs > 0 && s_rec[kRecDirect]) {
+            // diagonal mortars: c on the face nodes straight from the upwind
+            // values, c[q][r] = sum_couplings dcoeff Es[q][q] Et[r][r] z_up[q][r]
+            // (each thread waits on its own values); no T, no mortar sums.
+            // The couplings overwrite rin at the face nodes: B rin is formed first.
+            __syncthreads();
+            for (int t = threadIdx.x; t < nf * nth; t += blockDim.x) {
+                const int ij = s_face[t / nth], r = t % nth, i = ij / ny, j = ij % ny;
+                T acc = T(0);
+                for (int c = 0; c < ncs; ++c) {
+                    const int* cp = s_cpl + kRecCpl * c;
+                    const int F = cp[kCplF];
+                    if (!on_face(F, i, j, nx, ny)) continue;
+                    const int q = (F % 2 == 0) ? j : i;
+                    const int n0 = cp[kCplN0];
+                    const T* Es = cs + cp[kCplOff];
+                    const T* Et = Es + cp[kCplM1] * n0;
+                    T val = T(0);
+                    if (!load_published(z + rec64(cp + kCplBase) + (int64_t)q * cp[kCplStr] + r, val, status))
+                        s_abort = 1;
+                    acc += s_dc[c] * (Es[q * n0 + q] * (Et[r * nth + r] * val));
+                }
+                rhs[ij * nth + r] = acc;
+            }
+        } else if (ncs >= 0) {
             // stage the upwind face lines as they are published (coalesced,
             // each value once; each thread waits on its own values)
             for (int c = 0; c < ncs; ++c) {
@@ -1143,6 +1168,27 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
                 }
             const int ncs = (int)act.size() <= kMaxCplStaged ? (int)act.size() : -1;
             R[kRecNcs] = ncs;
+            // diagonal mortars (conforming neighbours: the off-diagonal
+            // entries are rounding noise, below 1e-13 of the largest, and the
+            // preconditioner leaves them out): the face value (q, r) takes only
+            // the upwind value (q, r), so the couplings need no T and no sums
+            bool direct = ncs > 0;
+            auto diagonal = [&](int64_t off, int rows, int cols) {
+                double mx = 0.;
+                for (int q = 0; q < rows * cols; ++q) mx = std::max(mx, std::fabs(t.mort[(size_t)off + q]));
+                for (int a = 0; a < rows; ++a)
+                    for (int b = 0; b < cols; ++b)
+                        if (a != b && std::fabs(t.mort[(size_t)off + (size_t)a * cols + b]) > 1e-13 * mx) return false;
+                return mx > 0.;
+            };
+            for (int c = 0; c < ncs && direct; ++c) {
+                const int k = act[c];
+                const CplDev& cp = t.cpls[k];
+                const CplGeo& g = t.cgeo[k];
+                const int n0 = (cp.face % 2 == 0) ? C.ny : C.nx;
+                direct = g.m1 == n0 && g.nth1 == E.nth && diagonal(cp.es, g.m1, n0) && diagonal(cp.et, g.nth1, E.nth);
+            }
+            R[kRecDirect] = direct ? 1 : 0;
             int soff = 0;
             for (int c = 0; c < ncs; ++c) {
                 const int k = act[c];
