@@ -30,6 +30,8 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "rtg_internal.h"
 
 namespace rtg {
@@ -384,29 +386,54 @@ __device__ __forceinline__ double map_row(const double* g, const double* zl, int
 // sum_k col[k * cs] * v[k * vs] for k < n with four partial sums and the
 // loads unrolled 16 deep (block-inverse columns read from global memory on the
 // large elements need many loads in flight)
+// Storage of the element block inverses a sweep reads: BF16 for the FP32
+// sweep (an approximate inverse only defines the preconditioner, a fixed
+// linear operator; the FP32 inner solves take as many iterations with it),
+// FP64 for the FP64 sweep.  Entries are widened to T on use.
 template <typename T>
-__device__ __forceinline__ T strided_dot(const T* col, int cs, const T* v, int vs, int n) {
+struct BlockStore;
+template <>
+struct BlockStore<float> {
+    using type = __nv_bfloat16;
+};
+template <>
+struct BlockStore<double> {
+    using type = double;
+};
+__device__ __forceinline__ float widen(__nv_bfloat16 b) { return __bfloat162float(b); }
+__device__ __forceinline__ double widen(double b) { return b; }
+
+// shared-memory units of T an element block of n entries of TB takes
+// (16-byte multiples)
+template <typename T, typename TB>
+__host__ __device__ __forceinline__ int block_units(int n) {
+    return (int)((((int64_t)n * (int64_t)sizeof(TB) + 15) / 16) * 16 / (int64_t)sizeof(T));
+}
+
+template <typename T, typename TB>
+__device__ __forceinline__ T strided_dot(const TB* col, int cs, const T* v, int vs, int n) {
     T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
     int k = 0;
 #pragma unroll 4
     for (; k + 4 <= n; k += 4) {
-        a0 += col[(k + 0) * cs] * v[(k + 0) * vs];
-        a1 += col[(k + 1) * cs] * v[(k + 1) * vs];
-        a2 += col[(k + 2) * cs] * v[(k + 2) * vs];
-        a3 += col[(k + 3) * cs] * v[(k + 3) * vs];
+        a0 += widen(col[(k + 0) * cs]) * v[(k + 0) * vs];
+        a1 += widen(col[(k + 1) * cs]) * v[(k + 1) * vs];
+        a2 += widen(col[(k + 2) * cs]) * v[(k + 2) * vs];
+        a3 += widen(col[(k + 3) * cs]) * v[(k + 3) * vs];
     }
-    for (; k < n; ++k) a0 += col[k * cs] * v[k * vs];
+    for (; k < n; ++k) a0 += widen(col[k * cs]) * v[k * vs];
     return (a0 + a1) + (a2 + a3);
 }
 
-// Stage n values of an element block (global start 16-byte aligned: element
-// offsets are padded to 4 values) with 16-byte copies and a scalar tail.
-template <typename T>
-__device__ __forceinline__ void stage_block(T* dst, const T* src, int n) {
-    constexpr int kVec = 16 / (int)sizeof(T);
-    const int nv = n / kVec;
+// Stage an element block of n entries with 16-byte copies (its global start
+// is 16-byte aligned: block offsets are padded to 8 entries, and the array
+// holds 8 entries of padding past its end, so the last copy may run past the
+// block).  The destination holds block_units<T, TB>(n) units of T.
+template <typename TB>
+__device__ __forceinline__ void stage_block(TB* dst, const TB* src, int n) {
+    constexpr int kVec = 16 / (int)sizeof(TB);
+    const int nv = (n + kVec - 1) / kVec;
     for (int t = threadIdx.x; t < nv; t += blockDim.x) cp_async16(dst + t * kVec, src + t * kVec);
-    for (int t = nv * kVec + (int)threadIdx.x; t < n; t += blockDim.x) cp_async_small<sizeof(T)>(dst + t, src + t);
 }
 
 template <typename T>
@@ -419,10 +446,11 @@ struct UpwindMap {
 template <typename T>
 __global__ void __launch_bounds__(kSweepThreads, 4)
 sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstride, int ne,
-                        const uint8_t* __restrict__ active, const T* __restrict__ inv,
+                        const uint8_t* __restrict__ active, const typename BlockStore<T>::type* __restrict__ inv,
                         const T* __restrict__ rin, T* z, unsigned int* __restrict__ next,
                         int* __restrict__ status, UpwindMap<T> um, int rhs_cap, int bcap,
                         unsigned long long* __restrict__ trace) {
+    using TB = typename BlockStore<T>::type;
     extern __shared__ __align__(16) unsigned char sraw[];
     T* rhs = reinterpret_cast<T*>(sraw);      // rin, then the couplings c (face nodes)
     T* zpre = rhs + rhs_cap;                  // B rin
@@ -463,7 +491,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
         const int bm = s_rec[kRecFlags] >> 4;
         const int64_t dof_off = rec64(s_rec + kRecDof);
         // ---- independent of the sweep: block inverse, residual, mortars
-        const T* B = inv + rec64(s_rec + kRecInv);
+        const TB* B = inv + rec64(s_rec + kRecInv);
         const int bsize = nth * nn * nn;
         if ((s_rec[kRecOk] & kOkBit) && s_rec[kRecReg + kP] <= um.reg_cap) {
             // ---- one-phase path: zpre = B rin and G_e staged before the wait,
@@ -474,7 +502,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             const int gsz = ld * nloc;             // a multiple of kVec
             T* zl = Bs;
             T* Gs = Bs + ld;
-            T* Bg = Gs + gsz;
+            TB* Bg = reinterpret_cast<TB*>(Gs + gsz);
             const T* Gg = um.G + rec64(s_rec + kRecGoff + 2 * kP);
             const int64_t* up = um.up + rec64(s_rec + kRecUoff);
             for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
@@ -541,18 +569,19 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             }
             continue;
         }
-        const bool staged = bsize <= bcap;
+        const bool staged = block_units<T, TB>(bsize) <= bcap;
+        TB* Bsb = reinterpret_cast<TB*>(Bs);
         if (staged) {   // asynchronous copies: every load in flight at once
-            stage_block(Bs, B, bsize);
+            stage_block(Bsb, B, bsize);
         } else {
             // too large for shared memory: pull the block into L2 now (one
             // prefetch per 128-byte line, all in flight) for the products below
             const char* b0 = reinterpret_cast<const char*>(B);
-            const int64_t nbytes = (int64_t)bsize * sizeof(T);
+            const int64_t nbytes = (int64_t)bsize * sizeof(TB);
             for (int64_t o = (int64_t)threadIdx.x * 128; o < nbytes; o += (int64_t)blockDim.x * 128)
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(b0 + o));
         }
-        const T* Bv = staged ? Bs : B;
+        const TB* Bv = staged ? Bsb : B;
         for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
             const int ij = l / nth;
             rhs[l] = bdry_node_s(bm, ij / ny, ij % ny, nx, ny) ? T(0) : rin[dof_off + l];
@@ -705,17 +734,17 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
         // ---- z = zpre - B c over the face columns of B
         for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
             const int r = t / nn, ij = t % nn;
-            const T* col = Bv + r * nn * nn + ij;
+            const TB* col = Bv + r * nn * nn + ij;
             T a0 = zpre[ij * nth + r], a1 = T(0), a2 = T(0), a3 = T(0);
             int f = 0;
 #pragma unroll 2
             for (; f + 4 <= nf; f += 4) {
-                a0 -= col[s_face[f + 0] * nn] * rhs[s_face[f + 0] * nth + r];
-                a1 -= col[s_face[f + 1] * nn] * rhs[s_face[f + 1] * nth + r];
-                a2 -= col[s_face[f + 2] * nn] * rhs[s_face[f + 2] * nth + r];
-                a3 -= col[s_face[f + 3] * nn] * rhs[s_face[f + 3] * nth + r];
+                a0 -= widen(col[s_face[f + 0] * nn]) * rhs[s_face[f + 0] * nth + r];
+                a1 -= widen(col[s_face[f + 1] * nn]) * rhs[s_face[f + 1] * nth + r];
+                a2 -= widen(col[s_face[f + 2] * nn]) * rhs[s_face[f + 2] * nth + r];
+                a3 -= widen(col[s_face[f + 3] * nn]) * rhs[s_face[f + 3] * nth + r];
             }
-            for (; f < nf; ++f) a0 -= col[s_face[f] * nn] * rhs[s_face[f] * nth + r];
+            for (; f < nf; ++f) a0 -= widen(col[s_face[f] * nn]) * rhs[s_face[f] * nth + r];
             st_relaxed(z + dof_off + (int64_t)ij * nth + r, (a0 + a1) + (a2 + a3));
         }
         // the stored values are the publication (downstream elements wait on
@@ -734,6 +763,12 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             trace[kTr * e + 7] = (unsigned long long)(ck4 - ck3);
         }
     }
+}
+
+// BF16 copy of the FP32 block inverses (round to nearest even), the FP32 sweep's
+__global__ void to_bf16_kernel(const float* __restrict__ in, __nv_bfloat16* __restrict__ out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __float2bfloat16_rn(in[i]);
 }
 
 // Builds the upwind maps G_e = -B_e C_e of the one-phase elements in FP64
@@ -791,6 +826,7 @@ struct Sweep {
     uint8_t* d_active = nullptr;
     double* d_inv64 = nullptr;
     float* d_inv32 = nullptr;
+    __nv_bfloat16* d_inv16 = nullptr;   // the FP32 sweep's copy
     int64_t* d_inv_off = nullptr;
     int64_t inv_entries = 0;
     int max_nloc = 0;
@@ -962,9 +998,9 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             inv_off[e] = hit->second;
             continue;
         }
-        // each distinct block set starts on 4 values (16 bytes in FP32, 32 in
-        // FP64), so that the sweep stages it with 16-byte copies
-        off = (off + 3) & ~int64_t(3);
+        // each distinct block set starts on 8 values (16 bytes in BF16), so
+        // that the sweep stages it with 16-byte copies
+        off = (off + 7) & ~int64_t(7);
         inv_off[e] = off;
         shared.emplace(std::move(key), off);
         for (int r = 0; r < E.nth; ++r) {
@@ -978,8 +1014,13 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     s->d_lev_elems = sw_alloc<int32_t>(s, ne);
     s->d_active = sw_alloc<uint8_t>(s, active.size());
     s->d_inv_off = sw_alloc<int64_t>(s, ne);
-    s->d_inv64 = sw_alloc<double>(s, off);
-    s->d_inv32 = sw_alloc<float>(s, off);
+    // 8 entries of padding past the last block: a staging copy may run past
+    // the end of its block
+    s->d_inv64 = sw_alloc<double>(s, off + 8);
+    s->d_inv32 = sw_alloc<float>(s, off + 8);
+    s->d_inv16 = sw_alloc<__nv_bfloat16>(s, off + 8);
+    RTG_CUDA(cudaMemsetAsync(s->d_inv64, 0, sizeof(double) * (size_t)(off + 8), st));
+    RTG_CUDA(cudaMemsetAsync(s->d_inv32, 0, sizeof(float) * (size_t)(off + 8), st));
     int32_t* d_be = sw_alloc<int32_t>(s, blk_elem.size());
     int32_t* d_br = sw_alloc<int32_t>(s, blk_r.size());
     int64_t* d_bo = sw_alloc<int64_t>(s, blk_off.size());
@@ -1001,6 +1042,9 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
     RTG_CUDA(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     RTG_CUDA(cudaStreamSynchronize(st));
     if (status) throw RtgError{RTG_ERR_NONFINITE, "singular element block in the sweep preconditioner"};
+    to_bf16_kernel<<<std::max<int64_t>(1, std::min<int64_t>((off + 8 + 255) / 256, 152 * 8)), 256, 0, st>>>(
+        s->d_inv32, s->d_inv16, off + 8), count_launch();
+    RTG_CUDA(cudaGetLastError());
     s->d_next = sw_alloc<unsigned int>(s, 1);
     s->d_status = sw_alloc<int>(s, 1);
     RTG_CUDA(cudaMemset(s->d_status, 0, sizeof(int)));
@@ -1046,8 +1090,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             // upwind values (one map row long), G_e, then B_e
             const int64_t bsize = (int64_t)E.nth * C.nx * C.ny * C.nx * C.ny;
             const int64_t ld32 = map_ld<float>((int)nup), ld64 = map_ld<double>((int)nup);
-            const int64_t region32 = ld32 + ld32 * nloc + bsize;
-            const int64_t region64 = ld64 + ld64 * nloc + bsize;
+            const int64_t region32 = ld32 + ld32 * nloc + block_units<float, __nv_bfloat16>((int)bsize);
+            const int64_t region64 = ld64 + ld64 * nloc + block_units<double, double>((int)bsize);
             uint8_t ok = 0;
             if (region32 * 4 + 2 * rhs_cap * 4 <= (int64_t)kSweepSmemBudget) ok |= 1;
             if (region64 * 8 + 2 * rhs_cap * 8 <= (int64_t)kSweepSmemBudget) ok |= 2;
@@ -1245,7 +1289,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
                  const int* stop, bool prefilled) {
     Sweep* s = get_sweep(h, st);
     const bool f64 = sizeof(T) == 8;
-    const T* inv = f64 ? (const T*)s->d_inv64 : (const T*)s->d_inv32;
+    using TB = typename BlockStore<T>::type;
+    const TB* inv = f64 ? (const TB*)(const void*)s->d_inv64 : (const TB*)(const void*)s->d_inv16;
     OpView<T> v = *reinterpret_cast<const OpView<T>*>(f64 ? (const void*)&h->v64 : (const void*)&h->v32);
     v.skip = skip;
     v.stop = stop;
@@ -1278,7 +1323,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
             sh.threads = kShapeThreads[q];
             const size_t rhs_bytes = sizeof(T) * (size_t)(2 * rhs_cap + s->max_c);
             const int64_t fit = (int64_t)((budget - std::min(rhs_bytes, budget)) / sizeof(T));
-            sh.bcap = (int)std::max<int64_t>(0, std::min<int64_t>(s->max_b, fit));
+            sh.bcap = (int)std::max<int64_t>(0, std::min<int64_t>(block_units<T, TB>((int)s->max_b), fit));
             sh.reg_cap = (int)std::max<int64_t>(0, (int64_t)(budget / sizeof(T)) - 2 * rhs_cap);
             const int64_t gmax = std::min<int64_t>(f64 ? s->gmax64 : s->gmax32, sh.reg_cap);
             sh.smem = sizeof(T) * (size_t)(2 * rhs_cap + std::max<int64_t>((int64_t)sh.bcap + s->max_c, gmax));

@@ -62,7 +62,8 @@ def test_sweep_linearity_fullsize():
     z12 = ctx.precondition(2.0 * r1 + 0.5 * r2)
     assert _rel(z12, 2.0 * z1 + 0.5 * z2) < 1e-12
     z1f = ctx.precondition(r1.float(), prec=1).double()
-    assert _rel(z1f, z1) < 1e-5
+    # the FP32 sweep reads BF16 block inverses (about 2e-3 from the FP64 sweep)
+    assert _rel(z1f, z1) < 1e-2
     ctx.close()
 
 

@@ -113,7 +113,8 @@ def test_to_scipy_small():
 
 def test_sweep_preconditioner_properties(case):
     """P^{-1} r: finite, zero at inflow-boundary DOFs, repeatable across calls
-    (the sentinel fill before every sweep), FP32 within 1e-4 of FP64, linear."""
+    (the sentinel fill before every sweep), FP32 (BF16 block inverses) within
+    1e-2 of FP64, linear."""
     import torch
     from rtg import _lib
     name, g, mesh, prob = case
@@ -129,7 +130,7 @@ def test_sweep_preconditioner_properties(case):
         # quad_none's element blocks have no outflow terms and are nearly
         # singular, so FP32 and FP64 sweeps legitimately differ there
         z32 = ctx.precondition(r, prec=_lib.RTG_FP32).cpu().numpy()
-        assert np.linalg.norm(z32 - z1) <= 1e-4 * np.linalg.norm(z1)
+        assert np.linalg.norm(z32 - z1) <= 1e-2 * np.linalg.norm(z1)
     z3 = ctx.precondition(2.5 * r).cpu().numpy()
     assert np.linalg.norm(z3 - 2.5 * z1) <= 1e-12 * np.linalg.norm(z3)
 

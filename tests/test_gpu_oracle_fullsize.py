@@ -14,8 +14,8 @@ direct solve of the same system to 1.4e-14).
   weighted relative L2 norm);
 * the mixed-precision solve (FP32 inner GMRES, FP64 refinement) reaches the
   1e-8 error target against the oracle's solution;
-* the sweep preconditioner in both precisions matches the oracle's sweep to
-  1e-4 (FP32-built element inverses).
+* the sweep preconditioner matches the oracle's sweep to 1e-4 in FP64 (FP32-
+  built element inverses) and to 1e-2 in FP32 (their BF16 copies).
 """
 import numpy as np
 import pytest
@@ -104,7 +104,8 @@ def test_sweep_matches_oracle_sized(sized):
     random residual: these meshes hold conforming elements whose couplings
     take the sweep's diagonal-mortar path, and hanging and angularly refined
     ones that take the mortar sums.  The GPU inverts the element blocks in
-    FP32, so agreement is to about 1e-5; the bound is 1e-4."""
+    FP32, so the FP64 sweep agrees to about 1e-5 (bound 1e-4); the FP32 sweep
+    reads BF16 copies of them, about 2e-3 (bound 1e-2)."""
     from oracle import rt_oracle as O
     from rtg import _lib
     name, o, _, _, ctx, _ = sized
@@ -112,7 +113,7 @@ def test_sweep_matches_oracle_sized(sized):
     rng = np.random.default_rng(23)
     r = np.where(o["mask"], rng.standard_normal(len(o["mask"])), 0.)
     z_ref = P(r)
-    for prec in (_lib.RTG_FP64, _lib.RTG_FP32):
+    for prec, tol in ((_lib.RTG_FP64, 1e-4), (_lib.RTG_FP32, 1e-2)):
         z = ctx.precondition(r, prec=prec).double().cpu().numpy()
         err = np.linalg.norm(z - z_ref) / np.linalg.norm(z_ref)
-        assert err <= 1e-4, (name, prec, err)
+        assert err <= tol, (name, prec, err)
