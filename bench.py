@@ -386,9 +386,9 @@ def profiled_traffic(name):
 
 def sweep_bytes(ctx, prec_bytes):
     """Algorithmic bytes of one sweep kernel: read r, write z, read the element
-    block inverses (BF16 for the FP32 sweep, FP64 for the FP64 one), the upwind
-    maps of the one-phase elements and their upwind value indices (8 bytes
-    each); upwind face values re-read through L2 count 0."""
+    block inverses and the upwind maps of the one-phase elements (both BF16 for
+    the FP32 sweep, FP64 for the FP64 one) and the maps' upwind value indices
+    (8 bytes each); upwind face values re-read through L2 count 0."""
     from rtg import _lib
     lev, lag, inv = C.c_int(), C.c_int(), C.c_int64()
     _lib.check(ctx.lib.rtg_sweep_info(ctx.h, C.byref(lev), C.byref(lag), C.byref(inv), None))
@@ -396,7 +396,7 @@ def sweep_bytes(ctx, prec_bytes):
     prec = _lib.RTG_FP32 if prec_bytes == 4 else _lib.RTG_FP64
     _lib.check(ctx.lib.rtg_sweep_maps(ctx.h, prec, C.byref(one), C.byref(gm), C.byref(up), None))
     blk_bytes = 2 if prec_bytes == 4 else 8
-    total = 2 * prec_bytes * ctx.N + blk_bytes * inv.value + prec_bytes * gm.value + 8 * up.value
+    total = 2 * prec_bytes * ctx.N + blk_bytes * (inv.value + gm.value) + 8 * up.value
     return int(total), int(lev.value), int(lag.value)
 
 

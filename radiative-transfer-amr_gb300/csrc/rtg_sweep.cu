@@ -325,13 +325,28 @@ __global__ void sweep_fill_kernel(OpView<T> v, int ne, T* __restrict__ z, unsign
     }
 }
 
-// Row length (values) of an element's upwind map in precision T: nup rounded
-// up so that a row is a whole number of 16-byte units and the number of units
-// is odd (rows of consecutive outputs then start in different 16-byte bank
-// groups, so 16-byte loads of a quarter warp do not conflict).
+// Storage of the upwind maps a sweep reads: BF16 for the FP32 sweep (like the
+// block inverses: the map only defines the preconditioner, a fixed linear
+// operator), FP64 for the FP64 sweep.  Entries are widened to T on use.
+template <typename T>
+struct MapStore;
+template <>
+struct MapStore<float> {
+    using type = __nv_bfloat16;
+};
+template <>
+struct MapStore<double> {
+    using type = double;
+};
+
+// Row length (entries) of an element's upwind map in the sweep of precision
+// T: nup rounded up so that a row is a whole number of 16-byte units of the
+// stored type and the number of units is odd (rows of consecutive outputs
+// then start in different 16-byte bank groups, so 16-byte loads of a quarter
+// warp do not conflict).
 template <typename T>
 __host__ __device__ __forceinline__ int map_ld(int nup) {
-    constexpr int kVec = 16 / (int)sizeof(T);
+    constexpr int kVec = 16 / (int)sizeof(typename MapStore<T>::type);
     if (nup <= 0) return 0;
     int r = (nup + kVec - 1) / kVec * kVec;
     if ((r / kVec) % 2 == 0) r += kVec;
@@ -368,6 +383,30 @@ __device__ __forceinline__ float map_row(const float* g, const float* zl, int q0
         a1 = fmaf(gv.y, zv.y, a1);
         a2 = fmaf(gv.z, zv.z, a2);
         a3 = fmaf(gv.w, zv.w, a3);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+// BF16 map (the FP32 sweep): a 16-byte unit holds eight entries, widened to
+// FP32 against two 16-byte units of upwind values
+__device__ __forceinline__ float map_row(const __nv_bfloat16* g, const float* zl, int q0, int q1, float acc) {
+    float a0 = acc, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    const uint4* g4 = reinterpret_cast<const uint4*>(g);
+    const float4* z4 = reinterpret_cast<const float4*>(zl);
+    for (int q = q0; q < q1; ++q) {
+        const uint4 gv = g4[q];
+        const float4 za = z4[2 * q], zb = z4[2 * q + 1];
+        const float2 g01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv.x));
+        const float2 g23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv.y));
+        const float2 g45 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv.z));
+        const float2 g67 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&gv.w));
+        a0 = fmaf(g01.x, za.x, a0);
+        a1 = fmaf(g01.y, za.y, a1);
+        a2 = fmaf(g23.x, za.z, a2);
+        a3 = fmaf(g23.y, za.w, a3);
+        a0 = fmaf(g45.x, zb.x, a0);
+        a1 = fmaf(g45.y, zb.y, a1);
+        a2 = fmaf(g67.x, zb.z, a2);
+        a3 = fmaf(g67.y, zb.w, a3);
     }
     return (a0 + a1) + (a2 + a3);
 }
@@ -440,7 +479,7 @@ template <typename T>
 struct UpwindMap {
     int reg_cap = 0;                 // the largest one-phase region this launch's shared memory holds (values)
     const int64_t* up = nullptr;     // upwind value offsets into z
-    const T* G = nullptr;            // maps (this precision's copy)
+    const typename MapStore<T>::type* G = nullptr;   // maps (this precision's copy)
 };
 
 template <typename T>
@@ -496,14 +535,15 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
         if ((s_rec[kRecOk] & kOkBit) && s_rec[kRecReg + kP] <= um.reg_cap) {
             // ---- one-phase path: zpre = B rin and G_e staged before the wait,
             // then z = zpre + G_e z_upwind once the upwind values arrive
-            constexpr int kVec = 16 / sizeof(T);   // values per 16-byte copy
+            using TG = typename MapStore<T>::type;
+            constexpr int kVec = 16 / sizeof(TG);  // map entries per 16-byte copy
             const int nup = s_rec[kRecNup];
-            const int ld = map_ld<T>(nup);
+            const int ld = map_ld<T>(nup);         // upwind values (T) and map row entries (TG)
             const int gsz = ld * nloc;             // a multiple of kVec
             T* zl = Bs;
-            T* Gs = Bs + ld;
+            TG* Gs = reinterpret_cast<TG*>(Bs + ld);
             TB* Bg = reinterpret_cast<TB*>(Gs + gsz);
-            const T* Gg = um.G + rec64(s_rec + kRecGoff + 2 * kP);
+            const TG* Gg = um.G + rec64(s_rec + kRecGoff + 2 * kP);
             const int64_t* up = um.up + rec64(s_rec + kRecUoff);
             for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
             stage_block(Bg, B, bsize);
@@ -772,7 +812,8 @@ __global__ void to_bf16_kernel(const float* __restrict__ in, __nv_bfloat16* __re
 }
 
 // Builds the upwind maps G_e = -B_e C_e of the one-phase elements in FP64
-// (and their FP32 copies; rows of map_ld values, padding left zero): entry
+// (and the FP32 sweep's BF16 copies, rounded to nearest even; rows of map_ld
+// entries, padding left zero): entry
 // (u, l) with u = (coupling k, jj, a) and l = (ij, r) is -dcoeff_k Et_k[a][r] sum_q B_r[ij][f_q] Es_k[jj][q] over the
 // nodes f_q of coupling k's face that are not inflow-boundary nodes.  One CTA
 // per element.
@@ -780,7 +821,7 @@ __global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restr
                                         const double* __restrict__ inv, const int64_t* __restrict__ inv_elem_off,
                                         const int32_t* __restrict__ elems, const int32_t* __restrict__ nup_e,
                                         const int64_t* __restrict__ goff64, const int64_t* __restrict__ goff32,
-                                        double* __restrict__ G64, float* __restrict__ G32) {
+                                        double* __restrict__ G64, __nv_bfloat16* __restrict__ G16) {
     const int e = elems[blockIdx.x];
     const ElemDev E = v.elems[e];
     const ColDev C = v.cols[E.col];
@@ -811,7 +852,7 @@ __global__ void build_upwind_map_kernel(OpView<double> v, const uint8_t* __restr
         }
         const double val = -v.cplc[k] * et * acc;
         G64[goff64[e] + (int64_t)l * map_ld<double>(nup) + u] = val;
-        G32[goff32[e] + (int64_t)l * map_ld<float>(nup) + u] = (float)val;
+        G16[goff32[e] + (int64_t)l * map_ld<float>(nup) + u] = __float2bfloat16_rn((float)val);
     }
 }
 
@@ -852,7 +893,7 @@ struct Sweep {
     int32_t* d_gnup = nullptr;
     int64_t *d_goff64 = nullptr, *d_goff32 = nullptr, *d_uoff = nullptr, *d_up = nullptr;
     double* d_G64 = nullptr;
-    float* d_G32 = nullptr;
+    __nv_bfloat16* d_G16 = nullptr;     // the FP32 sweep's copy
     int64_t gmax32 = 0, gmax64 = 0;     // largest staged region (values) per precision
     int64_t g_entries = 0;
     int n_onephase32 = 0, n_onephase64 = 0;
@@ -1090,7 +1131,9 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             // upwind values (one map row long), G_e, then B_e
             const int64_t bsize = (int64_t)E.nth * C.nx * C.ny * C.nx * C.ny;
             const int64_t ld32 = map_ld<float>((int)nup), ld64 = map_ld<double>((int)nup);
-            const int64_t region32 = ld32 + ld32 * nloc + block_units<float, __nv_bfloat16>((int)bsize);
+            // FP32 sweep: upwind values in FP32, G_e and B_e in BF16 (ld32 is a
+            // multiple of 8, so the map is a whole number of FP32 values)
+            const int64_t region32 = ld32 + ld32 * nloc / 2 + block_units<float, __nv_bfloat16>((int)bsize);
             const int64_t region64 = ld64 + ld64 * nloc + block_units<double, double>((int)bsize);
             uint8_t ok = 0;
             if (region32 * 4 + 2 * rhs_cap * 4 <= (int64_t)kSweepSmemBudget) ok |= 1;
@@ -1148,9 +1191,9 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
         s->d_uoff = sw_alloc<int64_t>(s, ne);
         s->d_up = sw_alloc<int64_t>(s, up.size());
         s->d_G64 = sw_alloc<double>(s, gtot64);
-        s->d_G32 = sw_alloc<float>(s, gtot32);
+        s->d_G16 = sw_alloc<__nv_bfloat16>(s, gtot32);
         RTG_CUDA(cudaMemset(s->d_G64, 0, sizeof(double) * std::max<int64_t>(gtot64, 1)));
-        RTG_CUDA(cudaMemset(s->d_G32, 0, sizeof(float) * std::max<int64_t>(gtot32, 1)));
+        RTG_CUDA(cudaMemset(s->d_G16, 0, sizeof(__nv_bfloat16) * std::max<int64_t>(gtot32, 1)));
         int32_t* d_gel = sw_alloc<int32_t>(s, gel.size());
         RTG_CUDA(cudaMemcpy(s->d_gok, gok.data(), ne, cudaMemcpyHostToDevice));
         RTG_CUDA(cudaMemcpy(s->d_gnup, gnup.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
@@ -1163,7 +1206,7 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             RTG_CUDA(cudaMemcpy(d_gel, gel.data(), sizeof(int32_t) * gel.size(), cudaMemcpyHostToDevice));
             build_upwind_map_kernel<<<(int)gel.size(), 256, 0, st>>>(h->v64, s->d_active, s->d_inv64, s->d_inv_off,
                                                                     d_gel, s->d_gnup, s->d_goff64, s->d_goff32, s->d_G64,
-                                                                    s->d_G32), count_launch();
+                                                                    s->d_G16), count_launch();
             RTG_CUDA(cudaGetLastError());
         }
         // ---- element records in claim order (the words are listed with kRecE)
@@ -1302,7 +1345,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     const int rhs_cap = (std::max(s->max_nloc, 1) + 1) & ~1;   // even: 16-byte aligned region after rhs, zpre
     UpwindMap<T> um;
     um.up = s->d_up;
-    um.G = f64 ? (const T*)s->d_G64 : (const T*)s->d_G32;
+    using TG = typename MapStore<T>::type;
+    um.G = f64 ? (const TG*)(const void*)s->d_G64 : (const TG*)(const void*)s->d_G16;
     auto launch = [&](const Sweep::Shape& sh) {
         um.reg_cap = sh.reg_cap;
         sweep_persistent_kernel<T><<<sh.grid, sh.threads, sh.smem, st>>>(
