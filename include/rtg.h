@@ -195,16 +195,18 @@ int rtg_apply(rtg_handle* h, uint32_t flags, int prec, const void* x, void* y,
  * the candidate list (16, 32 or 64 angular rows per work item; one CTA per
  * column or per work item; one launch, or one launch per shared-memory class
  * of the CTAs; FP32 also, with one CTA per column and 32 or 64 rows, with the
- * scattering product on the tensor cores) is built and the whole apply
- * timed; the fastest is kept.  This returns the
- * FP32 table (host, cap_rows rows of 9 int32: rows per item, items per CTA
- * (0: the whole column), split launches (0/1), tensor-core scattering (0/1),
+ * scattering product on the tensor cores, the scattering CTAs of one angular
+ * mesh next to each other) is built and the whole apply timed; the fastest
+ * is kept.  This returns the FP32 table (host, cap_rows rows of 9 int32: rows
+ * per item, items per CTA (0: the whole column), split launches (0/1),
+ * tensor-core scattering (0: none; 1: scattering CTAs heaviest first; 2:
+ * grouped by angular mesh),
  * chosen (0/1), time in ns (-1: not timed), work items, CTAs, launches) and
  * the number of shapes, tuning first if needed. */
 int rtg_apply_tuning(rtg_handle* h, int32_t* table, int cap_rows, int* nclasses, void* stream);
 /* Fixes the apply plan of one precision to a shape instead of the autotuned
  * one: shape = {rows per item, items per CTA (0: whole column), split
- * launches (0/1), tensor-core scattering (0/1, FP32 only)}; NULL returns to
+ * launches (0/1), tensor-core scattering (0, 1 or 2 as above, FP32 only)}; NULL returns to
  * autotuning on the next apply.  Synchronizes the device and drops the
  * solver's captured graphs (they hold the old plan's launches). */
 int rtg_apply_shape(rtg_handle* h, int prec, const int32_t* shape);
@@ -230,9 +232,9 @@ int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stre
 int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_entries, void* stream);
 /* The sweep's one-phase elements in precision prec (those whose upwind map
  * G_e = -B_e C_e, from upwind face values to the element's values, is applied
- * in one step after the inputs arrive), and the map entries and upwind value
- * indices one sweep in that precision reads; builds the sweep if needed.  Any
- * output may be NULL. */
+ * in one step after the inputs arrive), and the map entries (BF16 in the FP32
+ * sweep, FP64 in the FP64 one) and upwind value indices one sweep in that
+ * precision reads; builds the sweep if needed.  Any output may be NULL. */
 int rtg_sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind_entries,
                    void* stream);
 /* One sweep as rtg_precondition, recording for every element e

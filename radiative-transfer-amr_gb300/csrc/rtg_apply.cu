@@ -1255,7 +1255,9 @@ struct PlanShape {
     int rows = kTileRows;
     int gcap = 0;
     int split = 0;
-    int tc = 0;    // FP32: scattering of the tiled columns on the tensor cores (scat_tc_kernel)
+    int tc = 0;    // FP32: scattering of the tiled columns on the tensor cores (scat_tc_kernel),
+                   // CTAs heaviest first; 2: the same with the columns of one angular mesh in
+                   // consecutive CTAs
 };
 
 // One timed plan shape of the autotuner (time in ns, -1: not run).
@@ -1742,7 +1744,22 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
     p->d_tiles = (TileItem*)up(tv.data(), sizeof(TileItem) * tv.size());
     p->d_tile_cpl = (TileCpl*)up(ent.data(), sizeof(TileCpl) * ent.size());
     p->d_tgroups = (int4*)up(tg.data(), sizeof(int4) * tg.size());
-    std::stable_sort(tcv.begin(), tcv.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    if (tc >= 2) {
+        // columns of one angular mesh read the same W tiles: their CTAs run
+        // next to each other (meshes by total cost, heaviest first), so that
+        // the tiles come from L2 after the first read
+        std::map<int, int64_t> sig_cost;
+        for (auto& pr : tcv) sig_cost[t.cols[pr.second.col].sig] += pr.first;
+        std::stable_sort(tcv.begin(), tcv.end(), [&](auto& a, auto& b) {
+            const int sa = t.cols[a.second.col].sig, sb = t.cols[b.second.col].sig;
+            const int64_t ca = sig_cost[sa], cb = sig_cost[sb];
+            if (ca != cb) return ca > cb;
+            if (sa != sb) return sa < sb;
+            return a.second.row0 < b.second.row0;
+        });
+    } else {
+        std::stable_sort(tcv.begin(), tcv.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    }
     std::vector<TcItem> tci;
     for (auto& pr : tcv) {
         tci.push_back(pr.second);
@@ -1934,10 +1951,12 @@ static ApplyPlan* tune_plan(rtg_handle* h, cudaStream_t s) {
             for (int gcap : {0, 1})
                 for (int split : {0, 1}) shapes.push_back(PlanShape{rows, gcap, split, 0});
         // tensor-core scattering (FP32): one CTA per column, items of 32 or 64
-        // rows (one CTA per item ties with these on the two-scatterer problem
-        // and is left out of the list; rtg_apply_shape can still pin it)
+        // rows, the scattering CTAs of one angular mesh next to each other
+        // (one CTA per item ties with these on the two-scatterer problem, and
+        // the heaviest-first order of the scattering CTAs is 1.7 % slower there;
+        // both are left out of the list, rtg_apply_shape can still pin them)
         if (!f64)
-            for (int rows : {32, 64}) shapes.push_back(PlanShape{rows, 0, 0, 1});
+            for (int rows : {32, 64}) shapes.push_back(PlanShape{rows, 0, 0, 2});
         for (const PlanShape& sh : shapes) {
             ApplyPlan* p = shape_plan<T>(h, sh, par);
             TuneRecord r{sh, 0, -1, p->ntiles, p->tg_begin[kSmemClasses], plan_launches(p)};
@@ -2001,8 +2020,8 @@ int apply_shape(rtg_handle* h, int prec, const int32_t* shape) {
     }
     const PlanShape sh{shape[0], shape[1], shape[2], shape[3]};
     if (sh.rows < 1 || sh.rows > 1024 || sh.gcap < 0 || (sh.split != 0 && sh.split != 1) ||
-        (sh.tc != 0 && sh.tc != 1) || (prec == RTG_FP64 && sh.tc))
-        throw RtgError{RTG_ERR_ARG, "apply shape: rows in [1, 1024], gcap >= 0, split and tc 0 or 1 (tc: FP32 only)"};
+        sh.tc < 0 || sh.tc > 2 || (prec == RTG_FP64 && sh.tc))
+        throw RtgError{RTG_ERR_ARG, "apply shape: rows in [1, 1024], gcap >= 0, split 0 or 1, tc 0, 1 or 2 (tc: FP32 only)"};
     if (prec == RTG_FP64)
         force_shape<double>(h, sh);
     else

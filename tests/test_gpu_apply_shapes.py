@@ -10,8 +10,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-FP32_SHAPES = [(rows, gcap, split, tc) for tc in (0, 1) for rows in (16, 64) for gcap in (0, 1)
-               for split in (0, 1)]
+FP32_SHAPES = ([(rows, gcap, split, tc) for tc in (0, 1) for rows in (16, 64) for gcap in (0, 1)
+                for split in (0, 1)] + [(rows, 0, 0, 2) for rows in (16, 64)])
 FP64_SHAPES = [(rows, gcap, split, 0) for rows in (16, 64) for gcap in (0, 1) for split in (0, 1)]
 
 
@@ -79,6 +79,7 @@ def test_bad_shape_rejected():
     spec = W.manufactured_problem()
     ctx = DeviceContext(mesh, spec.kappa, spec.sigma, spec.Phi)
     for prec, shape in ((_lib.RTG_FP64, (16, 0, 0, 1)), (_lib.RTG_FP32, (0, 0, 0, 0)),
-                        (_lib.RTG_FP32, (16, -1, 0, 0)), (_lib.RTG_FP32, (16, 0, 2, 0))):
+                        (_lib.RTG_FP32, (16, -1, 0, 0)), (_lib.RTG_FP32, (16, 0, 2, 0)),
+                        (_lib.RTG_FP32, (16, 0, 0, 3)), (_lib.RTG_FP64, (16, 0, 0, 2))):
         arr = np.asarray(shape, dtype=np.int32)
         assert ctx.lib.rtg_apply_shape(ctx.h, prec, _lib.ptr(arr, C.c_int32)) == _lib.RTG_ERR_ARG
