@@ -315,7 +315,8 @@ struct TileCpl {
     int stride, es, et;
     float dc;
     int k, tested;
-    int pad[2];               // 64 bytes: copied in 16-byte pieces
+    int diag;                 // bit 0: Es diagonal (m1 == n0, off-diagonal entries exactly 0); bit 1: Et diagonal
+    int pad;                  // 64 bytes: copied in 16-byte pieces
 };
 constexpr int kMaxItemCpl = 96;
 static_assert(sizeof(TileCpl) == 64, "coupling records are copied in 16-byte pieces");
@@ -361,6 +362,19 @@ __device__ __forceinline__ void boundary_node(int f, int nx, int ny, int& i, int
 
 __host__ __device__ __forceinline__ int boundary_nodes(int nx, int ny) {
     return (nx == 1 || ny == 1) ? nx * ny : 2 * (nx + ny) - 4;
+}
+
+// sum_jj Es[jj][q] T[jj][r] of one coupling at face node q, row r; with a
+// diagonal Es its one nonzero term, and with Es and Et both diagonal (no T
+// formed) Es[q][q] (Et[r][r] x_line[q][r]): the same roundings as the full sums,
+// whose other terms are exact zeros
+template <typename T, typename Cpl>
+__device__ __forceinline__ T face_sum(const Cpl& en, const T* Es, const T* Et, const T* Tb, const T* x, int q, int r) {
+    if (en.diag == 3) return Es[q * en.n0 + q] * (Et[r * en.nth + r] * x[en.base + (int64_t)q * en.stride + r]);
+    if (en.diag & 1) return Es[q * en.n0 + q] * Tb[en.toff + q * en.nth + r];
+    T sacc = T(0);
+    for (int jj = 0; jj < en.m1; ++jj) sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+    return sacc;
 }
 
 // four consecutive values from 16-byte-aligned shared memory
@@ -669,23 +683,35 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
         // inflow face fluxes of the item's elements into Fy (the W region is free)
         if (fl.bc) {
             for (int t = threadIdx.x; t < Mp * nijp; t += blockDim.x) Fy[t] = T(0);
-            // T[jj][r] of every coupling, flattened over (coupling, jj, r); t
-            // grows per thread, so the coupling index only moves forward
+            // T[jj][r] = sum_a Et[a][r] x_line[jj][a] of every coupling: one warp
+            // per coupling, its lanes over (jj, r).  Couplings whose Es and Et
+            // are both diagonal (conforming neighbours) have no T: the flux
+            // phase reads their line values directly.  With a diagonal Et the
+            // sum is its one nonzero term (the others add exact zeros).
             {
-                int c = 0;
-                for (int t = threadIdx.x; t < it.ttot; t += blockDim.x) {
-                    while (t >= sc[c].toff + sc[c].m1 * sc[c].nth) ++c;
+                const int lane = threadIdx.x & 31, nwarp = (int)blockDim.x >> 5;
+                const int nent = it.cpl_end - it.cpl_begin;
+                for (int c = (int)threadIdx.x >> 5; c < nent; c += nwarp) {
                     const TileCpl& en = sc[c];
-                    if (kParity && en.tested) continue;   // summed term by term below
-                    const int q = t - en.toff, jj = small_div(q, s_rcp[en.nth]), r = q - jj * en.nth;
+                    if ((kParity && en.tested) || en.diag == 3) continue;   // tested: summed term by term below
+                    const int nth = en.nth, nt1 = en.nt1, cnt = en.m1 * nth;
+                    const bool dt = en.diag & 2;
                     const T* Et = (kParity ? par.mortc : v.mort) + en.et;
-                    const T* xl = x + en.base + (int64_t)jj * en.stride;
-                    // every load of the line issued before the sum (nt1 <= kMaxNodes)
-                    T acc = T(0);
+                    for (int q = lane; q < cnt; q += 32) {
+                        const int jj = small_div(q, s_rcp[nth]), r = q - jj * nth;
+                        const T* xl = x + en.base + (int64_t)jj * en.stride;
+                        T acc = T(0);
+                        if (dt) {
+                            acc = Et[r * nth + r] * xl[r];
+                        } else {
+                            // the loads of up to 8 line values issued before their sum
 #pragma unroll
-                    for (int a = 0; a < kMaxNodes; ++a)
-                        if (a < en.nt1) acc = fma(Et[a * en.nth + r], xl[a], acc);
-                    Tb[t] = acc;
+                            for (int a = 0; a < 8; ++a)
+                                if (a < nt1) acc = fma(Et[a * nth + r], xl[a], acc);
+                            for (int a = 8; a < nt1; ++a) acc = fma(Et[a * nth + r], xl[a], acc);
+                        }
+                        Tb[en.toff + q] = acc;
+                    }
                 }
             }
             __syncthreads();
@@ -733,16 +759,11 @@ apply_tiled_kernel(OpView<T> v, TileParity<T> par, uint32_t flags, const int4* _
                                 }
                             } else {
                                 const T* Es = par.mortc + en.es;
-                                T sacc = T(0);
-                                for (int jj = 0; jj < en.m1; ++jj)
-                                    sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
-                                acc += sacc;
+                                acc += face_sum(en, Es, par.mortc + en.et, Tb, x, q, r);
                             }
                         } else {
                             const T* Es = v.mort + en.es;
-                            T sacc = T(0);
-                            for (int jj = 0; jj < en.m1; ++jj)
-                                sacc = fma(Es[jj * en.n0 + q], Tb[en.toff + jj * en.nth + r], sacc);
+                            const T sacc = face_sum(en, Es, v.mort + en.et, Tb, x, q, r);
                             acc = fma(T(en.dc), sacc, acc);
                         }
                     }
@@ -1276,6 +1297,7 @@ struct ParityTables {
     uint64_t* d_thr = nullptr;
     std::vector<int> esc, etc;     // per coupling: offsets of dcoeff*Es and Et in the cleaned table
     std::vector<char> tested;      // per coupling: summed term by term
+    std::vector<uint8_t> diag;     // per coupling: cleaned Es (bit 0) / Et (bit 1) diagonal
     int64_t nodes[4] = {0, 0, 0, 0};   // nodes per scattering class
     int64_t ntested = 0;
 };
@@ -1314,6 +1336,25 @@ static void free_parity(const ParityTables* pt) {
     cudaFree(pt->d_colfull);
     cudaFree(pt->d_thr);
     delete pt;
+}
+
+// 1 when an m x n mortar block (row-major) is square with exact zeros off the
+// diagonal
+template <typename V>
+static uint8_t mortar_diag(const V* b, int m, int n) {
+    if (m != n) return 0;
+    for (int a = 0; a < m; ++a)
+        for (int c = 0; c < n; ++c)
+            if (a != c && b[a * n + c] != V(0)) return 0;
+    return 1;
+}
+// the same for a block with the entries flagged in z zeroed
+static uint8_t mortar_diag_clean(const double* b, const std::vector<char>& z, int m, int n) {
+    if (m != n) return 0;
+    for (int a = 0; a < m; ++a)
+        for (int c = 0; c < n; ++c)
+            if (a != c && !z[a * n + c] && b[a * n + c] != 0.) return 0;
+    return 1;
 }
 
 // Resolves the FP64 drop rules of the tiled path on the host, with the same
@@ -1398,6 +1439,7 @@ static ParityTables* build_parity(const rtg_handle* h) {
     pt->esc.assign(ncpl, 0);
     pt->etc.assign(ncpl, 0);
     pt->tested.assign(ncpl, 0);
+    pt->diag.assign(ncpl, 0);
     std::map<std::pair<int, std::vector<char>>, int> et_seen;   // (Et offset, zeroed entries) -> offset
     for (int e = 0; e < (int)t.elems.size(); ++e) {
         const ElemDev& E = t.elems[e];
@@ -1444,6 +1486,8 @@ static ParityTables* build_parity(const rtg_handle* h) {
             }
             pt->esc[k] = (int)mortc.size();
             for (int q = 0; q < nes; ++q) mortc.push_back(esz[q] ? 0. : des[q]);
+            pt->diag[k] = mortar_diag(mortc.data() + pt->esc[k], g.m1, n0) |
+                          (mortar_diag_clean(et, etz, g.nth1, E.nth) << 1);
             auto key = std::make_pair((int)cp.et, etz);
             auto f = et_seen.find(key);
             if (f != et_seen.end()) {
@@ -1600,6 +1644,16 @@ static ApplyPlan* make_plan(const rtg_handle* h, const std::vector<int>* cap = n
                             tc.dc = (float)t.cplc[kk];
                             tc.k = kk;
                             tc.tested = parity ? par->tested[kk] : 0;
+                            if (parity) {
+                                tc.diag = tc.tested ? 0 : par->diag[kk];
+                            } else {
+                                // the FP32 tables are the FP32 roundings of these
+                                std::vector<float> es32(g.m1 * tc.n0), et32(g.nth1 * E.nth);
+                                for (size_t q = 0; q < es32.size(); ++q) es32[q] = (float)t.mort[cp.es + q];
+                                for (size_t q = 0; q < et32.size(); ++q) et32[q] = (float)t.mort[cp.et + q];
+                                tc.diag = mortar_diag(es32.data(), g.m1, tc.n0) |
+                                          (mortar_diag(et32.data(), g.nth1, E.nth) << 1);
+                            }
                             en.push_back(tc);
                             tsz += g.m1 * E.nth;
                         }
