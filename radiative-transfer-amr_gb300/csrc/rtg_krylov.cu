@@ -2,7 +2,8 @@
 // (rt/solve.py:81-132).  Vectors stay full length (N) with the inflow-boundary
 // entries held at zero, so every product is one masked operator apply.
 //
-//  * method 0 (plain): GMRES(m) in FP64, CGS2 Arnoldi, Givens on the host.
+//  * method 0 (plain): GMRES(m) in FP64, classical Gram-Schmidt Arnoldi (one
+//    projection, PETSc's default), Givens on the device.
 //  * method 1 (mixed): FP64 iterative refinement around FP32 GMRES(m): the
 //    true residual r = b - A x is formed with the FP64 operator, the
 //    correction A d = r is solved with FP32 applies and FP32 basis vectors
@@ -123,7 +124,7 @@ __global__ void multi_dot_kernel(const T* __restrict__ V, int64_t ldv, int k, co
 // step, 3 non-finite); a nonzero code raises *stop so that the step after it
 // does nothing.
 struct ArnoldiState {
-    const double* hcol;   // projections of the step (h1 + h2)
+    const double* hcol;   // projections of the step
     double* H;
     double* cs;
     double* sn;
@@ -167,25 +168,24 @@ __device__ void arnoldi_update(const ArnoldiState a_st, const double* hcol, doub
     if (code) *stop = code;
 }
 
-// Fused Gram-Schmidt pass: w -= sum_{q<k} h[q] V_q, then out[q] = <V_q, w>
-// for q < k (kNorm false) or out[0] = <w, w> (kNorm true), with one read of V
-// and w.  Reductions as in multi_dot_kernel (last block, fixed order).
+// Fused Gram-Schmidt pass: w -= sum_{q<k} h[q] V_q, then out[0] = <w, w>
+// and, for a device-driven step, the Arnoldi update, with one read of V and
+// w.  Reductions as in multi_dot_kernel (last block, fixed order).
 constexpr int kFuseMax = 32;   // vectors of the fused pass (longer bases use the separate kernels)
 
-template <typename T, bool kNorm>
+template <typename T>
 __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k,
                                 const double* __restrict__ h, int64_t n, double* __restrict__ partial,
                                 unsigned int* __restrict__ ticket, double* __restrict__ out,
-                                const double* __restrict__ add, double* __restrict__ out_sum,
                                 const int* __restrict__ stop, ArnoldiState ast) {
-    constexpr int K = kNorm ? 1 : kFuseMax;
+    constexpr int K = 1;
     if (stop && *stop) return;
     __shared__ Acc<T> hs[kFuseMax];
     __shared__ double red[K][kRedThreads / 32];
     __shared__ int s_last;
     if ((int)threadIdx.x < k) hs[threadIdx.x] = (Acc<T>)h[threadIdx.x];
     __syncthreads();
-    const int nout = kNorm ? 1 : k;
+    const int nout = 1;
     Acc<T> acc[K];
 #pragma unroll
     for (int q = 0; q < K; ++q) acc[q] = Acc<T>(0);
@@ -201,14 +201,7 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
                 if (q0 + q < k) sv = fma(-hs[q0 + q], (Acc<T>)vv[q], sv);
         }
         w[i] = (T)sv;
-        if (kNorm) {
-            acc[0] = fma(sv, sv, acc[0]);
-        } else {
-            // the second read of V_q[i] hits the cache line the first one loaded
-#pragma unroll
-            for (int q = 0; q < K; ++q)
-                if (q < k) acc[q] = fma((Acc<T>)V[(int64_t)q * ldv + i], sv, acc[q]);
-        }
+        acc[0] = fma(sv, sv, acc[0]);
     }
 #pragma unroll
     for (int q = 0; q < K; ++q) {
@@ -236,9 +229,8 @@ __global__ void axpy_dot_kernel(T* __restrict__ w, const T* __restrict__ V, int6
         for (int o = 16; o > 0; o >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, o);
         if (lane == 0) {
             out[q] = sq;
-            if (add) out_sum[q] = sq + add[q];
             // the norm pass of a device-driven step ends with the Arnoldi update
-            if (kNorm && ast.H) arnoldi_update(ast, ast.hcol, sqrt(sq));
+            if (ast.H) arnoldi_update(ast, ast.hcol, sqrt(sq));
         }
     }
     if (threadIdx.x == 0) *ticket = 0u;
@@ -308,12 +300,6 @@ __device__ __forceinline__ void block_reduce_out(const T (&acc)[NO], int nout, d
 template <int KMAX>
 __host__ __device__ constexpr int pack_group() { return KMAX <= 16 ? KMAX : 8; }
 
-// Blocks of kRedThreads per SM the register budget aims at: one where the
-// FP64 update-and-dot pass keeps 16 or more accumulators in doubles besides
-// its packs (the 128-register cap of two blocks would spill), two elsewhere.
-template <typename T, int KMAX, bool kNorm>
-__host__ __device__ constexpr int vec_min_blocks() { return !kNorm && sizeof(T) == 8 && KMAX >= 16 ? 1 : 2; }
-
 // multi_dot_kernel with 16-byte loads: out[q] = <V_q, w> for q < k <= KMAX.
 // Each thread takes Pack<T>::n consecutive entries per step, the loads of up
 // to 16 basis vectors issued before their FMAs; the last block also takes
@@ -361,19 +347,16 @@ __global__ void __launch_bounds__(kRedThreads, 2) multi_dot_vec_kernel(
 }
 
 // axpy_dot_kernel with 16-byte loads: w -= sum_{q<k} h[q] V_q, then
-// out[q] = <V_q, w> (kNorm false) or out[0] = <w, w> (kNorm true).  With at
-// most 16 basis vectors a thread keeps the packs it loaded for the dot
-// products; with more, the second read of V_q hits the cache.  The update
-// subtracts the terms in q order, as the scalar kernel does.
-template <typename T, int KMAX, bool kNorm>
-__global__ void __launch_bounds__(kRedThreads, vec_min_blocks<T, KMAX, kNorm>()) axpy_dot_vec_kernel(
+// out[0] = <w, w> and the Arnoldi update.  The update subtracts the terms in
+// q order, as the scalar kernel does.
+template <typename T, int KMAX>
+__global__ void __launch_bounds__(kRedThreads, 2) axpy_dot_vec_kernel(
     T* __restrict__ w, const T* __restrict__ V, int64_t ldv, int k, const double* __restrict__ h, int64_t n,
     double* __restrict__ partial, unsigned int* __restrict__ ticket, double* __restrict__ out,
-    const double* __restrict__ add, double* __restrict__ out_sum, const int* __restrict__ stop, ArnoldiState ast) {
+    const int* __restrict__ stop, ArnoldiState ast) {
     constexpr int P = Pack<T>::n;
-    constexpr int NO = kNorm ? 1 : KMAX;
+    constexpr int NO = 1;
     constexpr int G = pack_group<KMAX>();
-    constexpr bool kKeep = KMAX == G;
     if (stop && *stop) return;
     __shared__ T hs[KMAX];
     if ((int)threadIdx.x < k) hs[threadIdx.x] = (T)h[threadIdx.x];
@@ -399,18 +382,8 @@ __global__ void __launch_bounds__(kRedThreads, vec_min_blocks<T, KMAX, kNorm>())
                 }
         }
         *reinterpret_cast<Pack<T>*>(w + c * P) = sv;
-        if (kNorm) {
 #pragma unroll
-            for (int e = 0; e < P; ++e) acc[0] = fma(sv.v[e], sv.v[e], acc[0]);
-        } else {
-#pragma unroll
-            for (int q = 0; q < NO; ++q)
-                if (q < k) {
-                    const Pack<T> vq = kKeep ? vp[q % G] : load_pack(V + (int64_t)q * ldv + c * P);
-#pragma unroll
-                    for (int e = 0; e < P; ++e) acc[q] = fma(vq.v[e], sv.v[e], acc[q]);
-                }
-        }
+        for (int e = 0; e < P; ++e) acc[0] = fma(sv.v[e], sv.v[e], acc[0]);
     }
     if (blockIdx.x == gridDim.x - 1) {
         const int64_t i = np * P + threadIdx.x;
@@ -420,16 +393,10 @@ __global__ void __launch_bounds__(kRedThreads, vec_min_blocks<T, KMAX, kNorm>())
             for (int q = 0; q < KMAX; ++q)
                 if (q < k) si = fma(-hs[q], V[(int64_t)q * ldv + i], si);
             w[i] = si;
-            if (kNorm) {
-                acc[0] = fma(si, si, acc[0]);
-            } else {
-#pragma unroll
-                for (int q = 0; q < NO; ++q)
-                    if (q < k) acc[q] = fma(V[(int64_t)q * ldv + i], si, acc[q]);
-            }
+            acc[0] = fma(si, si, acc[0]);
         }
     }
-    block_reduce_out<T, NO>(acc, kNorm ? 1 : k, partial, ticket, out, add, out_sum, kNorm ? &ast : nullptr);
+    block_reduce_out<T, NO>(acc, 1, partial, ticket, out, nullptr, nullptr, &ast);
 }
 
 // w -= sum_q h[q] V_q
@@ -564,7 +531,7 @@ struct Workspace {
     // grids of the 16-byte Gram-Schmidt kernels (blocks resident on every SM,
     // at most kRedBlocks): [FP64][KMAX 8, 16, 32] and [FP64][KMAX][norm pass]
     int gdot[2][3] = {};
-    int gaxd[2][3][2] = {};
+    int gaxd[2][3] = {};
     double* partial = nullptr;  // kRedBlocks x (m+1)
     unsigned int* ticket = nullptr;   // last-block ticket of multi_dot_kernel (0 between launches)
     // device Arnoldi state of the lagged-check inner loop
@@ -577,7 +544,7 @@ struct Workspace {
     std::map<std::tuple<int, int, int, int>, std::pair<cudaGraphExec_t, long long>> graphs;   // exec, kernels
     cudaStream_t cap = nullptr;       // capture stream
     bool warm[2] = {false, false};    // a cycle ran uncaptured (plans and launch shapes exist), per precision
-    double* hdev = nullptr;     // h1 [m+2], h2 [m+2], hout [m+2], nrm [1]
+    double* hdev = nullptr;     // y of the cycle's update [m+2], (unused) [m+2], projections [m+2], nrm [1]
     double* hhost = nullptr;    // pinned
     // the last Arnoldi cycle with at least one step: its j x j triangular
     // factor R (Givens-reduced Hessenberg, columns m + 1 apart) is in dH
@@ -666,18 +633,12 @@ void init_vec_grids(Workspace* ws) {
     ws->gdot[1][0] = resident_grid((const void*)multi_dot_vec_kernel<double, 8>);
     ws->gdot[1][1] = resident_grid((const void*)multi_dot_vec_kernel<double, 16>);
     ws->gdot[1][2] = resident_grid((const void*)multi_dot_vec_kernel<double, 32>);
-    ws->gaxd[0][0][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 8, false>);
-    ws->gaxd[0][1][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 16, false>);
-    ws->gaxd[0][2][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 32, false>);
-    ws->gaxd[0][0][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 8, true>);
-    ws->gaxd[0][1][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 16, true>);
-    ws->gaxd[0][2][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 32, true>);
-    ws->gaxd[1][0][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 8, false>);
-    ws->gaxd[1][1][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 16, false>);
-    ws->gaxd[1][2][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 32, false>);
-    ws->gaxd[1][0][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 8, true>);
-    ws->gaxd[1][1][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 16, true>);
-    ws->gaxd[1][2][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 32, true>);
+    ws->gaxd[0][0] = resident_grid((const void*)axpy_dot_vec_kernel<float, 8>);
+    ws->gaxd[0][1] = resident_grid((const void*)axpy_dot_vec_kernel<float, 16>);
+    ws->gaxd[0][2] = resident_grid((const void*)axpy_dot_vec_kernel<float, 32>);
+    ws->gaxd[1][0] = resident_grid((const void*)axpy_dot_vec_kernel<double, 8>);
+    ws->gaxd[1][1] = resident_grid((const void*)axpy_dot_vec_kernel<double, 16>);
+    ws->gaxd[1][2] = resident_grid((const void*)axpy_dot_vec_kernel<double, 32>);
 }
 
 // the 16-byte kernels take vectors that start on 16-byte boundaries, ldv apart
@@ -711,27 +672,27 @@ void dots(Workspace* ws, const T* V, int64_t ldv, int k, const T* w, int64_t n, 
     count_launch();
 }
 
-// w -= V h over k <= 32 vectors fused with out = V^T w (kNorm false) or
-// out[0] = <w, w> and the Arnoldi update of ast (kNorm true)
-template <typename T, bool kNorm>
+// w -= V h over k <= 32 vectors fused with out[0] = <w, w> and the Arnoldi
+// update of ast
+template <typename T>
 void axpy_dot(Workspace* ws, T* w, const T* V, int64_t ldv, int k, const double* h, int64_t n, double* out,
-              const double* add, double* out_sum, const int* stop, ArnoldiState ast, cudaStream_t s) {
+              const int* stop, ArnoldiState ast, cudaStream_t s) {
     if (!packed(V, ldv) || !packed((const T*)w, 0)) {
-        axpy_dot_kernel<T, kNorm><<<kRedBlocks, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket,
-                                                                    out, add, out_sum, stop, ast), count_launch();
+        axpy_dot_kernel<T><<<kRedBlocks, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out, stop,
+                                                             ast), count_launch();
         return;
     }
     const int ki = kmax_index(k);
-    const int g = ws->gaxd[sizeof(T) == 8][ki][kNorm ? 1 : 0];
+    const int g = ws->gaxd[sizeof(T) == 8][ki];
     if (ki == 0)
-        axpy_dot_vec_kernel<T, 8, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
-                                                                   add, out_sum, stop, ast);
+        axpy_dot_vec_kernel<T, 8><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out, stop,
+                                                            ast);
     else if (ki == 1)
-        axpy_dot_vec_kernel<T, 16, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
-                                                                    add, out_sum, stop, ast);
+        axpy_dot_vec_kernel<T, 16><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out, stop,
+                                                             ast);
     else
-        axpy_dot_vec_kernel<T, 32, kNorm><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out,
-                                                                    add, out_sum, stop, ast);
+        axpy_dot_vec_kernel<T, 32><<<g, kRedThreads, 0, s>>>(w, V, ldv, k, h, n, ws->partial, ws->ticket, out, stop,
+                                                             ast);
     count_launch();
 }
 
@@ -807,8 +768,6 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
     // r = rhs - A x = rhs (x = 0)
     int total = 0;
     bool first = true;
-    double* h1 = ws->hdev;
-    double* h2 = ws->hdev + (m + 2);
     double* ho = ws->hdev + 2 * (m + 2);
     double* nr = ws->hdev + 3 * (m + 2);
     while (total < max_it) {
@@ -870,16 +829,17 @@ GmresResult gmres(rtg_handle* h, Workspace* ws, const T* rhs, T* xT, T* wbuf, T*
             } else {
                 launch_apply<T>(h, vs, RTG_SYSTEM | RTG_MASK_ROWS, vj, wbuf, s);
             }
-            // classical Gram-Schmidt, twice (CGS2); ho = h1 + h2
-            dots<T>(ws, V, ld, j + 1, wbuf, N, h1, nullptr, nullptr, s, stop);
+            // classical Gram-Schmidt, one projection, as PETSc's GMRES does by
+            // default (KSPGMRESClassicalGramSchmidtOrthogonalization without
+            // refinement; the reference's rt/solve.py:80-100 calls it): ho =
+            // V^T w, then w -= V ho with ||w||^2.  On the two-scatterer problem
+            // it takes the iterations and reaches the errors of two projections
+            // in both precisions (one read of V per step less)
+            dots<T>(ws, V, ld, j + 1, wbuf, N, ho, nullptr, nullptr, s, stop);
             if (j + 1 <= kFuseMax) {
-                // w -= V h1 fused with h2 = V^T w; then w -= V h2 fused with ||w||^2
-                axpy_dot<T, false>(ws, wbuf, V, ld, j + 1, h1, N, h2, h1, ho, stop, ArnoldiState{}, s);
-                axpy_dot<T, true>(ws, wbuf, V, ld, j + 1, h2, N, nr, nullptr, nullptr, stop, ast, s);
+                axpy_dot<T>(ws, wbuf, V, ld, j + 1, ho, N, nr, stop, ast, s);
             } else {
-                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ld, j + 1, h1, N), count_launch();
-                dots<T>(ws, V, ld, j + 1, wbuf, N, h2, h1, ho, s);
-                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ld, j + 1, h2, N), count_launch();
+                multi_axpy_kernel<T><<<grid_for(N), 256, 0, s>>>(wbuf, V, ld, j + 1, ho, N), count_launch();
                 dots<T>(ws, wbuf, 0, 1, wbuf, N, nr, nullptr, nullptr, s);
             }
             T* zn = (flex && j + 1 < m) ? Z + (int64_t)(j + 1) * ld : nullptr;
