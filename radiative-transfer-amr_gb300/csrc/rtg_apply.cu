@@ -19,6 +19,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
+#include <future>
 #include <map>
 #include <string>
 #include <tuple>
@@ -2011,14 +2013,40 @@ static ApplyPlan* tune_plan(rtg_handle* h, cudaStream_t s) {
         // both are left out of the list, rtg_apply_shape can still pin them)
         if (!f64)
             for (int rows : {32, 64}) shapes.push_back(PlanShape{rows, 0, 0, 2});
-        for (const PlanShape& sh : shapes) {
-            ApplyPlan* p = shape_plan<T>(h, sh, par);
+        // the plans are built on host threads at once (host tables read only;
+        // each thread makes its own uploads), then timed one by one
+        int dev = 0;
+        RTG_CUDA(cudaGetDevice(&dev));
+        std::vector<std::future<ApplyPlan*>> built;
+        for (const PlanShape& sh : shapes)
+            built.push_back(std::async(std::launch::async, [h, sh, par, dev]() {
+                RTG_CUDA(cudaSetDevice(dev));
+                return shape_plan<T>(h, sh, par);
+            }));
+        std::vector<ApplyPlan*> plans(shapes.size(), nullptr);
+        std::exception_ptr failed;
+        for (size_t q = 0; q < built.size(); ++q) {
+            try {
+                plans[q] = built[q].get();
+            } catch (...) {
+                if (!failed) failed = std::current_exception();
+            }
+        }
+        if (failed) {
+            for (ApplyPlan* p : plans) free_plan(p);
+            std::rethrow_exception(failed);
+        }
+        for (size_t q = 0; q < shapes.size(); ++q) {
+            const PlanShape& sh = shapes[q];
+            ApplyPlan* p = plans[q];
+            plans[q] = nullptr;
             TuneRecord r{sh, 0, -1, p->ntiles, p->tg_begin[kSmemClasses], plan_launches(p)};
             float tt = 1e30f;
             try {
                 tt = time_plan<T>(h, p, x, y, e0, e1, s);
             } catch (...) {
                 free_plan(p);
+                for (ApplyPlan* rest : plans) free_plan(rest);
                 throw;
             }
             r.ns = (int)std::min(tt * 1e6f, 2.e9f);

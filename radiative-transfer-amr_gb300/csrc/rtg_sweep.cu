@@ -1377,13 +1377,15 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
                                                                    sh.smem));
             sh.grid = std::max(1, std::min<int>((int)h->host.elems.size(), std::max(per_sm, 1) * nsm));
         }
-        // time each (after one warm-up); a smaller budget must win by 3 %
+        // time each: rounds over all shapes (so that a drift of the clocks
+        // meets every shape alike), the first round a warm-up, best of the
+        // other five; a smaller budget must win by 3 %
         cudaEvent_t e0, e1;
         RTG_CUDA(cudaEventCreate(&e0));
         RTG_CUDA(cudaEventCreate(&e1));
-        for (int q = 0; q < kSweepShapes; ++q) {
-            float best = 1e30f;
-            for (int rep = 0; rep < 3; ++rep) {
+        for (int q = 0; q < kSweepShapes; ++q) s->shape_ms[pi][q] = 1e30f;
+        for (int rep = 0; rep < 6; ++rep)
+            for (int q = 0; q < kSweepShapes; ++q) {
                 sweep_fill_kernel<T><<<std::max(1, std::min((int)h->host.elems.size(), 152 * 8)), 256, 0, st>>>(
                     v, (int)h->host.elems.size(), z, s->d_next), count_launch();
                 RTG_CUDA(cudaEventRecord(e0, st));
@@ -1392,10 +1394,8 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
                 RTG_CUDA(cudaEventSynchronize(e1));
                 float ms = 0.f;
                 RTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (rep > 0) best = std::min(best, ms);
+                if (rep > 0) s->shape_ms[pi][q] = std::min(s->shape_ms[pi][q], ms);
             }
-            s->shape_ms[pi][q] = best;
-        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         int best_q = 0;
