@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0, help="profile mode: two-scatterer recipe scale")
     ap.add_argument("--rtol", type=float, default=1e-9, help="profile mode: solver tolerance")
     ap.add_argument("--max-it", type=int, default=3000, help="profile mode: iteration cap")
+    ap.add_argument("--fp32-shape", default=None,
+                    help="profile mode: pin the FP32 apply plan, 'rows,gcap,split,tc' (rtg_apply_shape)")
     return ap.parse_args()
 
 
@@ -77,7 +79,9 @@ def run_profile(args):
     solve_mixed, solve_plain (one solve to --rtol each), apply_fp32,
     sweep_fp32, apply_fp64, sweep_fp64 -- so that ncu --nvtx --nvtx-include
     "<name>/" captures exactly one piece.  --scale < 1 takes the two-scatterer
-    recipe with fewer refinement rounds (a smaller case of the same kernels)."""
+    recipe with fewer refinement rounds (a smaller case of the same kernels);
+    --fp32-shape pins the FP32 apply plan (e.g. the tensor-core plan, which
+    the autotuner picks at full size only)."""
     import torch
     from rtg import Problem, _lib, learned as LN, workloads as W
     torch.cuda.set_device(0)
@@ -87,6 +91,9 @@ def run_profile(args):
         _, mesh, spec = workload(args.workload)
     prob = Problem(spec.kappa, spec.sigma, spec.Phi, spec.f, spec.bcs_dirac)
     ctx = prob.context(mesh)
+    if args.fp32_shape:
+        shape = np.asarray([int(v) for v in args.fp32_shape.split(",")], dtype=np.int32)
+        _lib.check(ctx.lib.rtg_apply_shape(ctx.h, _lib.RTG_FP32, _lib.ptr(shape, C.c_int32)))
     LN.set_params(ctx, LN.load(LN.DEFAULT_NET)[0])
     f_dev = ctx.forcing(spec.f)
     g_dev = ctx.inflow(spec.bcs_dirac)
