@@ -232,9 +232,11 @@ int rtg_precondition(rtg_handle* h, int prec, const void* r, void* z, void* stre
 int rtg_sweep_info(rtg_handle* h, int* levels, int* lagged, int64_t* inverse_entries, void* stream);
 /* The sweep's one-phase elements in precision prec (those whose upwind map
  * G_e = -B_e C_e, from upwind face values to the element's values, is applied
- * in one step after the inputs arrive), and the map entries (BF16 in the FP32
- * sweep, FP64 in the FP64 one) and upwind value indices one sweep in that
- * precision reads; builds the sweep if needed.  Any output may be NULL. */
+ * in one step after the inputs arrive: the elements with a map that fits the
+ * launch shape the first sweep in that precision chose, or before it every
+ * element with a map), and the map entries (BF16 in the FP32 sweep, FP64 in
+ * the FP64 one) and upwind value indices one sweep in that precision reads;
+ * builds the sweep if needed.  Any output may be NULL. */
 int rtg_sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind_entries,
                    void* stream);
 /* One sweep as rtg_precondition, recording for every element e

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <queue>
 #include <unordered_map>
 #include <vector>
@@ -477,7 +478,9 @@ __device__ __forceinline__ void stage_block(TB* dst, const TB* src, int n) {
 
 template <typename T>
 struct UpwindMap {
-    int reg_cap = 0;                 // the largest one-phase region this launch's shared memory holds (values)
+    int reg_cap = 0;                 // the largest one-phase region (upwind values and map) this launch takes (values)
+    int stage_cap = 0;               // values of shared memory after rhs and zpre: a one-phase element whose
+                                     // region and block inverse fit stages the inverse too
     const int64_t* up = nullptr;     // upwind value offsets into z
     const typename MapStore<T>::type* G = nullptr;   // maps (this precision's copy)
 };
@@ -546,7 +549,11 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             const TG* Gg = um.G + rec64(s_rec + kRecGoff + 2 * kP);
             const int64_t* up = um.up + rec64(s_rec + kRecUoff);
             for (int t = threadIdx.x; t < gsz / kVec; t += blockDim.x) cp_async16(Gs + t * kVec, Gg + t * kVec);
-            stage_block(Bg, B, bsize);
+            // B is read once here (B rin, before the wait): staged with the map
+            // when both fit, else read where it lies (coalesced over ij)
+            const bool bstaged = s_rec[kRecReg + kP] + block_units<T, TB>(bsize) <= um.stage_cap;
+            if (bstaged) stage_block(Bg, B, bsize);
+            const TB* Bv = bstaged ? Bg : B;
             for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
                 const int ij = l / nth;
                 rhs[l] = bdry_node_s(bm, ij / ny, ij % ny, nx, ny) ? T(0) : rin[dof_off + l];
@@ -556,7 +563,7 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
             __syncthreads();
             for (int t = threadIdx.x; t < nloc; t += blockDim.x) {
                 const int r = t / nn, ij = t % nn;
-                zpre[ij * nth + r] = strided_dot(Bg + r * nn * nn + ij, nn, rhs + r, nth, nn);
+                zpre[ij * nth + r] = strided_dot(Bv + r * nn * nn + ij, nn, rhs + r, nth, nn);
             }
             long long ck0 = 0, ck1 = 0;
             if (trace && threadIdx.x == 0) {
@@ -894,10 +901,15 @@ struct Sweep {
     int64_t *d_goff64 = nullptr, *d_goff32 = nullptr, *d_uoff = nullptr, *d_up = nullptr;
     double* d_G64 = nullptr;
     __nv_bfloat16* d_G16 = nullptr;     // the FP32 sweep's copy
-    int64_t gmax32 = 0, gmax64 = 0;     // largest staged region (values) per precision
+    int64_t gmax32 = 0, gmax64 = 0;     // largest one-phase region with its block inverse (values) per precision
     int64_t g_entries = 0;
-    int n_onephase32 = 0, n_onephase64 = 0;
-    int64_t g_read[2] = {0, 0}, up_read[2] = {0, 0};   // per sweep (FP32, FP64): map entries and upwind indices read
+    // per precision (FP32, FP64), the elements with a map: the region the map
+    // and the upwind values take (values), map entries, upwind indices; a
+    // launch shape uses the maps whose region fits it
+    struct MapUse {
+        int64_t region, entries, nup;
+    };
+    std::vector<MapUse> onephase[2];
 };
 
 namespace {
@@ -1131,10 +1143,13 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
             // upwind values (one map row long), G_e, then B_e
             const int64_t bsize = (int64_t)E.nth * C.nx * C.ny * C.nx * C.ny;
             const int64_t ld32 = map_ld<float>((int)nup), ld64 = map_ld<double>((int)nup);
-            // FP32 sweep: upwind values in FP32, G_e and B_e in BF16 (ld32 is a
-            // multiple of 8, so the map is a whole number of FP32 values)
-            const int64_t region32 = ld32 + ld32 * nloc / 2 + block_units<float, __nv_bfloat16>((int)bsize);
-            const int64_t region64 = ld64 + ld64 * nloc + block_units<double, double>((int)bsize);
+            // FP32 sweep: upwind values in FP32, G_e in BF16 (ld32 is a multiple
+            // of 8, so the map is a whole number of FP32 values); B_e (read
+            // once, before the wait) joins them in shared memory when it fits
+            const int64_t region32 = ld32 + ld32 * nloc / 2;
+            const int64_t region64 = ld64 + ld64 * nloc;
+            const int64_t with_b32 = region32 + block_units<float, __nv_bfloat16>((int)bsize);
+            const int64_t with_b64 = region64 + block_units<double, double>((int)bsize);
             uint8_t ok = 0;
             if (region32 * 4 + 2 * rhs_cap * 4 <= (int64_t)kSweepSmemBudget) ok |= 1;
             if (region64 * 8 + 2 * rhs_cap * 8 <= (int64_t)kSweepSmemBudget) ok |= 2;
@@ -1170,13 +1185,10 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
                 for (int jj = 0; jj < g.m1; ++jj)
                     for (int a = 0; a < g.nth1; ++a) up.push_back(g.base + (int64_t)jj * g.stride + a);
             }
-            if (ok & 1) s->gmax32 = std::max(s->gmax32, region32), ++s->n_onephase32;
-            if (ok & 2) s->gmax64 = std::max(s->gmax64, region64), ++s->n_onephase64;
+            if (ok & 1) s->gmax32 = std::max(s->gmax32, with_b32);
+            if (ok & 2) s->gmax64 = std::max(s->gmax64, with_b64);
             for (int p = 0; p < 2; ++p)
-                if (ok & (1 << p)) {
-                    s->g_read[p] += (p ? ld64 : ld32) * nloc;
-                    s->up_read[p] += nup;
-                }
+                if (ok & (1 << p)) s->onephase[p].push_back({p ? region64 : region32, (p ? ld64 : ld32) * nloc, nup});
             if (built) gel.push_back(e);
         }
         s->g_entries = gtot64 + gtot32;
@@ -1349,6 +1361,7 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st, unsigned long
     um.G = f64 ? (const TG*)(const void*)s->d_G64 : (const TG*)(const void*)s->d_G16;
     auto launch = [&](const Sweep::Shape& sh) {
         um.reg_cap = sh.reg_cap;
+        um.stage_cap = (int)(sh.smem / sizeof(T)) - 2 * rhs_cap;
         sweep_persistent_kernel<T><<<sh.grid, sh.threads, sh.smem, st>>>(
             v, s->d_rec, s->rec_stride, (int)h->host.elems.size(), s->d_active, inv, r, z, s->d_next, s->d_status,
             um, rhs_cap, sh.bcap, trace), count_launch();
@@ -1420,9 +1433,20 @@ void apply_sweep(rtg_handle* h, const T* r, T* z, cudaStream_t st) {
 void sweep_maps(rtg_handle* h, int prec, int* onephase, int64_t* map_entries, int64_t* upwind, cudaStream_t st) {
     Sweep* s = get_sweep(h, st);
     const int p = prec == RTG_FP64 ? 1 : 0;
-    if (onephase) *onephase = p ? s->n_onephase64 : s->n_onephase32;
-    if (map_entries) *map_entries = s->g_read[p];
-    if (upwind) *upwind = s->up_read[p];
+    // the maps the chosen launch shape reads (every element with a map before
+    // the first sweep has chosen one)
+    const int64_t cap = s->pick[p] >= 0 ? s->shape[p][s->pick[p]].reg_cap : std::numeric_limits<int64_t>::max();
+    int n = 0;
+    int64_t ent = 0, nup = 0;
+    for (const Sweep::MapUse& u : s->onephase[p])
+        if (u.region <= cap) {
+            ++n;
+            ent += u.entries;
+            nup += u.nup;
+        }
+    if (onephase) *onephase = n;
+    if (map_entries) *map_entries = ent;
+    if (upwind) *upwind = nup;
 }
 
 // level of each element in the sweep order (host array of nelem)
