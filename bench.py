@@ -661,9 +661,10 @@ def run_ours(args):
                      "frac_of_traffic": (sweep_traffic / t_sweep / 1e9 / peak) if sweep_traffic else None,
                      "kernel": "sweep_persistent_kernel<float>", "bytes_per_launch": sb, "launch_s": t_sweep,
                      "peak_kind": peak_kind,
-                     "note": "bytes_per_launch counts every element's reads of its block inverse and map; "
-                             "elements with identical blocks share them, so the DRAM traffic (ncu) is lower and "
-                             "part of the bytes come from L2; {} wavefront levels, {:.2f} us per level".format(
+                     "note": "bytes_per_launch counts every element's reads of its block inverse and of the "
+                             "map it uses (one-phase elements); elements with identical blocks share them, so the "
+                             "DRAM traffic (ncu) is lower and part of the bytes come from L2; {} wavefront levels, "
+                             "{:.2f} us per level".format(
                                  nlev, 1e6 * t_sweep / max(nlev, 1))},
         "apply_roofline": {"bound": "hbm", "achieved": bytes_apply / t_apply / 1e9, "peak": peak, "unit": "GB/s",
                            "frac": bytes_apply / t_apply / 1e9 / peak, "kernel": "apply_tiled_kernel (FP32 system)",
