@@ -229,7 +229,8 @@ constexpr int kRecHead = 25;
 // staging offset, coupling index, (unused); then the face nodes (ascending ij)
 constexpr int kRecCpl = 12;
 constexpr int kCplF = 0, kCplM1 = 1, kCplNt1 = 2, kCplN0 = 3, kCplStr = 4, kCplEs = 5, kCplEt = 6, kCplBase = 7,
-              kCplOff = 9, kCplK = 10;
+              kCplOff = 9, kCplK = 10,
+              kCplDiag = 11;   // bit 0: Es diagonal, bit 1: Et diagonal (off-diagonal entries below 1e-13 of the largest)
 constexpr int kRecMax = kRecHead + kRecCpl * kMaxCplStaged + kMaxFaceNodes;
 
 __device__ __forceinline__ int64_t rec64(const int* w) {
@@ -717,13 +718,19 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
                     }
                     if (c >= ncs) break;
                     const int* cp = s_cpl + kRecCpl * c;
+                    const int dg = cp[kCplDiag];
+                    if (dg == 3) continue;   // Es and Et diagonal: the face phase reads the line itself
                     const int m1 = cp[kCplM1], nt1 = cp[kCplNt1];
                     const T* Et = cs + cp[kCplOff] + m1 * cp[kCplN0];
                     const T* zl = Et + nt1 * nth;
                     T* Tm = cs + cp[kCplOff] + m1 * cp[kCplN0] + nt1 * nth + m1 * nt1;
                     const int q = t - base, jj = q / nth, r = q % nth;
                     T acc = T(0);
-                    for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
+                    if (dg & 2) {
+                        acc = Et[r * nth + r] * zl[jj * nt1 + r];
+                    } else {
+                        for (int a = 0; a < nt1; ++a) acc += Et[a * nth + r] * zl[jj * nt1 + a];
+                    }
                     Tm[jj * nth + r] = acc;
                 }
             }
@@ -736,12 +743,20 @@ sweep_persistent_kernel(OpView<T> v, const int32_t* __restrict__ rec, int rstrid
                     const int* cp = s_cpl + kRecCpl * c;
                     const int F = cp[kCplF];
                     if (!on_face(F, i, j, nx, ny)) continue;
-                    const int m1 = cp[kCplM1], n0 = cp[kCplN0];
+                    const int m1 = cp[kCplM1], n0 = cp[kCplN0], nt1 = cp[kCplNt1], dg = cp[kCplDiag];
                     const int qq = (F % 2 == 0) ? j : i;
                     const T* Es = cs + cp[kCplOff];
-                    const T* Tm = Es + m1 * n0 + cp[kCplNt1] * nth + m1 * cp[kCplNt1];
+                    const T* Et = Es + m1 * n0;
+                    const T* zl = Et + nt1 * nth;
+                    const T* Tm = zl + m1 * nt1;
                     T sacc = T(0);
-                    for (int jj = 0; jj < m1; ++jj) sacc += Es[jj * n0 + qq] * Tm[jj * nth + r];
+                    if (dg == 3) {
+                        sacc = Es[qq * n0 + qq] * (Et[r * nth + r] * zl[qq * nt1 + r]);
+                    } else if (dg & 1) {
+                        sacc = Es[qq * n0 + qq] * Tm[qq * nth + r];
+                    } else {
+                        for (int jj = 0; jj < m1; ++jj) sacc += Es[jj * n0 + qq] * Tm[jj * nth + r];
+                    }
                     acc += s_dc[c] * sacc;
                 }
                 rhs[ij * nth + r] = acc;
@@ -1305,6 +1320,8 @@ Sweep* get_sweep(rtg_handle* h, cudaStream_t st) {
                 put64(&w[kCplBase], g.base);
                 w[kCplOff] = soff;
                 w[kCplK] = k;
+                w[kCplDiag] = (g.m1 == n0 && diagonal(cp.es, g.m1, n0) ? 1 : 0) |
+                              (g.nth1 == E.nth && diagonal(cp.et, g.nth1, E.nth) ? 2 : 0);
                 R.insert(R.end(), w, w + kRecCpl);
                 soff += g.m1 * n0 + g.nth1 * E.nth + g.m1 * g.nth1 + g.m1 * E.nth;
             }
